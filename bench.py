@@ -1,0 +1,300 @@
+"""Benchmark: transitions/s of the GPU simulator on one GB300 (and its CPU reference arm).
+
+Default workload: the 1000-node synthetic network (in-degree Poisson(2) capped at 6, 10% constant
+nodes, lognormal(0, 0.5) rates, 10 outputs, 1e6 trajectories, max_time 50, tick 0.5), generated
+from a fixed seed. One step is one full simulation of all trajectories (mbg_sim_run), including
+the clearing of the result buffers and the fixed-point aggregation. The L2 is flushed (256 MiB
+write) between timed steps.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--workload medium|small|large]
+  python bench.py --impl reference ...   # the CPU restatement of the reference path
+
+Under torchrun (WORLD_SIZE > 1) every rank simulates its own range of trajectory ids (weak
+scaling); there is no collective on the data path, only a barrier and a max over ranks of the
+step time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOADS = {
+    "small": "20-node random network, 2-3 regulators per node, all rates 1, all nodes output, istate 0.5, "
+             "1e5 trajectories, max_time 100, tick 1, seed 42",
+    "medium": "1000-node random network, in-degree Poisson(2) capped at 6, 10% constant nodes, rates "
+              "lognormal(0,0.5), 10 outputs, istate 0.5, 1e6 trajectories, max_time 50, tick 0.5",
+    "large": "5000-node random network, power-law in-degree (2.5, 1..20), rates lognormal(0,1), 20 outputs, "
+             "istate 0.3, 2^20 trajectories, max_time 20, tick 0.2",
+}
+CPU_SAMPLE_SECONDS = 15.0
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class Clocks:
+    """Samples nvidia-smi clocks and throttle reasons every 200 ms while running."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in self.lines:
+            f = [x.strip() for x in l.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = max(mx, float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx or None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def load_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except OSError:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "sm_max_mhz": 2070.0}, "fallback"
+
+
+def model_work_per_transition(net, info):
+    """Thread-level operations of one transition of the reference algorithm (every rate
+    re-evaluated, summed and scanned): sum_i c_i + 2N + 4 n_out + 40, where c_i counts one
+    extract per regulator reference, one op per AND/OR/NOT and 2 for the compare and select."""
+    total = 0
+    for f in net.logic:
+        refs = sum(1 for tok in f.replace("(", " ").replace(")", " ").replace("!", " ! ").split()
+                   if tok.startswith("N"))
+        ops = f.count("&") + f.count("|") + f.count("!")
+        total += 2 * refs + ops + 2
+    return total + 2 * info.nodes + 4 * info.outputs + 40
+
+
+def make_network(name):
+    from upmabossg_gb300 import synth
+    return getattr(synth, name)()
+
+
+def cpu_reference(net, bnd, cfg, frac_bits, seconds, threads=0, seed=None):
+    """Times the oracle port (the reference path restated on the CPU) on a bounded sample."""
+    import oracle
+    pilot = oracle.run(bnd, cfg, frac_bits=frac_bits, n_traj=32, threads=threads, seed=seed)
+    per_traj = max(pilot.seconds / 32 * pilot.threads, 1e-6)  # thread-seconds per trajectory
+    ncores = threads or (os.cpu_count() or 1)
+    n = int(max(64, min(net.sample_count, seconds * ncores / per_traj)))
+    r = oracle.run(bnd, cfg, frac_bits=frac_bits, n_traj=n, threads=threads, seed=seed)
+    tps = r.counters["transitions"] / r.seconds
+    return {"value": tps, "unit": "transitions/s", "cores": r.threads, "kind": "port",
+            "sample": f"first {n} of {net.sample_count} trajectories ({r.counters['transitions']} transitions, "
+                      f"{r.seconds:.1f} s)"}
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    import oracle  # noqa: F401
+    net = make_network(args.workload)
+    bnd, cfg = net.bnd(), net.cfg()
+    import upmabossg_gb300 as mbg
+    model = mbg.Model.from_strings(bnd, cfg)  # host-side parse only: the fixed-point scale
+    vals = []
+    last = None
+    for i in range(args.warmup + args.steps):
+        last = cpu_reference(net, bnd, cfg, model.info.frac_bits, args.cpu_seconds / 2)
+        if i >= args.warmup:
+            vals.append(last["value"])
+    value = statistics.mean(vals)
+    line = {"impl": "reference", "metric": "transitions/s", "value": value, "unit": "transitions/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": None,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
+            "data": "synthetic", "config": {"workload": WORKLOADS[args.workload]},
+            "cpu_baseline": dict(last, value=value),
+            "e2e": {"value": value, "unit": "transitions/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args):
+    ws, rank, local = dist_env()
+    import upmabossg_gb300 as mbg
+    if mbg.device_count() < 1:
+        raise SystemExit("bench: no CUDA device")
+    import torch
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    net = make_network(args.workload)
+    n_total = net.sample_count
+    n_rank = n_total // ws
+    base = rank * n_rank
+    bnd, cfg = net.bnd(), net.cfg()
+    model = mbg.Model.from_strings(bnd, cfg)
+    sim = mbg.Simulation(model, n_traj=n_rank, traj_base=base, device=local, layout=args.layout)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{local}")
+
+    def barrier():
+        torch.cuda.synchronize()
+        if ws > 1:
+            torch.distributed.barrier()
+            torch.cuda.synchronize()
+
+    for _ in range(args.warmup):
+        sim.run()
+    kernel_ms, sim_ms, transitions = [], [], []
+    with Clocks(local) as clk:
+        barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            sim.run()
+            s = sim.summary()
+            kernel_ms.append(s["kernel_ms"])
+            sim_ms.append(s["sim_ms"])
+            transitions.append(s["transitions"])
+        barrier()
+        wall = time.perf_counter() - t0
+    step_ms = sum(sim_ms) / len(sim_ms)
+    if ws > 1:
+        t = torch.tensor([step_ms], device=f"cuda:{local}")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        step_ms = float(t.item())
+    trans_step = transitions[-1]
+    value = trans_step * ws / (step_ms * 1e-3)
+    summary = sim.summary()
+
+    # end to end through the public API: parse + create (H2D of the model) + run + results (D2H)
+    e2e_ms = []
+    h2d = d2h = 0
+    for i in range(max(2, args.steps // 2) + 1):
+        t1 = time.perf_counter()
+        m2 = mbg.Model.from_strings(bnd, cfg)
+        s2 = mbg.Simulation(m2, n_traj=n_rank, traj_base=base, device=local, layout=args.layout)
+        s2.run()
+        P, TH = s2.probtraj()
+        F = s2.final_states()
+        fs, fp = s2.fixed_points()
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t1
+        if i > 0:
+            e2e_ms.append(dt * 1e3)
+        # model text in, raw u64 window sums + TH sums + u32 final counts + fixed points out
+        h2d = len(bnd) + len(cfg)
+        d2h = P.size * 8 + TH.size * 8 + F.size * 4 + fs.nbytes + fp.size * 4
+        s2.close()
+        m2.close()
+    e2e_value = trans_step * ws / (statistics.mean(e2e_ms) * 1e-3)
+
+    peaks, peaks_kind = load_peaks()
+    info = model.info
+    w_tr = model_work_per_transition(net, info)
+    sms = 152
+    clock = peaks.get("sm_max_mhz", 2070.0) * 1e6
+    peak_ops = sms * 128 * clock
+    kms = sum(kernel_ms) / len(kernel_ms)
+    achieved = trans_step * w_tr / (kms * 1e-3)
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", f"traffic_{args.workload}.json")
+    if os.path.exists(tpath):
+        with open(tpath) as f:
+            traffic = json.load(f).get("dram_bytes_per_launch")
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu:
+        cpu = cpu_reference(net, bnd, cfg, info.frac_bits, args.cpu_seconds)
+    clocks = clk.summary()
+    line = {
+        "metric": "transitions/s", "value": value, "unit": "transitions/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u64", "data": "synthetic",
+        "config": {"workload": WORKLOADS[args.workload], "trajectories": n_total,
+                   "transitions_per_step": trans_step * ws, "layout": ["", "thread", "warp"][summary["layout"]],
+                   "l2": "flushed between steps (256 MiB write)", "wall_s": wall},
+        "e2e": {"value": e2e_value, "unit": "transitions/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h, "ms_per_step": statistics.mean(e2e_ms),
+                "path": "mbg_model_parse_strings + mbg_sim_create + mbg_sim_run + probtraj/final/fixed-point reads"},
+        "gpu_launches": 3 * args.steps,
+        "roofline": {"bound": "issue", "achieved": achieved / 1e9, "peak": peak_ops / 1e9, "unit": "Gop/s",
+                     "frac": achieved / peak_ops, "traffic": traffic,
+                     "kernel_ms": kms, "ops_per_transition": w_tr,
+                     "peak_source": f"152 SMs x 128 lanes x {clock / 1e6:.0f} MHz ({peaks_kind} sm_max_mhz)"},
+        "cpu_baseline": cpu,
+        "clocks": clocks,
+        "summary": {k: summary[k] for k in ("transitions", "fixed_points", "finished", "errors", "fixed_point_states")},
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="medium", choices=sorted(WORKLOADS))
+    ap.add_argument("--layout", type=int, default=0)
+    ap.add_argument("--cpu-seconds", type=float, default=CPU_SAMPLE_SECONDS)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,142 @@
+/* MaBoSS-style continuous-time Boolean network simulator for one NVIDIA GB300 (sm_103a).
+ *
+ * C ABI of libmbg.so: plain pointers and sizes, status codes, caller-owned handles. The
+ * `MaBoSSG` command line is a thin client of this interface. Reference interfaces replaced
+ * (paths inside DominicJW/UPMaBoSSG):
+ *
+ *   mbg_model_parse_files / _strings  driver::parse, src/parser/driver.cpp:16-31 (+ parse_one 33-43)
+ *   mbg_model_info                    main.cpp:128-152 (cfg constants, output mask and limits)
+ *   mbg_sim_create                    kernel_compiler::compile_simulation, src/kernel_compiler.cpp:61-164,
+ *                                     simulation_runner ctor, src/simulation_runner.cu:42-52, and the
+ *                                     stats constructors, main.cpp:60-74
+ *   mbg_sim_run                       simulation_runner::run_simulation, src/simulation_runner.cu:54-180,
+ *                                     and stats_composite::finalize, src/statistics/stats_composite.cpp:14
+ *   mbg_sim_probtraj                  window_average_small_stats::finalize + get_single_result_prob,
+ *                                     src/statistics/window_average_small.cpp:91-140
+ *   mbg_sim_final_states              final_states_stats::finalize, src/statistics/final_states.cpp:45-51
+ *   mbg_sim_fixed_points              fixed_states_stats result map, src/statistics/fixed_states.cu:118-124
+ *   mbg_write_probtraj_csv            window_average_small_stats::write_csv, window_average_small.cpp:181-250
+ *   mbg_write_fp_csv                  fixed_states_stats::write_csv, src/statistics/fixed_states.cu:154-187
+ *   mbg_print_results                 stats_composite::visualize (final, fixed, window order of main.cpp:65-74)
+ *
+ * Every call returns a status; nothing exits or traps. Handles are not thread safe; distinct
+ * handles may be used from distinct threads. Each simulation handle uses one device and the
+ * stream passed to mbg_sim_run.
+ */
+#ifndef MBG_H
+#define MBG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    MBG_OK = 0,
+    MBG_ERR_ARG = 1,      /* invalid argument */
+    MBG_ERR_IO = 2,       /* file cannot be read or written */
+    MBG_ERR_PARSE = 3,    /* .bnd / .cfg syntax or semantic error */
+    MBG_ERR_MODEL = 4,    /* model outside the supported limits */
+    MBG_ERR_CUDA = 5,     /* CUDA runtime error or no device */
+    MBG_ERR_JIT = 6,      /* NVRTC compilation failed */
+    MBG_ERR_NOMEM = 7,    /* device or host allocation failed */
+    MBG_ERR_DEVICE = 8,   /* a kernel reported an error flag */
+    MBG_ERR_STATE = 9     /* call out of order (e.g. results before run) */
+} mbg_status;
+
+typedef struct mbg_model mbg_model;
+typedef struct mbg_sim mbg_sim;
+
+typedef struct {
+    int32_t nodes;          /* N */
+    int32_t words;          /* ceil(N / 32) state words */
+    int32_t outputs;        /* non-internal nodes */
+    int32_t windows;        /* ceil(max_time / time_tick) */
+    int32_t discrete_time;  /* cfg discrete_time != 0 */
+    int32_t frac_bits;      /* fixed-point fraction bits of the rates */
+    int32_t max_regulators; /* largest number of nodes a rate reads */
+    int32_t palette_nodes;  /* nodes with multi-valued rates */
+    double max_time, time_tick;
+    uint64_t sample_count, seed;
+} mbg_model_info;
+
+/* Trajectory layout: 0 auto (autotuned cutoff), 1 thread per trajectory (NVRTC-compiled
+ * evaluator), 2 warp per trajectory (table driven). */
+enum { MBG_LAYOUT_AUTO = 0, MBG_LAYOUT_THREAD = 1, MBG_LAYOUT_WARP = 2 };
+
+typedef struct {
+    uint64_t n_traj;           /* 0: cfg sample_count */
+    uint64_t traj_base;        /* id of the first trajectory (Philox stream) */
+    uint64_t seed;             /* used when use_cfg_seed == 0 */
+    int32_t use_cfg_seed;      /* 1: cfg seed_pseudorandom (default) */
+    int32_t layout;            /* MBG_LAYOUT_* */
+    int32_t record_trajectories; /* keep per-trajectory end state, time, transitions, status */
+    int32_t device;            /* CUDA device ordinal */
+    uint32_t max_steps;        /* per-trajectory step cap; 0: none */
+    int32_t block_size;        /* threads per block; 0: default */
+    int32_t blocks_per_sm;     /* 0: occupancy limit */
+    int32_t thread_cutoff;     /* AUTO: largest N run thread per trajectory; 0: default */
+} mbg_sim_opts;
+
+typedef struct {
+    uint64_t trajectories;     /* trajectories simulated */
+    uint64_t transitions;      /* accepted flips (time < max_time) */
+    uint64_t steps;            /* loop iterations, including terminal ones */
+    uint64_t finished, fixed_points, step_limited, errors;
+    uint64_t fixed_point_states; /* distinct fixed states */
+    uint32_t device_error;     /* device error bits */
+    int32_t layout;            /* layout that ran */
+    double sim_ms;             /* device time of the last mbg_sim_run (CUDA events) */
+    double kernel_ms;          /* device time of its simulation kernel alone */
+    double jit_ms;             /* NVRTC compile time at create (0 if cached) */
+} mbg_run_summary;
+
+const char* mbg_last_error(void);
+const char* mbg_version(void);
+int mbg_device_count(void);
+
+mbg_status mbg_model_parse_files(const char* bnd_path, const char* cfg_path, mbg_model** out);
+mbg_status mbg_model_parse_strings(const char* bnd_text, const char* cfg_text, mbg_model** out);
+void mbg_model_destroy(mbg_model* m);
+mbg_status mbg_model_info_get(const mbg_model* m, mbg_model_info* out);
+const char* mbg_model_node_name(const mbg_model* m, int32_t i);
+/* Output node indices (node order), `cap` entries at most; returns the count. */
+int32_t mbg_model_outputs(const mbg_model* m, int32_t* idx, int32_t cap);
+
+/* Generates the model's thread-per-trajectory kernel and compiles it with NVRTC for sm_103a
+ * without loading it (needs no GPU). */
+mbg_status mbg_model_jit_check(const mbg_model* m, double* compile_ms);
+
+void mbg_sim_opts_default(mbg_sim_opts* o);
+mbg_status mbg_sim_create(const mbg_model* m, const mbg_sim_opts* o, mbg_sim** out);
+void mbg_sim_destroy(mbg_sim* s);
+/* Runs all trajectories on `stream` (a cudaStream_t, NULL for the legacy stream) and waits. */
+mbg_status mbg_sim_run(mbg_sim* s, void* stream);
+mbg_status mbg_sim_summary(const mbg_sim* s, mbg_run_summary* out);
+/* windows x 2^outputs probabilities and the per-window transition entropy, as the reference
+ * reports them (time share / (n x tick), or count / n in discrete time). */
+mbg_status mbg_sim_probtraj(mbg_sim* s, double* probs, double* tr_entropy);
+/* Raw fixed-point sums: windows x 2^outputs (time x 2^32, or counts) and windows TH sums. */
+mbg_status mbg_sim_probtraj_raw(mbg_sim* s, uint64_t* sums, uint64_t* th_sums);
+/* 2^outputs final-state probabilities. */
+mbg_status mbg_sim_final_states(mbg_sim* s, double* probs);
+/* Distinct fixed points in reference order (highest state word first): states (n x words),
+ * probabilities; `cap` entries at most, `*count` gets the total. */
+mbg_status mbg_sim_fixed_points(mbg_sim* s, uint32_t* states, double* probs, size_t cap, size_t* count);
+/* Per-trajectory end records (record_trajectories): n_traj x words states, end times,
+ * transitions and statuses (1 finished, 2 fixed point, 3 step limit, 4 error). */
+mbg_status mbg_sim_trajectories(mbg_sim* s, uint32_t* states, double* times, uint32_t* transitions,
+                                uint8_t* status);
+
+mbg_status mbg_write_probtraj_csv(mbg_sim* s, const char* prefix);
+mbg_status mbg_write_fp_csv(mbg_sim* s, const char* prefix);
+/* The reference's stdout report (final points, fixed points, windows) to a file path or "-". */
+mbg_status mbg_print_results(mbg_sim* s, const char* path);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MBG_H */

@@ -1,0 +1,89 @@
+"""Shared helpers of the test suite: device runs, oracle runs and their comparison."""
+from __future__ import annotations
+
+import json
+import os
+
+import numpy as np
+
+import oracle
+import upmabossg_gb300 as mbg
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+TWO32 = 4294967296.0
+
+
+def golden_model(name):
+    with open(os.path.join(GOLDEN, "models", name + ".bnd")) as f:
+        bnd = f.read()
+    with open(os.path.join(GOLDEN, "models", name + ".cfg")) as f:
+        cfg = f.read()
+    return bnd, cfg
+
+
+def golden_result(name):
+    with open(os.path.join(GOLDEN, name + ".json")) as f:
+        return json.load(f)
+
+
+def run_device(bnd, cfg, n_traj, layout=mbg.LAYOUT_AUTO, seed=None, record=True, **kw):
+    model = mbg.Model.from_strings(bnd, cfg)
+    sim = mbg.Simulation(model, n_traj=n_traj, layout=layout, seed=seed, record_trajectories=record, **kw)
+    sim.run()
+    return model, sim
+
+
+def run_oracle(bnd, cfg, model, n_traj, seed=None, **kw):
+    return oracle.run(bnd, cfg, frac_bits=model.info.frac_bits, n_traj=n_traj, seed=seed,
+                      keep_trajectories=True, **kw)
+
+
+def compare_trajectories(sim, orc, max_tie_frac=0.01):
+    """Per-trajectory parity: states, statuses and transition counts bit-exact, end times within
+    1e-5 relative, for every trajectory the oracle does not flag as a tie. Returns the tie count."""
+    st, t, tr, status = sim.trajectories()
+    ties = orc.ties != 0
+    n_ties = int(ties.sum())
+    assert n_ties <= max(1, max_tie_frac * len(ties)), f"{n_ties} ties in {len(ties)} trajectories"
+    ok = ~ties
+    bad = np.nonzero(ok & (status != orc.status))[0]
+    assert bad.size == 0, f"status differs for trajectories {bad[:10]}: dev {status[bad[:10]]} orc {orc.status[bad[:10]]}"
+    bad = np.nonzero(ok & (tr != orc.transitions))[0]
+    assert bad.size == 0, f"transitions differ for {bad[:10]}: dev {tr[bad[:10]]} orc {orc.transitions[bad[:10]]}"
+    bad = np.nonzero(ok & np.any(st != orc.states, axis=1))[0]
+    assert bad.size == 0, f"end states differ for trajectories {bad[:10]}"
+    rel = np.abs(t - orc.times) / np.maximum(np.abs(orc.times), 1e-30)
+    assert float(rel[ok].max(initial=0)) <= 1e-5, f"end times differ: max rel {rel[ok].max()}"
+    return n_ties
+
+
+def compare_histograms(model, sim, orc, n_traj):
+    """Window sums within 1e-5 x n x tick (time units), TH within 1e-4 relative, final states
+    and fixed points exact up to tied trajectories."""
+    info = model.info
+    raw, th_raw = sim.probtraj_raw()
+    dev = raw.astype(np.float64) / (1.0 if info.discrete_time else TWO32)
+    ref = orc.dense_hist()
+    scale = n_traj * (1.0 if info.discrete_time else info.time_tick)
+    n_ties = int((orc.ties != 0).sum())
+    tol = 1e-5 * scale + (n_ties + 1) * (1.0 if info.discrete_time else info.time_tick) * 1.01
+    err = np.abs(dev - ref).max()
+    assert err <= tol, f"window sums differ by {err} (tol {tol})"
+    th_dev = th_raw.astype(np.float64) / TWO32
+    th_err = np.abs(th_dev - orc.th)
+    assert np.all(th_err <= 1e-4 * np.abs(orc.th) + 1e-4 * scale + n_ties * scale / n_traj * 5), \
+        f"TH sums differ: max {th_err.max()}"
+    fin = np.rint(sim.final_states() * n_traj)
+    assert np.abs(fin - orc.final).sum() <= 2 * n_ties, "final-state histograms differ"
+    fp_states, fp_probs = sim.fixed_points()
+    ofix = orc.states[orc.status == 2]
+    if ofix.size:
+        uo, co = np.unique(ofix, axis=0, return_counts=True)
+    else:
+        uo, co = np.zeros((0, info.words), np.uint32), np.zeros(0, np.int64)
+    if n_ties == 0:
+        assert len(fp_states) == len(uo), f"{len(fp_states)} fixed points on the device, {len(uo)} in the oracle"
+        dev_map = {tuple(s): int(round(p * n_traj)) for s, p in zip(fp_states, fp_probs)}
+        orc_map = {tuple(s): int(c) for s, c in zip(uo, co)}
+        assert dev_map == orc_map, "fixed points differ"
+    return err

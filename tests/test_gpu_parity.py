@@ -1,0 +1,123 @@
+"""GPU path versus the host FP64 oracle on the same Philox streams, through the C ABI.
+
+Per trajectory: end state words, status and number of transitions bit-exact, end time within
+1e-5 relative; trajectories the oracle flags as ties (an FP32 dt landing within 1e-6 of max_time,
+or an FP64 pick that differs from the exact fixed-point pick) are counted and excluded.
+Aggregates: window sums within 1e-5 x n x tick, TH within 1e-4 relative, final states and fixed
+points exact.
+"""
+import numpy as np
+import pytest
+
+import upmabossg_gb300 as mbg
+from upmabossg_gb300 import synth
+
+from helpers import compare_histograms, compare_trajectories, golden_model, run_device, run_oracle
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("layout", [mbg.LAYOUT_THREAD, mbg.LAYOUT_WARP])
+def test_small_network_parity(layout):
+    net = synth.small()
+    bnd, cfg = net.bnd(), net.cfg()
+    n = 4000
+    model, sim = run_device(bnd, cfg, n, layout=layout)
+    orc = run_oracle(bnd, cfg, model, n)
+    s = sim.summary()
+    assert s["layout"] == layout
+    assert s["transitions"] == orc.counters["transitions"] or orc.counters["time_ties"] > 0
+    compare_trajectories(sim, orc)
+    compare_histograms(model, sim, orc, n)
+
+
+def test_medium_network_parity():
+    net = synth.medium()
+    bnd, cfg = net.bnd(), net.cfg(sample_count=192)
+    model, sim = run_device(bnd, cfg, 192, layout=mbg.LAYOUT_WARP)
+    orc = run_oracle(bnd, cfg, model, 192)
+    compare_trajectories(sim, orc)
+    compare_histograms(model, sim, orc, 192)
+
+
+@pytest.mark.parametrize("layout", [mbg.LAYOUT_THREAD, mbg.LAYOUT_WARP])
+def test_mid_network_parity(layout):
+    net = synth.sweep_instance(2)  # 268 nodes, 8 outputs, lognormal rates
+    bnd, cfg = net.bnd(), net.cfg(sample_count=400)
+    model, sim = run_device(bnd, cfg, 400, layout=layout)
+    orc = run_oracle(bnd, cfg, model, 400)
+    compare_trajectories(sim, orc)
+    compare_histograms(model, sim, orc, 400)
+
+
+def test_large_network_parity():
+    net = synth.large()
+    bnd, cfg = net.bnd(), net.cfg(sample_count=24, max_time=5)
+    model, sim = run_device(bnd, cfg, 24, layout=mbg.LAYOUT_WARP)
+    orc = run_oracle(bnd, cfg, model, 24)
+    compare_trajectories(sim, orc)
+    compare_histograms(model, sim, orc, 24)
+
+
+@pytest.mark.parametrize("name,n", [("cellcycle", 3000), ("metastasis", 300), ("sizek", 300), ("montagud", 200)])
+def test_reference_models_parity(name, n):
+    bnd, cfg = golden_model(name)
+    model, sim = run_device(bnd, cfg, n)
+    orc = run_oracle(bnd, cfg, model, n)
+    compare_trajectories(sim, orc)
+    compare_histograms(model, sim, orc, n)
+
+
+def test_thread_and_warp_layouts_agree():
+    """Both layouts run the same integer arithmetic and the same clock: identical window sums,
+    final states and fixed points."""
+    net = synth.sweep_instance(2)
+    bnd, cfg = net.bnd(), net.cfg(sample_count=3000)
+    _, a = run_device(bnd, cfg, 3000, layout=mbg.LAYOUT_THREAD, record=False)
+    _, b = run_device(bnd, cfg, 3000, layout=mbg.LAYOUT_WARP, record=False)
+    ra, _ = a.probtraj_raw()
+    rb, _ = b.probtraj_raw()
+    assert np.array_equal(ra, rb)
+    assert np.array_equal(a.final_states(), b.final_states())
+    fa, pa = a.fixed_points()
+    fb, pb = b.fixed_points()
+    assert np.array_equal(fa, fb) and np.array_equal(pa, pb)
+    assert a.summary()["transitions"] == b.summary()["transitions"]
+
+
+def test_run_is_deterministic():
+    net = synth.medium()
+    bnd, cfg = net.bnd(), net.cfg(sample_count=2000)
+    model, sim = run_device(bnd, cfg, 2000, record=False)
+    r1, t1 = sim.probtraj_raw()
+    s1 = sim.summary()
+    sim.run()
+    r2, t2 = sim.probtraj_raw()
+    assert np.array_equal(r1, r2) and np.array_equal(t1, t2)
+    assert sim.summary()["transitions"] == s1["transitions"]
+
+
+def test_trajectory_ids_are_partition_independent():
+    """Philox is keyed by trajectory id: two runs over [0, n/2) and [n/2, n) equal one run."""
+    net = synth.small()
+    bnd, cfg = net.bnd(), net.cfg()
+    _, full = run_device(bnd, cfg, 1000, record=False)
+    _, lo = run_device(bnd, cfg, 500, record=False)
+    _, hi = run_device(bnd, cfg, 500, record=False, traj_base=500)
+    a, _ = full.probtraj_raw()
+    b, _ = lo.probtraj_raw()
+    c, _ = hi.probtraj_raw()
+    assert np.array_equal(a, b + c)
+
+
+def test_step_limit_is_counted():
+    net = synth.medium()
+    bnd, cfg = net.bnd(), net.cfg(sample_count=64)
+    model, sim = run_device(bnd, cfg, 64, max_steps=50)
+    s = sim.summary()
+    assert s["step_limited"] > 0
+    assert s["step_limited"] + s["finished"] + s["fixed_points"] == 64
+    st, t, tr, status = sim.trajectories()
+    assert np.all(tr[status == 3] == 50)
+    orc = run_oracle(bnd, cfg, model, 64, max_steps=50)
+    assert np.array_equal(status, orc.status)

@@ -1,0 +1,19 @@
+// Host-callable launchers of the ahead-of-time kernels (sim_aot.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "sim_types.h"
+
+namespace mbg {
+
+cudaError_t launch_sim_warp(const SimParams& p, int grid, int block, size_t smem, cudaStream_t stream);
+cudaError_t sim_warp_configure(size_t smem);
+unsigned sim_warp_smem_per_warp(int n);
+cudaError_t sim_warp_occupancy(int block, size_t smem, int* blocks_per_sm);
+cudaError_t launch_fp_aggregate(const unsigned* fp_states, const unsigned* fp_count, unsigned capacity, int words,
+                                unsigned* slot_rep, unsigned* slot_cnt, unsigned n_slots, unsigned* out_states,
+                                unsigned* out_cnt, unsigned* n_unique, unsigned* error_flag, int sms,
+                                cudaStream_t stream);
+
+}  // namespace mbg

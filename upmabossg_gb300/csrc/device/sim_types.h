@@ -1,0 +1,80 @@
+// Plain data shared by the host library, the AOT kernels and the NVRTC-compiled kernels.
+// Includes nothing so that it can be pasted into an NVRTC program as is.
+#pragma once
+
+namespace mbg {
+
+// Trajectory end states. The first three match src/trajectory_status.h:3-8.
+enum TrajStatus : unsigned char {
+    TRAJ_CONTINUE = 0,
+    TRAJ_FINISHED = 1,
+    TRAJ_FIXED_POINT = 2,
+    TRAJ_STEP_LIMIT = 3,  // hit the per-trajectory step cap
+    TRAJ_ERROR = 4,       // a device-side consistency check failed
+};
+
+// Device error bits (SimParams::error_flag).
+enum DevError : unsigned int {
+    DEV_ERR_PICK = 1u,         // no node satisfied the prefix test
+    DEV_ERR_FP_OVERFLOW = 2u,  // fixed-point buffer full
+    DEV_ERR_SMEM = 4u,         // launch shape does not match the model
+};
+
+// Indices into SimParams::counters.
+enum Counter {
+    CNT_WORK = 0,         // next trajectory to start (work queue)
+    CNT_TRANSITIONS = 1,  // accepted transitions
+    CNT_FINISHED = 2,
+    CNT_FIXED = 3,
+    CNT_STEP_LIMIT = 4,
+    CNT_ERROR = 5,
+    CNT_STEPS = 6,        // loop iterations (transitions + terminal steps)
+    CNT_COUNT = 8,
+};
+
+// One node of the compiled model, 32 bytes.
+struct DevNode {
+    unsigned int tab_off;  // BINARY: word offset into tabs; PALETTE: byte offset into pidx
+    unsigned int reg_off;  // offset into regs
+    unsigned short k;      // number of regulators (the node itself excluded)
+    unsigned short kind;   // 0 binary, 1 palette
+    unsigned int pal_off;  // PALETTE: offset into palette
+    unsigned long long up, down;  // BINARY fixed-point rates
+};
+
+struct SimParams {
+    // model
+    const DevNode* nodes;
+    const unsigned short* regs;
+    const unsigned int* tabs;
+    const unsigned char* pidx;
+    const unsigned long long* palette;
+    const unsigned int* dep_off;  // n + 1
+    const unsigned short* deps;
+    const unsigned short* out_nodes;  // n_out
+    const short* out_pos;             // n: position among outputs or -1
+    const unsigned int* istate_thr;   // n
+    int n, words, n_out, windows;
+    int frac_bits, discrete;
+    double max_time, tick;
+    float to_real;  // 2^-frac_bits
+    unsigned int max_steps;
+    unsigned long long seed;
+    unsigned long long n_traj;       // trajectories of this launch
+    unsigned long long traj_base;    // id of the first trajectory (Philox key part)
+    // results
+    unsigned long long* hist;        // windows x 2^n_out, time x 2^32 (counts if discrete)
+    unsigned long long* th_hist;     // windows, TH x time x 2^32 (TH x 2^32 if discrete)
+    unsigned int* final_hist;        // 2^n_out
+    unsigned int* fp_states;         // fp_capacity x words
+    unsigned int* fp_count;
+    unsigned int fp_capacity;
+    unsigned int* traj_state;        // optional, n_traj x words
+    double* traj_time;               // optional
+    unsigned int* traj_transitions;  // optional
+    unsigned char* traj_status;      // optional
+    unsigned long long* counters;    // CNT_COUNT
+    unsigned int* error_flag;
+};
+
+}  // namespace mbg

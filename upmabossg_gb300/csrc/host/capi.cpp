@@ -1,0 +1,289 @@
+// extern "C" surface of libmbg (declared in include/mbg.h). Every entry point catches, maps the
+// error to an mbg_status and keeps the message for mbg_last_error(); nothing exits. The
+// reference instead prints and calls exit() on any CUDA, NVRTC or parse error
+// (src/utils.cpp:3-30, src/kernel_compiler.cpp:10-31, src/parser/driver.cpp:54-60).
+#include <cuda_runtime.h>
+
+#include <cstring>
+#include <fstream>
+#include <iostream>
+#include <memory>
+
+#include "sim.hpp"
+
+struct mbg_model {
+    mbg::Model model;
+    mbg::CompiledModel cm;
+    std::vector<std::string> names;
+};
+
+struct mbg_sim {
+    mbg::Sim sim;
+};
+
+namespace {
+
+thread_local std::string g_err;
+
+mbg_status fail(mbg_status st, const std::string& msg) {
+    g_err = msg;
+    return st;
+}
+
+template <class F>
+mbg_status guard(F&& f) {
+    try {
+        f();
+        g_err.clear();
+        return MBG_OK;
+    } catch (const mbg::ArgError& e) {
+        return fail(MBG_ERR_ARG, e.what());
+    } catch (const mbg::IoError& e) {
+        return fail(MBG_ERR_IO, e.what());
+    } catch (const mbg::ModelError& e) {
+        return fail(MBG_ERR_MODEL, e.what());
+    } catch (const mbg::NoMemError& e) {
+        return fail(MBG_ERR_NOMEM, e.what());
+    } catch (const mbg::DeviceError& e) {
+        return fail(MBG_ERR_DEVICE, e.what());
+    } catch (const mbg::StateError& e) {
+        return fail(MBG_ERR_STATE, e.what());
+    } catch (const mbg::CudaError& e) {
+        return fail(MBG_ERR_CUDA, e.what());
+    } catch (const mbg::JitError& e) {
+        return fail(MBG_ERR_JIT, e.what());
+    } catch (const mbg::Error& e) {
+        return fail(MBG_ERR_PARSE, e.what());
+    } catch (const std::bad_alloc&) {
+        return fail(MBG_ERR_NOMEM, "host allocation failed");
+    } catch (const std::exception& e) {
+        return fail(MBG_ERR_ARG, e.what());
+    }
+}
+
+mbg_status build_model(const std::string& bnd, const std::string& cfg, const std::string& bnd_name,
+                       const std::string& cfg_name, mbg_model** out) {
+    if (!out) return fail(MBG_ERR_ARG, "null output pointer");
+    *out = nullptr;
+    std::unique_ptr<mbg_model> m(new mbg_model());
+    mbg_status st = guard([&] {
+        mbg::parse_bnd(m->model, bnd, bnd_name);
+        mbg::parse_cfg(m->model, cfg, cfg_name);
+    });
+    if (st != MBG_OK) return st;
+    st = guard([&] {
+        try {
+            m->cm = mbg::compile_model(m->model);
+        } catch (const mbg::Error& e) {
+            throw mbg::ModelError(e.what());
+        }
+        for (auto& n : m->model.nodes) m->names.push_back(n.name);
+    });
+    if (st != MBG_OK) return st;
+    *out = m.release();
+    return MBG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* mbg_last_error(void) { return g_err.c_str(); }
+
+const char* mbg_version(void) { return "mbg-gb300 0.1 (sm_103a)"; }
+
+int mbg_device_count(void) {
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return n;
+}
+
+mbg_status mbg_model_parse_files(const char* bnd_path, const char* cfg_path, mbg_model** out) {
+    if (!bnd_path || !cfg_path) return fail(MBG_ERR_ARG, "null path");
+    std::string bnd, cfg;
+    try {
+        bnd = mbg::read_file(bnd_path);
+        cfg = mbg::read_file(cfg_path);
+    } catch (const std::exception& e) {
+        return fail(MBG_ERR_IO, e.what());
+    }
+    return build_model(bnd, cfg, bnd_path, cfg_path, out);
+}
+
+mbg_status mbg_model_parse_strings(const char* bnd_text, const char* cfg_text, mbg_model** out) {
+    if (!bnd_text || !cfg_text) return fail(MBG_ERR_ARG, "null text");
+    return build_model(bnd_text, cfg_text, "<bnd>", "<cfg>", out);
+}
+
+void mbg_model_destroy(mbg_model* m) { delete m; }
+
+mbg_status mbg_model_info_get(const mbg_model* m, mbg_model_info* out) {
+    if (!m || !out) return fail(MBG_ERR_ARG, "null argument");
+    const mbg::CompiledModel& cm = m->cm;
+    std::memset(out, 0, sizeof *out);
+    out->nodes = cm.n;
+    out->words = cm.words;
+    out->outputs = cm.n_out;
+    out->windows = cm.windows;
+    out->discrete_time = cm.discrete ? 1 : 0;
+    out->frac_bits = cm.frac_bits;
+    out->max_regulators = cm.max_k;
+    for (auto& n : cm.nodes) out->palette_nodes += n.kind == mbg::NODE_PALETTE;
+    out->max_time = cm.max_time;
+    out->time_tick = cm.tick;
+    out->sample_count = cm.sample_count;
+    out->seed = cm.seed;
+    return MBG_OK;
+}
+
+const char* mbg_model_node_name(const mbg_model* m, int32_t i) {
+    if (!m || i < 0 || i >= (int32_t)m->names.size()) return nullptr;
+    return m->names[i].c_str();
+}
+
+int32_t mbg_model_outputs(const mbg_model* m, int32_t* idx, int32_t cap) {
+    if (!m) return -1;
+    int32_t n = (int32_t)m->cm.out_nodes.size();
+    for (int32_t i = 0; i < n && i < cap && idx; ++i) idx[i] = m->cm.out_nodes[i];
+    return n;
+}
+
+mbg_status mbg_model_jit_check(const mbg_model* m, double* compile_ms) {
+    if (!m) return fail(MBG_ERR_ARG, "null model");
+    return guard([&] {
+        if (m->cm.words > 16) throw mbg::ModelError("thread layout supports at most 512 nodes");
+        double ms = mbg::jit_compile_only(mbg::generate_thread_model(m->cm, mbg::layout_model(m->cm)));
+        if (compile_ms) *compile_ms = ms;
+    });
+}
+
+void mbg_sim_opts_default(mbg_sim_opts* o) {
+    if (!o) return;
+    std::memset(o, 0, sizeof *o);
+    o->use_cfg_seed = 1;
+    o->layout = MBG_LAYOUT_AUTO;
+}
+
+mbg_status mbg_sim_create(const mbg_model* m, const mbg_sim_opts* o, mbg_sim** out) {
+    if (!m || !out) return fail(MBG_ERR_ARG, "null argument");
+    *out = nullptr;
+    mbg_sim_opts opts;
+    if (o) opts = *o;
+    else mbg_sim_opts_default(&opts);
+    std::unique_ptr<mbg_sim> s(new mbg_sim());
+    mbg_status st = guard([&] { s->sim.create(m->cm, m->names, opts); });
+    if (st != MBG_OK) return st;
+    *out = s.release();
+    return MBG_OK;
+}
+
+void mbg_sim_destroy(mbg_sim* s) { delete s; }
+
+mbg_status mbg_sim_run(mbg_sim* s, void* stream) {
+    if (!s) return fail(MBG_ERR_ARG, "null simulation");
+    return guard([&] { s->sim.run(static_cast<cudaStream_t>(stream)); });
+}
+
+mbg_status mbg_sim_summary(const mbg_sim* s, mbg_run_summary* out) {
+    if (!s || !out) return fail(MBG_ERR_ARG, "null argument");
+    if (!s->sim.ran) return fail(MBG_ERR_STATE, "summary requested before mbg_sim_run");
+    *out = s->sim.summary;
+    return MBG_OK;
+}
+
+mbg_status mbg_sim_probtraj(mbg_sim* s, double* probs, double* tr_entropy) {
+    if (!s) return fail(MBG_ERR_ARG, "null simulation");
+    return guard([&] {
+        s->sim.fetch();
+        const size_t n = s->sim.hist.size();
+        if (probs)
+            for (size_t i = 0; i < n; ++i) probs[i] = mbg::window_prob(s->sim, i);
+        if (tr_entropy)
+            for (int w = 0; w < s->sim.cm.windows; ++w) tr_entropy[w] = mbg::window_th(s->sim, w);
+    });
+}
+
+mbg_status mbg_sim_probtraj_raw(mbg_sim* s, uint64_t* sums, uint64_t* th_sums) {
+    if (!s) return fail(MBG_ERR_ARG, "null simulation");
+    return guard([&] {
+        s->sim.fetch();
+        if (sums) std::memcpy(sums, s->sim.hist.data(), s->sim.hist.size() * 8);
+        if (th_sums) std::memcpy(th_sums, s->sim.th.data(), s->sim.th.size() * 8);
+    });
+}
+
+mbg_status mbg_sim_final_states(mbg_sim* s, double* probs) {
+    if (!s || !probs) return fail(MBG_ERR_ARG, "null argument");
+    return guard([&] {
+        s->sim.fetch();
+        for (size_t i = 0; i < s->sim.fin.size(); ++i) probs[i] = (double)s->sim.fin[i] / (double)s->sim.n_traj;
+    });
+}
+
+mbg_status mbg_sim_fixed_points(mbg_sim* s, uint32_t* states, double* probs, size_t cap, size_t* count) {
+    if (!s) return fail(MBG_ERR_ARG, "null simulation");
+    return guard([&] {
+        s->sim.fetch();
+        const auto& f = s->sim.fixed;
+        if (count) *count = f.size();
+        const int W = s->sim.cm.words;
+        for (size_t i = 0; i < f.size() && i < cap; ++i) {
+            if (states) std::memcpy(states + i * W, f[i].words.data(), W * 4);
+            if (probs) probs[i] = (double)f[i].count / (double)s->sim.n_traj;
+        }
+    });
+}
+
+mbg_status mbg_sim_trajectories(mbg_sim* s, uint32_t* states, double* times, uint32_t* transitions,
+                                uint8_t* status) {
+    if (!s) return fail(MBG_ERR_ARG, "null simulation");
+    return guard([&] {
+        mbg::Sim& x = s->sim;
+        if (!x.ran) throw mbg::StateError("trajectories requested before mbg_sim_run");
+        if (!x.prm.traj_state) throw mbg::StateError("record_trajectories was not set at create");
+        cudaSetDevice(x.device);
+        auto cp = [](void* dst, const void* src, size_t bytes) {
+            cudaError_t e = cudaMemcpy(dst, src, bytes, cudaMemcpyDeviceToHost);
+            if (e != cudaSuccess) throw mbg::CudaError(std::string("cudaMemcpy D2H: ") + cudaGetErrorString(e));
+        };
+        if (states) cp(states, x.prm.traj_state, x.n_traj * x.cm.words * 4);
+        if (times) cp(times, x.prm.traj_time, x.n_traj * 8);
+        if (transitions) cp(transitions, x.prm.traj_transitions, x.n_traj * 4);
+        if (status) cp(status, x.prm.traj_status, x.n_traj);
+    });
+}
+
+mbg_status mbg_write_probtraj_csv(mbg_sim* s, const char* prefix) {
+    if (!s || !prefix) return fail(MBG_ERR_ARG, "null argument");
+    return guard([&] {
+        s->sim.fetch();
+        mbg::write_probtraj_csv(s->sim, std::string(prefix) + "_probtraj.csv");
+    });
+}
+
+mbg_status mbg_write_fp_csv(mbg_sim* s, const char* prefix) {
+    if (!s || !prefix) return fail(MBG_ERR_ARG, "null argument");
+    return guard([&] {
+        s->sim.fetch();
+        mbg::write_fp_csv(s->sim, std::string(prefix) + "_fp.csv");
+    });
+}
+
+mbg_status mbg_print_results(mbg_sim* s, const char* path) {
+    if (!s || !path) return fail(MBG_ERR_ARG, "null argument");
+    return guard([&] {
+        s->sim.fetch();
+        if (std::strcmp(path, "-") == 0) {
+            mbg::print_results(s->sim, std::cout);
+        } else {
+            std::ofstream f(path);
+            if (!f) throw mbg::IoError(std::string("cannot write ") + path);
+            mbg::print_results(s->sim, f);
+        }
+    });
+}
+
+}  // extern "C"

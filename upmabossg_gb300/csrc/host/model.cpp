@@ -1,0 +1,397 @@
+// Expression evaluation and compilation of a parsed model into per-node rate tables.
+//
+// Rate semantics restate src/generator.cpp:84-122: a node's rate is `rate_down` when the node is
+// on and `rate_up` when it is off, with @aliases resolved against the node's own attributes
+// (src/parser/expressions.cpp:223-231). The `@logic ? x : 0` fast path of generator.cpp:93-107
+// is the same function and needs no special case here: every node is tabulated over its
+// regulators instead of being emitted as source text.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <set>
+
+#include "model.hpp"
+
+namespace mbg {
+
+const Expr* Node::attr(const std::string& n) const {
+    for (auto& a : attrs)
+        if (a.first == n) return a.second.get();
+    return nullptr;
+}
+
+Model::Model() {
+    constants["discrete_time"] = 0;
+    constants["sample_count"] = 1000000;
+    constants["max_time"] = 10;
+    constants["time_tick"] = 0.1;
+    constants["seed_pseudorandom"] = 0;
+}
+
+int Model::node_index(const std::string& name) const {
+    for (size_t i = 0; i < nodes.size(); ++i)
+        if (nodes[i].name == name) return (int)i;
+    return -1;
+}
+
+double Model::constant(const std::string& n) const {
+    auto it = constants.find(n);
+    return it == constants.end() ? 0.0 : it->second;
+}
+
+bool Model::is_internal(int i) const {
+    const Expr* e = nodes[i].attr("is_internal");
+    return e && eval_const(*e, *this) != 0;
+}
+
+static double apply_unary(Op op, double x) {
+    switch (op) {
+        case Op::Plus: return x;
+        case Op::Minus: return -x;
+        case Op::Not: return x == 0 ? 1.0 : 0.0;
+        default: throw Error("Unknown unary operator");
+    }
+}
+
+static double apply_binary(Op op, double l, double r) {
+    switch (op) {
+        case Op::Plus: return l + r;
+        case Op::Minus: return l - r;
+        case Op::Star: return l * r;
+        case Op::Slash: return l / r;
+        case Op::And: return (l != 0 && r != 0) ? 1.0 : 0.0;
+        case Op::Or: return (l != 0 || r != 0) ? 1.0 : 0.0;
+        case Op::Xor: return ((l != 0) != (r != 0)) ? 1.0 : 0.0;
+        case Op::Eq: return l == r ? 1.0 : 0.0;
+        case Op::Ne: return l != r ? 1.0 : 0.0;
+        case Op::Le: return l <= r ? 1.0 : 0.0;
+        case Op::Lt: return l < r ? 1.0 : 0.0;
+        case Op::Ge: return l >= r ? 1.0 : 0.0;
+        case Op::Gt: return l > r ? 1.0 : 0.0;
+        default: throw Error("Unknown binary operator");
+    }
+}
+
+static double lookup_var(const Model& m, const std::string& name) {
+    auto it = m.variables.find(name);
+    if (it == m.variables.end()) throw Error("unknown variable " + name);
+    return it->second;
+}
+
+double eval_const(const Expr& e, const Model& m) {
+    switch (e.kind) {
+        case Expr::Kind::Literal: return e.value;
+        case Expr::Kind::Ident: throw Error("identifier " + e.name + " in expression which needs to be evaluated");
+        case Expr::Kind::Var: return lookup_var(m, e.name);
+        case Expr::Kind::Alias: throw Error("alias " + e.name + " in expression which needs to be evaluated");
+        case Expr::Kind::Unary: return apply_unary(e.op, eval_const(*e.a, m));
+        case Expr::Kind::Binary: return apply_binary(e.op, eval_const(*e.a, m), eval_const(*e.b, m));
+        case Expr::Kind::Ternary: return eval_const(*e.a, m) != 0 ? eval_const(*e.b, m) : eval_const(*e.c, m);
+        case Expr::Kind::Paren: return eval_const(*e.a, m);
+    }
+    return 0;
+}
+
+static const Expr& resolve_alias(const Expr& e, const Model& m, int cur) {
+    const Expr* a = m.nodes[cur].attr(e.name.substr(1));
+    if (!a) throw Error("Node " + m.nodes[cur].name + " does not have attribute " + e.name.substr(1));
+    return *a;
+}
+
+double eval_state(const Expr& e, const Model& m, int cur, const uint8_t* state) {
+    switch (e.kind) {
+        case Expr::Kind::Literal: return e.value;
+        case Expr::Kind::Ident: {
+            int i = m.node_index(e.name);
+            if (i < 0) throw Error("unknown node name: " + e.name);
+            return state[i] ? 1.0 : 0.0;
+        }
+        case Expr::Kind::Var: return lookup_var(m, e.name);
+        case Expr::Kind::Alias: return eval_state(resolve_alias(e, m, cur), m, cur, state);
+        case Expr::Kind::Unary: return apply_unary(e.op, eval_state(*e.a, m, cur, state));
+        case Expr::Kind::Binary:
+            return apply_binary(e.op, eval_state(*e.a, m, cur, state), eval_state(*e.b, m, cur, state));
+        case Expr::Kind::Ternary:
+            return eval_state(*e.a, m, cur, state) != 0 ? eval_state(*e.b, m, cur, state)
+                                                         : eval_state(*e.c, m, cur, state);
+        case Expr::Kind::Paren: return eval_state(*e.a, m, cur, state);
+    }
+    return 0;
+}
+
+void collect_support(const Expr& e, const Model& m, int cur, std::vector<int>& out, int depth) {
+    if (depth > 64) throw Error("alias recursion too deep in node " + m.nodes[cur].name);
+    switch (e.kind) {
+        case Expr::Kind::Ident: {
+            int i = m.node_index(e.name);
+            if (i < 0) throw Error("unknown node name: " + e.name);
+            out.push_back(i);
+            break;
+        }
+        case Expr::Kind::Alias: collect_support(resolve_alias(e, m, cur), m, cur, out, depth + 1); break;
+        default:
+            if (e.a) collect_support(*e.a, m, cur, out, depth);
+            if (e.b) collect_support(*e.b, m, cur, out, depth);
+            if (e.c) collect_support(*e.c, m, cur, out, depth);
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// Block evaluator: an expression flattened to postfix form over "input bits" (the node's
+// regulators, then the node itself), evaluated for 64 assignments at a time. Tabulating a node
+// with k regulators costs 2^(k+1) evaluations, so this matters for hub nodes.
+
+namespace {
+
+constexpr int kBlock = 64;
+
+struct Instr {
+    enum Code { Const, Bit, Un, Bin, Tern } code;
+    double c = 0;
+    int bit = 0;
+    Op op = Op::Plus;
+};
+
+void flatten(const Expr& e, const Model& m, int cur, const std::vector<int>& inputs, std::vector<Instr>& prog,
+             int depth) {
+    if (depth > 64) throw Error("alias recursion too deep in node " + m.nodes[cur].name);
+    switch (e.kind) {
+        case Expr::Kind::Literal: prog.push_back({Instr::Const, e.value}); break;
+        case Expr::Kind::Var: prog.push_back({Instr::Const, lookup_var(m, e.name)}); break;
+        case Expr::Kind::Ident: {
+            int i = m.node_index(e.name);
+            auto it = std::find(inputs.begin(), inputs.end(), i);
+            if (it == inputs.end()) throw Error("internal: node outside support");
+            Instr in{Instr::Bit};
+            in.bit = (int)(it - inputs.begin());
+            prog.push_back(in);
+            break;
+        }
+        case Expr::Kind::Alias: flatten(resolve_alias(e, m, cur), m, cur, inputs, prog, depth + 1); break;
+        case Expr::Kind::Paren: flatten(*e.a, m, cur, inputs, prog, depth); break;
+        case Expr::Kind::Unary: {
+            flatten(*e.a, m, cur, inputs, prog, depth);
+            Instr in{Instr::Un};
+            in.op = e.op;
+            prog.push_back(in);
+            break;
+        }
+        case Expr::Kind::Binary: {
+            flatten(*e.a, m, cur, inputs, prog, depth);
+            flatten(*e.b, m, cur, inputs, prog, depth);
+            Instr in{Instr::Bin};
+            in.op = e.op;
+            prog.push_back(in);
+            break;
+        }
+        case Expr::Kind::Ternary:
+            flatten(*e.a, m, cur, inputs, prog, depth);
+            flatten(*e.b, m, cur, inputs, prog, depth);
+            flatten(*e.c, m, cur, inputs, prog, depth);
+            prog.push_back({Instr::Tern});
+            break;
+    }
+}
+
+// Evaluates `prog` for assignments a0 .. a0+63, input bit j = (a >> j) & 1.
+void run_block(const std::vector<Instr>& prog, uint64_t a0, std::vector<double>& stack, double* out) {
+    size_t sp = 0;
+    for (const Instr& in : prog) {
+        switch (in.code) {
+            case Instr::Const: {
+                double* d = &stack[sp++ * kBlock];
+                for (int t = 0; t < kBlock; ++t) d[t] = in.c;
+                break;
+            }
+            case Instr::Bit: {
+                double* d = &stack[sp++ * kBlock];
+                for (int t = 0; t < kBlock; ++t) d[t] = (double)(((a0 + t) >> in.bit) & 1u);
+                break;
+            }
+            case Instr::Un: {
+                double* d = &stack[(sp - 1) * kBlock];
+                for (int t = 0; t < kBlock; ++t) d[t] = apply_unary(in.op, d[t]);
+                break;
+            }
+            case Instr::Bin: {
+                double* l = &stack[(sp - 2) * kBlock];
+                double* r = &stack[(sp - 1) * kBlock];
+                for (int t = 0; t < kBlock; ++t) l[t] = apply_binary(in.op, l[t], r[t]);
+                --sp;
+                break;
+            }
+            case Instr::Tern: {
+                double* c = &stack[(sp - 3) * kBlock];
+                double* x = &stack[(sp - 2) * kBlock];
+                double* y = &stack[(sp - 1) * kBlock];
+                for (int t = 0; t < kBlock; ++t) c[t] = c[t] != 0 ? x[t] : y[t];
+                sp -= 2;
+                break;
+            }
+        }
+    }
+    std::memcpy(out, stack.data(), sizeof(double) * kBlock);
+}
+
+size_t stack_depth(const std::vector<Instr>& prog) {
+    size_t sp = 0, mx = 0;
+    for (const Instr& in : prog) {
+        if (in.code == Instr::Const || in.code == Instr::Bit) ++sp;
+        else if (in.code == Instr::Bin) --sp;
+        else if (in.code == Instr::Tern) sp -= 2;
+        mx = std::max(mx, sp);
+    }
+    return mx;
+}
+
+}  // namespace
+
+uint64_t quantize_rate(double r, int frac_bits) {
+    double q = std::nearbyint(std::ldexp(r, frac_bits));
+    if (!(q < 18446744073709551616.0)) throw Error("rate too large for fixed point");
+    uint64_t v = (uint64_t)q;
+    if (v == 0 && r > 0) v = 1;  // a positive rate stays able to fire
+    return v;
+}
+
+CompiledModel compile_model(const Model& m) {
+    CompiledModel cm;
+    cm.n = (int)m.nodes.size();
+    if (cm.n == 0) throw Error("model has no nodes");
+    if (cm.n > kMaxNodes) throw Error("model has more than 65535 nodes");
+    cm.words = (cm.n + 31) / 32;
+    cm.nodes.resize(cm.n);
+    cm.out_pos.assign(cm.n, -1);
+    for (int i = 0; i < cm.n; ++i) {
+        if (!m.is_internal(i)) {
+            cm.out_pos[i] = (int)cm.out_nodes.size();
+            cm.out_nodes.push_back(i);
+        }
+    }
+    cm.n_out = (int)cm.out_nodes.size();
+
+    // Tabulate every node's rate over (self, regulators) in double.
+    std::vector<std::vector<double>> tabs(cm.n);
+    double sum_max = 0;
+    for (int i = 0; i < cm.n; ++i) {
+        const Node& nd = m.nodes[i];
+        const Expr* up = nd.attr("rate_up");
+        const Expr* down = nd.attr("rate_down");
+        if (!up || !down) throw Error("Node " + nd.name + " lacks rate_up or rate_down");
+        std::vector<int> sup;
+        collect_support(*up, m, i, sup);
+        collect_support(*down, m, i, sup);
+        std::sort(sup.begin(), sup.end());
+        sup.erase(std::unique(sup.begin(), sup.end()), sup.end());
+        CompiledNode& cn = cm.nodes[i];
+        for (int s : sup)
+            if (s != i) cn.regs.push_back(s);
+        const int k = (int)cn.regs.size();
+        if (k > kMaxBinaryRegs)
+            throw Error("node " + nd.name + " reads " + std::to_string(k) + " nodes (limit " +
+                        std::to_string(kMaxBinaryRegs) + ")");
+        cm.max_k = std::max(cm.max_k, k);
+        std::vector<int> inputs = cn.regs;
+        inputs.push_back(i);  // input bit k is the node itself
+        std::vector<Instr> pu, pd;
+        flatten(*up, m, i, inputs, pu, 0);
+        flatten(*down, m, i, inputs, pd, 0);
+        std::vector<double> stack(kBlock * (std::max(stack_depth(pu), stack_depth(pd)) + 1));
+        const uint64_t half = 1ull << k, total = half << 1;
+        std::vector<double>& tab = tabs[i];
+        tab.assign(std::max<uint64_t>(total, kBlock), 0.0);
+        double buf[kBlock];
+        for (uint64_t a0 = 0; a0 < total; a0 += kBlock) {
+            // assignments with the self bit (bit k) clear read rate_up, set read rate_down
+            uint64_t n_here = std::min<uint64_t>(kBlock, total - a0);
+            run_block(pu, a0, stack, buf);
+            for (uint64_t t = 0; t < n_here; ++t)
+                if (!(((a0 + t) >> k) & 1u)) tab[a0 + t] = buf[t];
+            run_block(pd, a0, stack, buf);
+            for (uint64_t t = 0; t < n_here; ++t)
+                if (((a0 + t) >> k) & 1u) tab[a0 + t] = buf[t];
+        }
+        tab.resize(total);
+        double mx = 0;
+        for (double r : tab) {
+            if (!(r >= 0) || std::isinf(r))
+                throw Error("node " + nd.name + " has a negative or non-finite rate");
+            mx = std::max(mx, r);
+        }
+        sum_max += mx;
+    }
+
+    // Fixed-point scale: the sum of every node's largest rate stays below 2^61.
+    int fb = 40;
+    if (sum_max > 0) fb = std::min(40, (int)std::floor(61.0 - std::log2(sum_max)));
+    if (fb < 8) throw Error("rates too large for the fixed-point representation");
+    cm.frac_bits = fb;
+
+    for (int i = 0; i < cm.n; ++i) {
+        CompiledNode& cn = cm.nodes[i];
+        const int k = (int)cn.regs.size();
+        const uint64_t half = 1ull << k, total = half << 1;
+        const std::vector<double>& tab = tabs[i];
+        std::set<double> upv, dnv;
+        for (uint64_t a = 0; a < total; ++a)
+            if (tab[a] != 0) (a < half ? upv : dnv).insert(tab[a]);
+        if (upv.size() <= 1 && dnv.size() <= 1) {
+            cn.kind = NODE_BINARY;
+            cn.up_real = upv.empty() ? 0 : *upv.begin();
+            cn.down_real = dnv.empty() ? 0 : *dnv.begin();
+            cn.up = quantize_rate(cn.up_real, fb);
+            cn.down = quantize_rate(cn.down_real, fb);
+            cn.bits.assign((total + 31) / 32, 0u);
+            for (uint64_t a = 0; a < total; ++a)
+                if (tab[a] != 0) cn.bits[a >> 5] |= 1u << (a & 31);
+        } else {
+            if (k > kMaxPaletteRegs)
+                throw Error("node " + m.nodes[i].name + " has a multi-valued rate over " + std::to_string(k) +
+                            " nodes (limit " + std::to_string(kMaxPaletteRegs) + ")");
+            std::set<double> all(tab.begin(), tab.end());
+            if (all.size() > 256) throw Error("node " + m.nodes[i].name + " has more than 256 distinct rates");
+            cn.kind = NODE_PALETTE;
+            cn.palette_real.assign(all.begin(), all.end());
+            for (double r : cn.palette_real) cn.palette.push_back(quantize_rate(r, fb));
+            cn.pidx.resize(total);
+            for (uint64_t a = 0; a < total; ++a)
+                cn.pidx[a] = (uint8_t)(std::lower_bound(cn.palette_real.begin(), cn.palette_real.end(), tab[a]) -
+                                       cn.palette_real.begin());
+        }
+    }
+
+    cm.deps.assign(cm.n, {});
+    for (int i = 0; i < cm.n; ++i) {
+        cm.deps[i].push_back(i);
+        for (int r : cm.nodes[i].regs) cm.deps[r].push_back(i);
+    }
+    for (auto& d : cm.deps) {
+        std::sort(d.begin(), d.end());
+        d.erase(std::unique(d.begin(), d.end()), d.end());
+    }
+
+    cm.istate.resize(cm.n);
+    cm.istate_thr.resize(cm.n);
+    for (int i = 0; i < cm.n; ++i) {
+        double p = m.nodes[i].istate;
+        if (!(p >= 0 && p <= 1)) throw Error("istate of node " + m.nodes[i].name + " is outside [0, 1]");
+        cm.istate[i] = p;
+        cm.istate_thr[i] = (uint32_t)std::floor(p * 16777216.0);
+    }
+
+    // run constants (main.cpp:128-132)
+    cm.discrete = m.constant("discrete_time") != 0;
+    cm.max_time = m.constant("max_time");
+    cm.tick = m.constant("time_tick");
+    double sc = m.constant("sample_count");
+    cm.sample_count = sc > 0 ? (uint64_t)sc : 0;
+    double seed = m.constant("seed_pseudorandom");
+    cm.seed = seed > 0 ? (uint64_t)seed : 0;
+    if (!(cm.max_time > 0) || !(cm.tick > 0)) throw Error("max_time and time_tick must be positive");
+    // window count as the reference computes it, in float (window_average_small.cpp:26)
+    cm.windows = (int)std::ceil((float)cm.max_time / (float)cm.tick);
+    if (cm.windows < 1) cm.windows = 1;
+    return cm;
+}
+
+}  // namespace mbg

@@ -1,0 +1,292 @@
+// Simulation handle: device image of the model, result buffers, kernel choice and launch.
+//
+// Replaces the batch runner src/simulation_runner.cu:54-180 (segments of <= 99 steps, trajectory
+// buffers, thrust partitions and refills between launches) with one persistent launch in which
+// every warp (or thread) pulls trajectory ids from a work counter until none are left, plus the
+// statistics objects of src/statistics/ whose work happens inside that launch.
+#include "sim.hpp"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+#include "../device/kernels.h"
+
+namespace mbg {
+
+namespace {
+
+void ck(cudaError_t e, const char* what) {
+    if (e != cudaSuccess) throw CudaError(std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+template <class T>
+T* dalloc(size_t n, std::vector<void*>& owned) {
+    if (n == 0) n = 1;
+    void* p = nullptr;
+    cudaError_t e = cudaMalloc(&p, n * sizeof(T));
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        throw NoMemError("cudaMalloc of " + std::to_string(n * sizeof(T)) + " bytes: " + cudaGetErrorString(e));
+    }
+    owned.push_back(p);
+    return static_cast<T*>(p);
+}
+
+template <class T>
+T* upload(const std::vector<T>& v, std::vector<void*>& owned) {
+    T* p = dalloc<T>(v.size(), owned);
+    if (!v.empty()) ck(cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice), "cudaMemcpy H2D");
+    return p;
+}
+
+uint32_t next_pow2(uint64_t x) {
+    uint64_t p = 1;
+    while (p < x) p <<= 1;
+    return (uint32_t)p;
+}
+
+}  // namespace
+
+DeviceLayout layout_model(const CompiledModel& cm) {
+    DeviceLayout d;
+    d.nodes.resize(cm.n);
+    d.tab_off.assign(cm.n, 0);
+    d.pal_off.assign(cm.n, 0);
+    for (int i = 0; i < cm.n; ++i) {
+        const CompiledNode& cn = cm.nodes[i];
+        DevNode& dn = d.nodes[i];
+        std::memset(&dn, 0, sizeof dn);
+        dn.reg_off = (uint32_t)d.regs.size();
+        for (int r : cn.regs) d.regs.push_back((uint16_t)r);
+        dn.k = (uint16_t)cn.regs.size();
+        dn.kind = (uint16_t)cn.kind;
+        if (cn.kind == NODE_BINARY) {
+            dn.tab_off = (uint32_t)d.tabs.size();
+            d.tabs.insert(d.tabs.end(), cn.bits.begin(), cn.bits.end());
+            dn.up = cn.up;
+            dn.down = cn.down;
+        } else {
+            dn.tab_off = (uint32_t)d.pidx.size();
+            d.pidx.insert(d.pidx.end(), cn.pidx.begin(), cn.pidx.end());
+            dn.pal_off = (uint32_t)d.palette.size();
+            d.palette.insert(d.palette.end(), cn.palette.begin(), cn.palette.end());
+        }
+        d.tab_off[i] = dn.tab_off;
+        d.pal_off[i] = dn.pal_off;
+    }
+    d.dep_off.push_back(0);
+    for (int i = 0; i < cm.n; ++i) {
+        for (int x : cm.deps[i]) d.deps.push_back((uint16_t)x);
+        d.dep_off.push_back((uint32_t)d.deps.size());
+    }
+    for (int o : cm.out_nodes) d.out_nodes.push_back((uint16_t)o);
+    for (int i = 0; i < cm.n; ++i) d.out_pos.push_back((int16_t)cm.out_pos[i]);
+    d.istate_thr = cm.istate_thr;
+    return d;
+}
+
+Sim::~Sim() {
+    if (ev0) cudaEventDestroy(ev0);
+    if (ev1) cudaEventDestroy(ev1);
+    if (evk0) cudaEventDestroy(evk0);
+    if (evk1) cudaEventDestroy(evk1);
+    if (host_small) cudaFreeHost(host_small);
+    for (void* p : owned) cudaFree(p);
+}
+
+void Sim::create(const CompiledModel& model, const std::vector<std::string>& node_names, const mbg_sim_opts& o) {
+    cm = model;
+    names = node_names;
+    opts = o;
+    n_traj = o.n_traj ? o.n_traj : cm.sample_count;
+    if (n_traj == 0) throw ArgError("no trajectories to simulate (n_traj and sample_count are 0)");
+    if (n_traj > 0xFFFFFFFFull) throw ArgError("more than 2^32 - 1 trajectories in one run");
+    seed = o.use_cfg_seed ? cm.seed : o.seed;
+    if (cm.n_out > 24) throw ModelError("more than 24 output nodes");
+    const uint64_t S = 1ull << cm.n_out;
+    const uint64_t hist_bytes = (uint64_t)cm.windows * S * 8;
+    if (hist_bytes > (16ull << 30)) throw ModelError("window histogram would exceed 16 GiB");
+    if (!cm.discrete && (double)n_traj * cm.tick >= 2147483648.0)
+        throw ModelError("n_traj x time_tick too large for the 2^-32 fixed-point window sums");
+
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        throw CudaError("no CUDA device available");
+    }
+    device = o.device;
+    if (device < 0 || device >= ndev) throw ArgError("device ordinal out of range");
+    ck(cudaSetDevice(device), "cudaSetDevice");
+    ck(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device), "cudaDeviceGetAttribute");
+
+    dl = layout_model(cm);
+    // model arrays
+    std::memset(&prm, 0, sizeof prm);
+    prm.nodes = upload(dl.nodes, owned);
+    prm.regs = upload(dl.regs, owned);
+    prm.tabs = upload(dl.tabs, owned);
+    prm.pidx = upload(dl.pidx, owned);
+    prm.palette = reinterpret_cast<const unsigned long long*>(upload(dl.palette, owned));
+    prm.dep_off = upload(dl.dep_off, owned);
+    prm.deps = upload(dl.deps, owned);
+    prm.out_nodes = upload(dl.out_nodes, owned);
+    prm.out_pos = upload(dl.out_pos, owned);
+    prm.istate_thr = upload(dl.istate_thr, owned);
+    prm.n = cm.n;
+    prm.words = cm.words;
+    prm.n_out = cm.n_out;
+    prm.windows = cm.windows;
+    prm.frac_bits = cm.frac_bits;
+    prm.discrete = cm.discrete ? 1 : 0;
+    prm.max_time = cm.max_time;
+    prm.tick = cm.tick;
+    prm.to_real = std::ldexp(1.0f, -cm.frac_bits);
+    prm.max_steps = o.max_steps ? o.max_steps : 0xFFFFFFFFu;
+    prm.seed = seed;
+    prm.n_traj = n_traj;
+    prm.traj_base = o.traj_base;
+    // results
+    prm.hist = dalloc<unsigned long long>((size_t)(cm.windows * S), owned);
+    prm.th_hist = dalloc<unsigned long long>((size_t)cm.windows, owned);
+    prm.final_hist = dalloc<unsigned int>((size_t)S, owned);
+    fp_capacity = (uint32_t)n_traj;
+    prm.fp_capacity = fp_capacity;
+    prm.fp_states = dalloc<unsigned int>((size_t)fp_capacity * cm.words, owned);
+    prm.fp_count = dalloc<unsigned int>(1, owned);
+    prm.counters = dalloc<unsigned long long>(CNT_COUNT, owned);
+    prm.error_flag = dalloc<unsigned int>(1, owned);
+    if (o.record_trajectories) {
+        prm.traj_state = dalloc<unsigned int>((size_t)n_traj * cm.words, owned);
+        prm.traj_time = dalloc<double>((size_t)n_traj, owned);
+        prm.traj_transitions = dalloc<unsigned int>((size_t)n_traj, owned);
+        prm.traj_status = dalloc<unsigned char>((size_t)n_traj, owned);
+    }
+    n_slots = std::max<uint32_t>(1024, next_pow2(2ull * fp_capacity));
+    slot_rep = dalloc<unsigned int>(n_slots, owned);
+    slot_cnt = dalloc<unsigned int>(n_slots, owned);
+    fp_out_states = dalloc<unsigned int>((size_t)fp_capacity * cm.words, owned);
+    fp_out_cnt = dalloc<unsigned int>(fp_capacity, owned);
+    fp_unique = dalloc<unsigned int>(1, owned);
+    ck(cudaMallocHost(&host_small, 256), "cudaMallocHost");
+    ck(cudaEventCreate(&ev0), "cudaEventCreate");
+    ck(cudaEventCreate(&ev1), "cudaEventCreate");
+    ck(cudaEventCreate(&evk0), "cudaEventCreate");
+    ck(cudaEventCreate(&evk1), "cudaEventCreate");
+
+    // layout
+    int cutoff = o.thread_cutoff > 0 ? o.thread_cutoff : 96;
+    layout = o.layout;
+    if (layout == MBG_LAYOUT_AUTO) layout = cm.n <= cutoff ? MBG_LAYOUT_THREAD : MBG_LAYOUT_WARP;
+    if (layout == MBG_LAYOUT_THREAD && cm.words > 16) throw ModelError("thread layout supports at most 512 nodes");
+    if (layout == MBG_LAYOUT_WARP && cm.n_out > 32) throw ModelError("warp layout supports at most 32 outputs");
+    block = o.block_size > 0 ? o.block_size : 256;
+    if (block % 32 != 0 || block > 256) throw ArgError("block_size must be a multiple of 32, at most 256");
+    int bps = 0;
+    if (layout == MBG_LAYOUT_THREAD) {
+        thread_kernel = jit_thread_kernel(generate_thread_model(cm, dl), jit_ms);
+        smem = 0;
+        ck(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, (const void*)thread_kernel, block, 0),
+           "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
+    } else {
+        smem = (size_t)(block / 32) * sim_warp_smem_per_warp(cm.n);
+        if (smem > 227 * 1024) throw ModelError("model too large for the warp layout's shared memory");
+        ck(sim_warp_configure(smem), "cudaFuncSetAttribute");
+        ck(sim_warp_occupancy(block, smem, &bps), "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
+    }
+    if (bps < 1) throw CudaError("kernel cannot be resident with this block size");
+    if (o.blocks_per_sm > 0) bps = std::min(bps, (int)o.blocks_per_sm);
+    grid = sms * bps;
+}
+
+void Sim::run(cudaStream_t stream) {
+    ck(cudaSetDevice(device), "cudaSetDevice");
+    const uint64_t S = 1ull << cm.n_out;
+    ck(cudaEventRecord(ev0, stream), "cudaEventRecord");
+    ck(cudaMemsetAsync(prm.hist, 0, cm.windows * S * 8, stream), "cudaMemsetAsync");
+    ck(cudaMemsetAsync(prm.th_hist, 0, cm.windows * 8, stream), "cudaMemsetAsync");
+    ck(cudaMemsetAsync(prm.final_hist, 0, S * 4, stream), "cudaMemsetAsync");
+    ck(cudaMemsetAsync(prm.fp_count, 0, 4, stream), "cudaMemsetAsync");
+    ck(cudaMemsetAsync(prm.counters, 0, CNT_COUNT * 8, stream), "cudaMemsetAsync");
+    ck(cudaMemsetAsync(prm.error_flag, 0, 4, stream), "cudaMemsetAsync");
+    ck(cudaEventRecord(evk0, stream), "cudaEventRecord");
+    if (layout == MBG_LAYOUT_THREAD) {
+        void* args[] = {(void*)&prm};
+        ck(cudaLaunchKernel((const void*)thread_kernel, dim3(grid), dim3(block), args, 0, stream),
+           "cudaLaunchKernel(mbg_sim_thread)");
+    } else {
+        ck(launch_sim_warp(prm, grid, block, smem, stream), "launch mbg_sim_warp");
+    }
+    ck(cudaEventRecord(evk1, stream), "cudaEventRecord");
+    ck(launch_fp_aggregate(prm.fp_states, prm.fp_count, fp_capacity, cm.words, slot_rep, slot_cnt, n_slots,
+                           fp_out_states, fp_out_cnt, fp_unique, prm.error_flag, sms, stream),
+       "launch fixed-point aggregation");
+    ck(cudaEventRecord(ev1, stream), "cudaEventRecord");
+    unsigned long long* hc = reinterpret_cast<unsigned long long*>(host_small);
+    ck(cudaMemcpyAsync(hc, prm.counters, CNT_COUNT * 8, cudaMemcpyDeviceToHost, stream), "cudaMemcpyAsync");
+    ck(cudaMemcpyAsync(hc + CNT_COUNT, prm.error_flag, 4, cudaMemcpyDeviceToHost, stream), "cudaMemcpyAsync");
+    ck(cudaMemcpyAsync(reinterpret_cast<char*>(hc + CNT_COUNT) + 4, fp_unique, 4, cudaMemcpyDeviceToHost, stream),
+       "cudaMemcpyAsync");
+    ck(cudaStreamSynchronize(stream), "simulation kernel");
+    float ms = 0, kms = 0;
+    cudaEventElapsedTime(&ms, ev0, ev1);
+    cudaEventElapsedTime(&kms, evk0, evk1);
+    summary = mbg_run_summary{};
+    summary.trajectories = n_traj;
+    summary.transitions = hc[CNT_TRANSITIONS];
+    summary.steps = hc[CNT_STEPS];
+    summary.finished = hc[CNT_FINISHED];
+    summary.fixed_points = hc[CNT_FIXED];
+    summary.step_limited = hc[CNT_STEP_LIMIT];
+    summary.errors = hc[CNT_ERROR];
+    uint32_t flags[2];
+    std::memcpy(flags, hc + CNT_COUNT, 8);
+    summary.device_error = flags[0];
+    summary.fixed_point_states = flags[1];
+    summary.layout = layout;
+    summary.sim_ms = ms;
+    summary.kernel_ms = kms;
+    summary.jit_ms = jit_ms;
+    ran = true;
+    fetched = false;
+    if (summary.device_error) throw DeviceError("device error flags 0x" + std::to_string(summary.device_error));
+}
+
+void Sim::fetch() {
+    if (!ran) throw StateError("results requested before mbg_sim_run");
+    if (fetched) return;
+    ck(cudaSetDevice(device), "cudaSetDevice");
+    const uint64_t S = 1ull << cm.n_out;
+    hist.resize(cm.windows * S);
+    th.resize(cm.windows);
+    fin.resize(S);
+    ck(cudaMemcpy(hist.data(), prm.hist, hist.size() * 8, cudaMemcpyDeviceToHost), "cudaMemcpy D2H");
+    ck(cudaMemcpy(th.data(), prm.th_hist, th.size() * 8, cudaMemcpyDeviceToHost), "cudaMemcpy D2H");
+    ck(cudaMemcpy(fin.data(), prm.final_hist, fin.size() * 4, cudaMemcpyDeviceToHost), "cudaMemcpy D2H");
+    // fixed points: representatives, counts, then their states
+    const uint32_t nu = (uint32_t)summary.fixed_point_states;
+    std::vector<uint32_t> words((size_t)nu * cm.words), cnt(nu);
+    if (nu) {
+        ck(cudaMemcpy(words.data(), fp_out_states, words.size() * 4, cudaMemcpyDeviceToHost), "cudaMemcpy D2H");
+        ck(cudaMemcpy(cnt.data(), fp_out_cnt, nu * 4, cudaMemcpyDeviceToHost), "cudaMemcpy D2H");
+    }
+    fixed.clear();
+    fixed.reserve(nu);
+    for (uint32_t u = 0; u < nu; ++u) {
+        FixedPoint f;
+        f.words.assign(words.begin() + (size_t)u * cm.words, words.begin() + (size_t)(u + 1) * cm.words);
+        f.count = cnt[u];
+        fixed.push_back(std::move(f));
+    }
+    // order of static_state_t::operator< (state.h:38-45): highest word first
+    std::sort(fixed.begin(), fixed.end(), [](const FixedPoint& a, const FixedPoint& b) {
+        for (size_t w = a.words.size(); w-- > 0;)
+            if (a.words[w] != b.words[w]) return a.words[w] < b.words[w];
+        return false;
+    });
+    fetched = true;
+}
+
+}  // namespace mbg

@@ -1,0 +1,63 @@
+// Simulation handle internals (behind the opaque mbg_sim of the C ABI).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../../include/mbg.h"
+#include "sim_host.hpp"
+
+namespace mbg {
+
+struct FixedPoint {
+    std::vector<uint32_t> words;
+    uint64_t count = 0;
+};
+
+class Sim {
+public:
+    ~Sim();
+    void create(const CompiledModel& cm, const std::vector<std::string>& names, const mbg_sim_opts& o);
+    void run(cudaStream_t stream);
+    void fetch();  // copies results to the host vectors below
+
+    CompiledModel cm;
+    std::vector<std::string> names;
+    mbg_sim_opts opts{};
+    uint64_t n_traj = 0, seed = 0;
+    int device = 0, sms = 0, layout = 0, grid = 0, block = 256;
+    size_t smem = 0;
+    double jit_ms = 0;
+    void* thread_kernel = nullptr;
+    DeviceLayout dl;
+    SimParams prm{};
+    uint32_t fp_capacity = 0, n_slots = 0;
+    unsigned* slot_rep = nullptr;
+    unsigned* slot_cnt = nullptr;
+    unsigned* fp_out_states = nullptr;
+    unsigned* fp_out_cnt = nullptr;
+    unsigned* fp_unique = nullptr;
+    void* host_small = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr, evk0 = nullptr, evk1 = nullptr;
+    std::vector<void*> owned;
+
+    bool ran = false, fetched = false;
+    mbg_run_summary summary{};
+    std::vector<uint64_t> hist, th;
+    std::vector<uint32_t> fin;
+    std::vector<FixedPoint> fixed;
+};
+
+// Output formats (output.cpp).
+void write_probtraj_csv(const Sim& s, const std::string& path);
+void write_fp_csv(const Sim& s, const std::string& path);
+void print_results(const Sim& s, std::ostream& os);
+double window_prob(const Sim& s, size_t idx);
+double window_th(const Sim& s, int w);
+std::string state_string(const std::vector<std::string>& names, const std::vector<uint32_t>& words, int n);
+std::string out_state_string(const Sim& s, uint32_t idx);
+
+}  // namespace mbg

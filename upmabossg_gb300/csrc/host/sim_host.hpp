@@ -1,0 +1,50 @@
+// Internal host-side interfaces of libmbg (not part of the C ABI).
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../device/sim_types.h"
+#include "model.hpp"
+
+namespace mbg {
+
+// Error classes mapped to mbg_status by the C ABI (parse errors are plain mbg::Error).
+struct ArgError : Error { using Error::Error; };
+struct ModelError : Error { using Error::Error; };
+struct CudaError : Error { using Error::Error; };
+struct NoMemError : Error { using Error::Error; };
+struct DeviceError : Error { using Error::Error; };
+struct StateError : Error { using Error::Error; };
+struct JitError : Error { using Error::Error; };
+struct IoError : Error { using Error::Error; };
+
+// Device image of a compiled model: the arrays SimParams points at, before upload.
+struct DeviceLayout {
+    std::vector<DevNode> nodes;
+    std::vector<uint16_t> regs;
+    std::vector<uint32_t> tabs;
+    std::vector<uint8_t> pidx;
+    std::vector<uint64_t> palette;
+    std::vector<uint32_t> dep_off;
+    std::vector<uint16_t> deps;
+    std::vector<uint16_t> out_nodes;
+    std::vector<int16_t> out_pos;
+    std::vector<uint32_t> istate_thr;
+    std::vector<uint32_t> tab_off, pal_off;  // per node
+};
+
+DeviceLayout layout_model(const CompiledModel& cm);
+
+// NVRTC source of the thread-per-trajectory kernel `mbg_sim_thread` specialised to one model.
+std::string generate_thread_model(const CompiledModel& cm, const DeviceLayout& dl);
+
+// Compiles (or fetches from the in-process / on-disk cache) the full NVRTC program made of the
+// shared device headers and `model_src`, loads it on the current device and returns the kernel
+// handle usable with cudaLaunchKernel. `compile_ms` is 0 on a cache hit. Throws mbg::Error.
+void* jit_thread_kernel(const std::string& model_src, double& compile_ms);
+// Compiles without loading (no device needed); returns milliseconds. Throws JitError.
+double jit_compile_only(const std::string& model_src);
+
+}  // namespace mbg
