@@ -105,6 +105,12 @@ const char* mbg_model_node_name(const mbg_model* m, int32_t i);
 /* Output node indices (node order), `cap` entries at most; returns the count. */
 int32_t mbg_model_outputs(const mbg_model* m, int32_t* idx, int32_t cap);
 
+/* Rate of node `node` in the full state `state` (one byte per node, 0 or 1), from the compiled
+ * tables, host side: the exact fixed-point value and the real value. Replaces the generated
+ * `<node>_rate` device functions of src/generator.cpp:84-122 as an inspectable function. */
+mbg_status mbg_model_rate(const mbg_model* m, int32_t node, const uint8_t* state, uint64_t* fixed_rate,
+                          double* rate);
+
 /* Generates the model's thread-per-trajectory kernel and compiles it with NVRTC for sm_103a
  * without loading it (needs no GPU). */
 mbg_status mbg_model_jit_check(const mbg_model* m, double* compile_ms);

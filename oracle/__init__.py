@@ -40,6 +40,7 @@ class _Opts(ctypes.Structure):
         ("threads", ctypes.c_int),
         ("max_steps", ctypes.c_uint32),
         ("keep_trajectories", ctypes.c_int),
+        ("legacy_final", ctypes.c_int),
     ]
 
 
@@ -120,7 +121,8 @@ class OracleResult:
 
 
 def run(bnd: str, cfg: str, *, frac_bits: int, n_traj: int = 0, seed=None, traj_base: int = 0,
-        threads: int = 0, max_steps: int = 0, keep_trajectories: bool = False) -> OracleResult:
+        threads: int = 0, max_steps: int = 0, keep_trajectories: bool = False,
+        legacy_final: bool = False) -> OracleResult:
     L = lib()
     o = _Opts()
     o.n_traj = n_traj
@@ -131,6 +133,7 @@ def run(bnd: str, cfg: str, *, frac_bits: int, n_traj: int = 0, seed=None, traj_
     o.threads = threads
     o.max_steps = max_steps
     o.keep_trajectories = 1 if keep_trajectories else 0
+    o.legacy_final = 1 if legacy_final else 0
     err = ctypes.create_string_buffer(1024)
     h = L.orc_run(bnd.encode(), cfg.encode(), ctypes.byref(o), err, 1024)
     if not h:

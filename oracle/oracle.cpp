@@ -230,6 +230,7 @@ extern "C" orc_result* orc_run(const char* bnd_text, const char* cfg_text, const
                 uint64_t step = 0;
                 uint32_t trans = 0;
                 uint8_t status = 0, tie = 0;
+                int legacy_flip = -1;
                 for (;;) {
                     uint64_t Q = 0;
                     double R = 0, Rout = 0;
@@ -283,6 +284,16 @@ extern "C" orc_result* orc_run(const char* bnd_text, const char* cfg_text, const
                     if (t1 >= max_time) {
                         t = max_time;
                         status = mbg::TRAJ_FINISHED;
+                        if (o->legacy_final) {
+                            uint64_t rt = mbg::pick_target(d.y, d.z, Q), acc = 0;
+                            for (int i = 0; i < n; ++i) {
+                                acc += q[i];
+                                if (acc > rt) {
+                                    legacy_flip = i;
+                                    break;
+                                }
+                            }
+                        }
                         break;
                     }
                     uint64_t rt = mbg::pick_target(d.y, d.z, Q);
@@ -316,7 +327,9 @@ extern "C" orc_result* orc_run(const char* bnd_text, const char* cfg_text, const
                     ++trans;
                 }
                 uint32_t so = 0;
+                if (legacy_flip >= 0) s[legacy_flip] ^= 1;
                 for (size_t p = 0; p < out_nodes.size(); ++p) so |= (uint32_t)s[out_nodes[p]] << p;
+                if (legacy_flip >= 0) s[legacy_flip] ^= 1;
                 L.cnt[0] += trans;
                 L.cnt[6] += step + (status == mbg::TRAJ_STEP_LIMIT ? 0 : 1);
                 if (status == mbg::TRAJ_FINISHED) ++L.cnt[1];

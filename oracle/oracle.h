@@ -41,6 +41,9 @@ typedef struct {
     int threads;         /* 0: hardware concurrency */
     uint32_t max_steps;  /* 0: unlimited */
     int keep_trajectories; /* store per-trajectory end records */
+    int legacy_final;    /* final-state histogram after one more flip: the rule of the earlier
+                            MaBoSSG build that produced the reference's test/*.res goldens (the
+                            current simulation.cu:143-147 ends before that flip) */
 } orc_opts;
 
 /* Runs the oracle on .bnd/.cfg texts. Returns NULL on error (message in err). */

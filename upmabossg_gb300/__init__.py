@@ -22,7 +22,8 @@ STATUS = {0: "OK", 1: "ARG", 2: "IO", 3: "PARSE", 4: "MODEL", 5: "CUDA", 6: "JIT
 # Every symbol include/mbg.h declares.
 EXPORTS = (
     "mbg_last_error", "mbg_version", "mbg_device_count", "mbg_model_parse_files", "mbg_model_parse_strings",
-    "mbg_model_destroy", "mbg_model_info_get", "mbg_model_node_name", "mbg_model_outputs", "mbg_model_jit_check",
+    "mbg_model_destroy", "mbg_model_info_get", "mbg_model_node_name", "mbg_model_outputs", "mbg_model_rate",
+    "mbg_model_jit_check",
     "mbg_sim_opts_default", "mbg_sim_create", "mbg_sim_destroy", "mbg_sim_run", "mbg_sim_summary",
     "mbg_sim_probtraj", "mbg_sim_probtraj_raw", "mbg_sim_final_states", "mbg_sim_fixed_points",
     "mbg_sim_trajectories", "mbg_write_probtraj_csv", "mbg_write_fp_csv", "mbg_print_results",
@@ -85,6 +86,7 @@ def lib():
             "mbg_model_info_get": (ctypes.c_int, [vp, ctypes.POINTER(ModelInfo)]),
             "mbg_model_node_name": (ctypes.c_char_p, [vp, i32]),
             "mbg_model_outputs": (i32, [vp, dp, i32]),
+            "mbg_model_rate": (ctypes.c_int, [vp, i32, dp, ctypes.POINTER(u64), ctypes.POINTER(ctypes.c_double)]),
             "mbg_model_jit_check": (ctypes.c_int, [vp, ctypes.POINTER(ctypes.c_double)]),
             "mbg_sim_opts_default": (None, [ctypes.POINTER(SimOpts)]),
             "mbg_sim_create": (ctypes.c_int, [vp, ctypes.POINTER(SimOpts), ctypes.POINTER(vp)]),
@@ -146,6 +148,16 @@ class Model:
         h = ctypes.c_void_p()
         _check(lib().mbg_model_parse_strings(bnd.encode(), cfg.encode(), ctypes.byref(h)))
         return cls(h)
+
+    def rate(self, node: int, state) -> tuple:
+        """(fixed-point rate, real rate) of `node` in the full state (sequence of 0/1 per node)."""
+        st = np.ascontiguousarray(np.asarray(state, dtype=np.uint8))
+        if st.size != self.info.nodes:
+            raise ValueError("state needs one entry per node")
+        q = ctypes.c_uint64()
+        r = ctypes.c_double()
+        _check(lib().mbg_model_rate(self._h, int(node), _p(st), ctypes.byref(q), ctypes.byref(r)))
+        return q.value, r.value
 
     def jit_check(self) -> float:
         ms = ctypes.c_double()

@@ -151,6 +151,31 @@ int32_t mbg_model_outputs(const mbg_model* m, int32_t* idx, int32_t cap) {
     return n;
 }
 
+mbg_status mbg_model_rate(const mbg_model* m, int32_t node, const uint8_t* state, uint64_t* fixed_rate,
+                          double* rate) {
+    if (!m || !state) return fail(MBG_ERR_ARG, "null argument");
+    const mbg::CompiledModel& cm = m->cm;
+    if (node < 0 || node >= cm.n) return fail(MBG_ERR_ARG, "node index out of range");
+    const mbg::CompiledNode& cn = cm.nodes[node];
+    const int k = (int)cn.regs.size();
+    uint64_t a = state[node] ? (1ull << k) : 0ull;
+    for (int j = 0; j < k; ++j)
+        if (state[cn.regs[j]]) a |= 1ull << j;
+    uint64_t q;
+    double r;
+    if (cn.kind == mbg::NODE_BINARY) {
+        bool on = (cn.bits[a >> 5] >> (a & 31)) & 1u;
+        q = on ? (state[node] ? cn.down : cn.up) : 0;
+        r = on ? (state[node] ? cn.down_real : cn.up_real) : 0.0;
+    } else {
+        q = cn.palette[cn.pidx[a]];
+        r = cn.palette_real[cn.pidx[a]];
+    }
+    if (fixed_rate) *fixed_rate = q;
+    if (rate) *rate = r;
+    return MBG_OK;
+}
+
 mbg_status mbg_model_jit_check(const mbg_model* m, double* compile_ms) {
     if (!m) return fail(MBG_ERR_ARG, "null model");
     return guard([&] {
