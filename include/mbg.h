@@ -141,6 +141,22 @@ mbg_status mbg_write_fp_csv(mbg_sim* s, const char* prefix);
 /* The reference's stdout report (final points, fixed points, windows) to a file path or "-". */
 mbg_status mbg_print_results(mbg_sim* s, const char* path);
 
+/* No counterpart in the reference. Fixed-point aggregation for callers that must not allocate
+ * device memory (a host that owns every allocation through its own pool, a latency-critical loop
+ * where cudaMalloc could stall the device, a fixed device footprint after start-up). All buffers
+ * are device memory owned by the caller: `states` holds n_states x words state words;
+ * `unique_states` (room for n_states x words) and `counts` (n_states) receive the distinct states
+ * and how often each occurs, in no particular order; `*n_unique` their number. Nothing is
+ * allocated: the hash table is a 512 KiB device array inside libmbg.so that every GPU loading the
+ * library keeps until exit. At most 32768 states per call (MBG_ERR_ARG beyond). The work is queued
+ * on `stream`; results are valid once the stream has completed it. The first call on a device
+ * looks the array's address up on that device, so make it before any stream capture. Calls share
+ * the array and each clears it first: calls queued on one stream are safe, calls that overlap on
+ * the GPU race. */
+mbg_status mbg_fixed_points_aggregate_noalloc(const uint32_t* states, uint32_t n_states, int32_t words,
+                                              uint32_t* unique_states, uint32_t* counts, uint32_t* n_unique,
+                                              void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -27,6 +27,7 @@ EXPORTS = (
     "mbg_sim_opts_default", "mbg_sim_create", "mbg_sim_destroy", "mbg_sim_run", "mbg_sim_summary",
     "mbg_sim_probtraj", "mbg_sim_probtraj_raw", "mbg_sim_final_states", "mbg_sim_fixed_points",
     "mbg_sim_trajectories", "mbg_write_probtraj_csv", "mbg_write_fp_csv", "mbg_print_results",
+    "mbg_fixed_points_aggregate_noalloc",
 )
 
 
@@ -101,6 +102,7 @@ def lib():
             "mbg_write_probtraj_csv": (ctypes.c_int, [vp, ctypes.c_char_p]),
             "mbg_write_fp_csv": (ctypes.c_int, [vp, ctypes.c_char_p]),
             "mbg_print_results": (ctypes.c_int, [vp, ctypes.c_char_p]),
+            "mbg_fixed_points_aggregate_noalloc": (ctypes.c_int, [vp, ctypes.c_uint32, i32, vp, vp, vp, vp]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)

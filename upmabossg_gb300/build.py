@@ -26,7 +26,7 @@ NVCC = os.path.join(CUDA, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 HOST_SOURCES = ["parser.cpp", "model.cpp", "codegen.cpp", "jit.cpp", "sim.cpp", "output.cpp", "capi.cpp"]
-DEVICE_SOURCES = ["sim_aot.cu"]
+DEVICE_SOURCES = ["sim_aot.cu", "noalloc.cu"]
 JIT_HEADERS = ["sim_types.h", "philox.h", "sim_core.cuh"]
 
 

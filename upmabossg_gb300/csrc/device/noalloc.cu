@@ -1,0 +1,135 @@
+// Fixed-point aggregation into caller-provided device buffers, with no device allocation.
+//
+// Who needs this: code that may not call cudaMalloc at the moment it wants the aggregation, for
+// example a host that runs the library inside its own memory pool and forbids other allocations,
+// code enqueueing work from a stream callback or between the launches of a latency-critical
+// loop (cudaMalloc can synchronise the device), or an application that must keep its device
+// footprint fixed after start-up. Such a caller hands in the fixed-point states it has and the
+// buffers for the result; the only scratch is the hash table below, a file-scope device array
+// that every GPU which loads libmbg.so holds until the process exits.
+//
+// Limits and sharing: at most kNoallocMaxStates states per call. All calls on one device share
+// the one table; every call clears it on its own stream first, so calls queued on one stream are
+// safe, but calls that overlap on the GPU (different streams, or different host threads without
+// ordering) race on the table and give wrong counts.
+#include <cuda_runtime.h>
+
+#include <mutex>
+#include <string>
+
+#include "../../../include/mbg.h"
+
+namespace mbg {
+// Records the message for mbg_last_error() and returns `st` (defined with the C ABI, capi.cpp).
+mbg_status set_error(mbg_status st, const std::string& msg);
+}  // namespace mbg
+
+namespace {
+
+constexpr unsigned kNoallocSlots = 1u << 16;          // hash slots
+constexpr unsigned kNoallocMaxStates = kNoallocSlots / 2;  // load factor at most 1/2
+constexpr int kMaxDevices = 64;
+
+// [0, slots): representative entry per slot, [slots, 2 slots): count per slot. 512 KiB.
+static __device__ __align__(256) unsigned g_fp_scratch[2 * kNoallocSlots];
+
+std::mutex g_setup_mu;
+unsigned* g_scratch_ptr[kMaxDevices] = {};
+
+__device__ __forceinline__ unsigned long long na_hash(const unsigned* w, int words) {
+    unsigned long long h = 0x9E3779B97F4A7C15ull ^ (unsigned long long)words;
+    for (int i = 0; i < words; ++i) {
+        h ^= w[i];
+        h *= 0xBF58476D1CE4E5B9ull;
+        h ^= h >> 29;
+    }
+    h *= 0x94D049BB133111EBull;
+    return h ^ (h >> 32);
+}
+
+__device__ __forceinline__ bool na_same(const unsigned* a, const unsigned* b, int words) {
+    for (int i = 0; i < words; ++i)
+        if (a[i] != b[i]) return false;
+    return true;
+}
+
+// Same insertion as mbg_fp_insert, with the entry count passed by value and the table in the
+// static scratch array. The table has twice as many slots as entries, so a probe always ends.
+__global__ void fp_insert_noalloc(const unsigned* __restrict__ states, unsigned n, int words,
+                                  unsigned* __restrict__ scratch) {
+    unsigned* rep = scratch;
+    unsigned* cnt = scratch + kNoallocSlots;
+    const unsigned mask = kNoallocSlots - 1u;
+    for (unsigned e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
+        const unsigned* me = states + (unsigned long long)e * words;
+        unsigned s = (unsigned)na_hash(me, words) & mask;
+        for (unsigned probe = 0; probe <= mask; ++probe) {
+            unsigned cur = atomicCAS(rep + s, 0xFFFFFFFFu, e);
+            if (cur == 0xFFFFFFFFu || na_same(states + (unsigned long long)cur * words, me, words)) {
+                atomicAdd(cnt + s, 1u);
+                break;
+            }
+            s = (s + 1u) & mask;
+        }
+    }
+}
+
+__global__ void fp_compact_noalloc(const unsigned* __restrict__ states, int words, const unsigned* __restrict__ scratch,
+                                   unsigned* __restrict__ out_states, unsigned* __restrict__ out_cnt,
+                                   unsigned* __restrict__ n_unique) {
+    const unsigned* rep = scratch;
+    const unsigned* cnt = scratch + kNoallocSlots;
+    for (unsigned s = blockIdx.x * blockDim.x + threadIdx.x; s < kNoallocSlots; s += gridDim.x * blockDim.x) {
+        unsigned r = rep[s];
+        if (r != 0xFFFFFFFFu) {
+            unsigned o = atomicAdd(n_unique, 1u);
+            out_cnt[o] = cnt[s];
+            for (int w = 0; w < words; ++w)
+                out_states[(unsigned long long)o * words + w] = states[(unsigned long long)r * words + w];
+        }
+    }
+}
+
+// Device address of the scratch array on the current device, looked up once per device.
+cudaError_t scratch_for_current_device(unsigned** out) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lock(g_setup_mu);
+    if (!g_scratch_ptr[dev]) {
+        void* p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_fp_scratch);
+        if (e != cudaSuccess) return e;
+        g_scratch_ptr[dev] = static_cast<unsigned*>(p);
+    }
+    *out = g_scratch_ptr[dev];
+    return cudaSuccess;
+}
+
+}  // namespace
+
+extern "C" mbg_status mbg_fixed_points_aggregate_noalloc(const uint32_t* states, uint32_t n_states, int32_t words,
+                                                         uint32_t* unique_states, uint32_t* counts,
+                                                         uint32_t* n_unique, void* stream) {
+    if (n_states > kNoallocMaxStates)
+        return mbg::set_error(MBG_ERR_ARG, "mbg_fixed_points_aggregate_noalloc: " + std::to_string(n_states) +
+                                               " states exceed the limit of " + std::to_string(kNoallocMaxStates) +
+                                               " per call");
+    if (words < 1 || !n_unique || (n_states > 0 && (!states || !unique_states || !counts)))
+        return mbg::set_error(MBG_ERR_ARG, "mbg_fixed_points_aggregate_noalloc: null buffer or words < 1");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    unsigned* scratch = nullptr;
+    cudaError_t e = scratch_for_current_device(&scratch);
+    if (e == cudaSuccess) e = cudaMemsetAsync(scratch, 0xFF, sizeof(unsigned) * kNoallocSlots, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(scratch + kNoallocSlots, 0, sizeof(unsigned) * kNoallocSlots, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(n_unique, 0, sizeof(unsigned), st);
+    if (e == cudaSuccess && n_states > 0) {
+        fp_insert_noalloc<<<128, 256, 0, st>>>(states, n_states, words, scratch);
+        fp_compact_noalloc<<<128, 256, 0, st>>>(states, words, scratch, unique_states, counts, n_unique);
+        e = cudaGetLastError();
+    }
+    if (e != cudaSuccess)
+        return mbg::set_error(MBG_ERR_CUDA, std::string("mbg_fixed_points_aggregate_noalloc: ") + cudaGetErrorString(e));
+    return mbg::set_error(MBG_OK, "");
+}

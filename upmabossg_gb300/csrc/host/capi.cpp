@@ -86,6 +86,10 @@ mbg_status build_model(const std::string& bnd, const std::string& cfg, const std
 
 }  // namespace
 
+namespace mbg {
+mbg_status set_error(mbg_status st, const std::string& msg) { return fail(st, msg); }
+}  // namespace mbg
+
 extern "C" {
 
 const char* mbg_last_error(void) { return g_err.c_str(); }
