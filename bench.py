@@ -176,7 +176,7 @@ def run_ours(args):
         import torch.distributed as dist
         dist.init_process_group("nccl")
     net = make_network(args.workload)
-    n_total = net.sample_count
+    n_total = args.n_traj or net.sample_count
     n_rank = n_total // ws
     base = rank * n_rank
     bnd, cfg = net.bnd(), net.cfg()
@@ -290,6 +290,7 @@ def main():
     ap.add_argument("--layout", type=int, default=0)
     ap.add_argument("--cpu-seconds", type=float, default=CPU_SAMPLE_SECONDS)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--n-traj", type=int, default=0, help="trajectories (default: the workload's); profiling only")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

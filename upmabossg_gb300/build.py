@@ -27,7 +27,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 HOST_SOURCES = ["parser.cpp", "model.cpp", "codegen.cpp", "jit.cpp", "sim.cpp", "output.cpp", "capi.cpp"]
 DEVICE_SOURCES = ["sim_aot.cu", "noalloc.cu"]
-JIT_HEADERS = ["sim_types.h", "philox.h", "sim_core.cuh"]
+JIT_HEADERS = ["sim_types.h", "philox.h", "sim_core.cuh", "sim_thread.cuh"]
 
 
 def _run(cmd, verbose):

@@ -7,10 +7,17 @@
 
 namespace mbg {
 
-cudaError_t launch_sim_warp(const SimParams& p, int grid, int block, size_t smem, cudaStream_t stream);
-cudaError_t sim_warp_configure(size_t smem);
-unsigned sim_warp_smem_per_warp(int n);
-cudaError_t sim_warp_occupancy(int block, size_t smem, int* blocks_per_sm);
+cudaError_t launch_sim_warp(const SimParams& p, bool cached_index, int grid, int block, size_t smem,
+                            cudaStream_t stream);
+cudaError_t sim_warp_configure(bool cached_index, size_t smem);
+unsigned sim_warp_smem_per_warp(int n, bool cached_index);
+cudaError_t sim_warp_occupancy(bool cached_index, int block, size_t smem, int* blocks_per_sm);
+cudaError_t launch_sim_warp_batch(const BatchDesc& b, bool cached_index, int grid, int block, size_t smem,
+                                  cudaStream_t stream);
+cudaError_t sim_warp_batch_configure(bool cached_index, size_t smem, int block, int* blocks_per_sm);
+unsigned sim_warp_batch_slice_bytes(int max_n, bool cached_index);
+cudaError_t launch_fp_aggregate_batch(const SimParams* params, const FpSlots* fps, int n_inst, int blocks_x,
+                                      cudaStream_t stream);
 cudaError_t launch_fp_aggregate(const unsigned* fp_states, const unsigned* fp_count, unsigned capacity, int words,
                                 unsigned* slot_rep, unsigned* slot_cnt, unsigned n_slots, unsigned* out_states,
                                 unsigned* out_cnt, unsigned* n_unique, unsigned* error_flag, int sms,

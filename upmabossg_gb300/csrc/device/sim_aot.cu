@@ -11,9 +11,27 @@
 
 namespace mbg {
 
-extern "C" __global__ void __launch_bounds__(256) mbg_sim_warp(const SimParams p) {
+// Cached-index variant (regulator index of every node kept in shared memory).
+extern "C" __global__ void __launch_bounds__(256, 4) mbg_sim_warp(const SimParams p) {
     extern __shared__ __align__(16) unsigned char smem[];
-    sim_warp_body(p, smem);
+    sim_warp_body<true>(p, smem);
+}
+
+// Gather variant, for models whose index cache would not fit beside enough warps.
+extern "C" __global__ void __launch_bounds__(256) mbg_sim_warp_gather(const SimParams p) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    sim_warp_body<false>(p, smem);
+}
+
+// Batched instances (parameter sweeps), both variants.
+extern "C" __global__ void __launch_bounds__(256, 4) mbg_sim_warp_batch(const BatchDesc b) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    sim_warp_batch_body<true>(b, smem);
+}
+
+extern "C" __global__ void __launch_bounds__(256) mbg_sim_warp_batch_gather(const BatchDesc b) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    sim_warp_batch_body<false>(b, smem);
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -79,22 +97,94 @@ extern "C" __global__ void mbg_fp_compact(const unsigned* __restrict__ fp_states
     }
 }
 
+// Batched aggregation: blockIdx.y selects the instance.
+extern "C" __global__ void mbg_fp_insert_batch(const SimParams* __restrict__ params, const FpSlots* __restrict__ fps) {
+    const SimParams& p = params[blockIdx.y];
+    const FpSlots f = fps[blockIdx.y];
+    unsigned n = *p.fp_count;
+    if (n > p.fp_capacity) n = p.fp_capacity;
+    const int words = p.words;
+    const unsigned mask = f.n_slots - 1u;
+    for (unsigned e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
+        const unsigned* me = p.fp_states + (unsigned long long)e * words;
+        unsigned s = (unsigned)hash_words(me, words) & mask;
+        bool placed = false;
+        for (unsigned probe = 0; probe <= mask; ++probe) {
+            const unsigned cur = atomicCAS(f.slot_rep + s, 0xFFFFFFFFu, e);
+            if (cur == 0xFFFFFFFFu || same_words(p.fp_states + (unsigned long long)cur * words, me, words)) {
+                atomicAdd(f.slot_cnt + s, 1u);
+                placed = true;
+                break;
+            }
+            s = (s + 1u) & mask;
+        }
+        if (!placed) atomicOr(p.error_flag, (unsigned)DEV_ERR_FP_OVERFLOW);
+    }
+}
+
+extern "C" __global__ void mbg_fp_compact_batch(const SimParams* __restrict__ params, const FpSlots* __restrict__ fps) {
+    const SimParams& p = params[blockIdx.y];
+    const FpSlots f = fps[blockIdx.y];
+    const int words = p.words;
+    for (unsigned s = blockIdx.x * blockDim.x + threadIdx.x; s < f.n_slots; s += gridDim.x * blockDim.x) {
+        const unsigned r = f.slot_rep[s];
+        if (r != 0xFFFFFFFFu) {
+            const unsigned o = atomicAdd(f.n_unique, 1u);
+            f.out_cnt[o] = f.slot_cnt[s];
+            for (int w = 0; w < words; ++w)
+                f.out_states[(unsigned long long)o * words + w] = p.fp_states[(unsigned long long)r * words + w];
+        }
+    }
+}
+
 // ---------------------------------------------------------------------------------------------
 // Host-side launchers.
 
-cudaError_t launch_sim_warp(const SimParams& p, int grid, int block, size_t smem, cudaStream_t stream) {
-    mbg_sim_warp<<<grid, block, smem, stream>>>(p);
+cudaError_t launch_sim_warp_batch(const BatchDesc& b, bool cached_index, int grid, int block, size_t smem,
+                                  cudaStream_t stream) {
+    if (cached_index) mbg_sim_warp_batch<<<grid, block, smem, stream>>>(b);
+    else mbg_sim_warp_batch_gather<<<grid, block, smem, stream>>>(b);
     return cudaGetLastError();
 }
 
-cudaError_t sim_warp_configure(size_t smem) {
-    return cudaFuncSetAttribute(mbg_sim_warp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+cudaError_t sim_warp_batch_configure(bool cached_index, size_t smem, int block, int* blocks_per_sm) {
+    const void* f = cached_index ? (const void*)mbg_sim_warp_batch : (const void*)mbg_sim_warp_batch_gather;
+    cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, f, block, smem);
 }
 
-unsigned sim_warp_smem_per_warp(int n) { return warp_smem_bytes(n); }
+unsigned sim_warp_batch_slice_bytes(int max_n, bool cached_index) {
+    return batch_params_bytes() + ((warp_smem_bytes(max_n, cached_index) + 15u) & ~15u);
+}
 
-cudaError_t sim_warp_occupancy(int block, size_t smem, int* blocks_per_sm) {
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, mbg_sim_warp, block, smem);
+cudaError_t launch_fp_aggregate_batch(const SimParams* params, const FpSlots* fps, int n_inst, int blocks_x,
+                                      cudaStream_t stream) {
+    dim3 grid(blocks_x, n_inst);
+    mbg_fp_insert_batch<<<grid, 256, 0, stream>>>(params, fps);
+    mbg_fp_compact_batch<<<grid, 256, 0, stream>>>(params, fps);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_sim_warp(const SimParams& p, bool cached_index, int grid, int block, size_t smem,
+                            cudaStream_t stream) {
+    if (cached_index) mbg_sim_warp<<<grid, block, smem, stream>>>(p);
+    else mbg_sim_warp_gather<<<grid, block, smem, stream>>>(p);
+    return cudaGetLastError();
+}
+
+cudaError_t sim_warp_configure(bool cached_index, size_t smem) {
+    return cached_index ? cudaFuncSetAttribute(mbg_sim_warp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)
+                        : cudaFuncSetAttribute(mbg_sim_warp_gather, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                               (int)smem);
+}
+
+unsigned sim_warp_smem_per_warp(int n, bool cached_index) { return warp_smem_bytes(n, cached_index); }
+
+cudaError_t sim_warp_occupancy(bool cached_index, int block, size_t smem, int* blocks_per_sm) {
+    return cached_index ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, mbg_sim_warp, block, smem)
+                        : cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, mbg_sim_warp_gather, block,
+                                                                        smem);
 }
 
 cudaError_t launch_fp_aggregate(const unsigned* fp_states, const unsigned* fp_count, unsigned capacity, int words,

@@ -32,14 +32,19 @@ enum Counter {
     CNT_COUNT = 8,
 };
 
-// One node of the compiled model, 32 bytes.
+// One node of the compiled model, 64 bytes (one aligned pair of 32-byte sectors). The first 16
+// bytes are all the warp layout's leaf pick reads; a truth table of up to 64 bits (k <= 5) is
+// stored inline so evaluating such a node needs no second dependent load.
+constexpr int kInlineRegs = 12;
 struct DevNode {
-    unsigned int tab_off;  // BINARY: word offset into tabs; PALETTE: byte offset into pidx
-    unsigned int reg_off;  // offset into regs
-    unsigned short k;      // number of regulators (the node itself excluded)
-    unsigned short kind;   // 0 binary, 1 palette
-    unsigned int pal_off;  // PALETTE: offset into palette
     unsigned long long up, down;  // BINARY fixed-point rates
+    unsigned int tab_off;         // BINARY: word offset into tabs; PALETTE: byte offset into pidx
+    unsigned int pal_off;         // PALETTE: offset into palette
+    unsigned short k;             // number of regulators (the node itself excluded)
+    unsigned short kind;          // 0 binary, 1 palette
+    unsigned int reg_off;         // offset of all k regulators in regs
+    unsigned short r[kInlineRegs];  // the first min(k, 12) regulators
+    unsigned long long table;     // BINARY with k <= 5: the 2^(k+1) table bits
 };
 
 struct SimParams {
@@ -50,12 +55,19 @@ struct SimParams {
     const unsigned char* pidx;
     const unsigned long long* palette;
     const unsigned int* dep_off;  // n + 1
-    const unsigned short* deps;
+    // For node k: every node d whose rate reads k, plus k itself, as (d << 16) | (k_d << 8) | pos,
+    // k_d = number of regulators of d, pos = position of k among them (0xFF for d == k).
+    const unsigned int* deps;
     const unsigned short* out_nodes;  // n_out
     const short* out_pos;             // n: position among outputs or -1
     const unsigned int* istate_thr;   // n
     int n, words, n_out, windows;
     int frac_bits, discrete;
+    int has_palette;                 // any NODE_PALETTE node
+    // Clock: unsigned fixed point with time_bits fraction bits (32 <= time_bits <= 40), so the
+    // step loop needs no FP64 arithmetic (GB300's FP64 rate is a small fraction of its FP32 rate).
+    int time_bits;
+    unsigned long long max_time_fx, tick_fx;
     double max_time, tick;
     float to_real;  // 2^-frac_bits
     unsigned int max_steps;
@@ -75,6 +87,25 @@ struct SimParams {
     unsigned char* traj_status;      // optional
     unsigned long long* counters;    // CNT_COUNT
     unsigned int* error_flag;
+};
+
+// A batched launch over many instances (sim_warp.cuh: sim_warp_batch_body).
+struct BatchDesc {
+    const SimParams* params;           // n_inst
+    const unsigned long long* prefix;  // n_inst + 1 cumulative trajectory counts
+    int n_inst;
+    unsigned long long* work;          // work-item counter
+    unsigned slice_bytes;              // per warp: SimParams copy (16-byte padded) + largest warp slice
+};
+
+// Fixed-point hash table and compacted output of one batched instance.
+struct FpSlots {
+    unsigned int* slot_rep;   // n_slots, 0xFFFFFFFF = empty
+    unsigned int* slot_cnt;   // n_slots
+    unsigned int n_slots;     // power of two, >= 2 x fp_capacity
+    unsigned int* out_states; // fp_capacity x words
+    unsigned int* out_cnt;    // fp_capacity
+    unsigned int* n_unique;
 };
 
 }  // namespace mbg

@@ -61,6 +61,7 @@ DeviceLayout layout_model(const CompiledModel& cm) {
         std::memset(&dn, 0, sizeof dn);
         dn.reg_off = (uint32_t)d.regs.size();
         for (int r : cn.regs) d.regs.push_back((uint16_t)r);
+        for (size_t j = 0; j < cn.regs.size() && j < (size_t)kInlineRegs; ++j) dn.r[j] = (uint16_t)cn.regs[j];
         dn.k = (uint16_t)cn.regs.size();
         dn.kind = (uint16_t)cn.kind;
         if (cn.kind == NODE_BINARY) {
@@ -68,6 +69,10 @@ DeviceLayout layout_model(const CompiledModel& cm) {
             d.tabs.insert(d.tabs.end(), cn.bits.begin(), cn.bits.end());
             dn.up = cn.up;
             dn.down = cn.down;
+            if (cn.regs.size() <= 5) {
+                dn.table = cn.bits[0];
+                if (cn.bits.size() > 1) dn.table |= (uint64_t)cn.bits[1] << 32;
+            }
         } else {
             dn.tab_off = (uint32_t)d.pidx.size();
             d.pidx.insert(d.pidx.end(), cn.pidx.begin(), cn.pidx.end());
@@ -79,13 +84,49 @@ DeviceLayout layout_model(const CompiledModel& cm) {
     }
     d.dep_off.push_back(0);
     for (int i = 0; i < cm.n; ++i) {
-        for (int x : cm.deps[i]) d.deps.push_back((uint16_t)x);
+        for (int x : cm.deps[i]) {
+            const auto& regs = cm.nodes[x].regs;
+            uint32_t pos = 0xFF;
+            for (size_t j = 0; j < regs.size(); ++j)
+                if (regs[j] == i) pos = (uint32_t)j;
+            d.deps.push_back(((uint32_t)x << 16) | ((uint32_t)regs.size() << 8) | pos);
+        }
         d.dep_off.push_back((uint32_t)d.deps.size());
     }
     for (int o : cm.out_nodes) d.out_nodes.push_back((uint16_t)o);
     for (int i = 0; i < cm.n; ++i) d.out_pos.push_back((int16_t)cm.out_pos[i]);
     d.istate_thr = cm.istate_thr;
     return d;
+}
+
+void set_model_constants(SimParams& prm, const CompiledModel& cm) {
+    prm.n = cm.n;
+    prm.words = cm.words;
+    prm.n_out = cm.n_out;
+    prm.windows = cm.windows;
+    prm.frac_bits = cm.frac_bits;
+    prm.discrete = cm.discrete ? 1 : 0;
+    prm.max_time = cm.max_time;
+    prm.tick = cm.tick;
+    prm.has_palette = 0;
+    for (auto& nd : cm.nodes) prm.has_palette |= nd.kind == NODE_PALETTE ? 1 : 0;
+    // clock fraction bits: max_time + tick stays below 2^(61 - bits)
+    const int tb = std::min(40, (int)std::floor(61.0 - std::log2(cm.max_time + cm.tick + 1.0)));
+    if (tb < 32) throw ModelError("max_time too large for the fixed-point clock");
+    prm.time_bits = tb;
+    prm.max_time_fx = (unsigned long long)std::nearbyint(std::ldexp(cm.max_time, tb));
+    prm.tick_fx = (unsigned long long)std::nearbyint(std::ldexp(cm.tick, tb));
+    prm.to_real = std::ldexp(1.0f, -cm.frac_bits);
+}
+
+void check_model_limits(const CompiledModel& cm, uint64_t n_traj) {
+    if (n_traj == 0) throw ArgError("no trajectories to simulate (n_traj and sample_count are 0)");
+    if (n_traj > 0xFFFFFFFFull) throw ArgError("more than 2^32 - 1 trajectories in one run");
+    if (cm.n_out > 24) throw ModelError("more than 24 output nodes");
+    const uint64_t hist_bytes = (uint64_t)cm.windows * (1ull << cm.n_out) * 8;
+    if (hist_bytes > (16ull << 30)) throw ModelError("window histogram would exceed 16 GiB");
+    if (!cm.discrete && (double)n_traj * cm.tick >= 2147483648.0)
+        throw ModelError("n_traj x time_tick too large for the 2^-32 fixed-point window sums");
 }
 
 Sim::~Sim() {
@@ -102,15 +143,9 @@ void Sim::create(const CompiledModel& model, const std::vector<std::string>& nod
     names = node_names;
     opts = o;
     n_traj = o.n_traj ? o.n_traj : cm.sample_count;
-    if (n_traj == 0) throw ArgError("no trajectories to simulate (n_traj and sample_count are 0)");
-    if (n_traj > 0xFFFFFFFFull) throw ArgError("more than 2^32 - 1 trajectories in one run");
     seed = o.use_cfg_seed ? cm.seed : o.seed;
-    if (cm.n_out > 24) throw ModelError("more than 24 output nodes");
+    check_model_limits(cm, n_traj);
     const uint64_t S = 1ull << cm.n_out;
-    const uint64_t hist_bytes = (uint64_t)cm.windows * S * 8;
-    if (hist_bytes > (16ull << 30)) throw ModelError("window histogram would exceed 16 GiB");
-    if (!cm.discrete && (double)n_traj * cm.tick >= 2147483648.0)
-        throw ModelError("n_traj x time_tick too large for the 2^-32 fixed-point window sums");
 
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
@@ -135,15 +170,7 @@ void Sim::create(const CompiledModel& model, const std::vector<std::string>& nod
     prm.out_nodes = upload(dl.out_nodes, owned);
     prm.out_pos = upload(dl.out_pos, owned);
     prm.istate_thr = upload(dl.istate_thr, owned);
-    prm.n = cm.n;
-    prm.words = cm.words;
-    prm.n_out = cm.n_out;
-    prm.windows = cm.windows;
-    prm.frac_bits = cm.frac_bits;
-    prm.discrete = cm.discrete ? 1 : 0;
-    prm.max_time = cm.max_time;
-    prm.tick = cm.tick;
-    prm.to_real = std::ldexp(1.0f, -cm.frac_bits);
+    set_model_constants(prm, cm);
     prm.max_steps = o.max_steps ? o.max_steps : 0xFFFFFFFFu;
     prm.seed = seed;
     prm.n_traj = n_traj;
@@ -191,10 +218,13 @@ void Sim::create(const CompiledModel& model, const std::vector<std::string>& nod
         ck(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, (const void*)thread_kernel, block, 0),
            "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
     } else {
-        smem = (size_t)(block / 32) * sim_warp_smem_per_warp(cm.n);
+        // keep every node's regulator index in shared memory while a block's share stays small
+        // enough for several resident blocks per SM; otherwise re-gather it on each update
+        cached_index = (size_t)(block / 32) * sim_warp_smem_per_warp(cm.n, true) <= 64 * 1024;
+        smem = (size_t)(block / 32) * sim_warp_smem_per_warp(cm.n, cached_index);
         if (smem > 227 * 1024) throw ModelError("model too large for the warp layout's shared memory");
-        ck(sim_warp_configure(smem), "cudaFuncSetAttribute");
-        ck(sim_warp_occupancy(block, smem, &bps), "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
+        ck(sim_warp_configure(cached_index, smem), "cudaFuncSetAttribute");
+        ck(sim_warp_occupancy(cached_index, block, smem, &bps), "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
     }
     if (bps < 1) throw CudaError("kernel cannot be resident with this block size");
     if (o.blocks_per_sm > 0) bps = std::min(bps, (int)o.blocks_per_sm);
@@ -217,7 +247,7 @@ void Sim::run(cudaStream_t stream) {
         ck(cudaLaunchKernel((const void*)thread_kernel, dim3(grid), dim3(block), args, 0, stream),
            "cudaLaunchKernel(mbg_sim_thread)");
     } else {
-        ck(launch_sim_warp(prm, grid, block, smem, stream), "launch mbg_sim_warp");
+        ck(launch_sim_warp(prm, cached_index, grid, block, smem, stream), "launch mbg_sim_warp");
     }
     ck(cudaEventRecord(evk1, stream), "cudaEventRecord");
     ck(launch_fp_aggregate(prm.fp_states, prm.fp_count, fp_capacity, cm.words, slot_rep, slot_cnt, n_slots,

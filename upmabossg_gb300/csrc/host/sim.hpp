@@ -30,6 +30,7 @@ public:
     uint64_t n_traj = 0, seed = 0;
     int device = 0, sms = 0, layout = 0, grid = 0, block = 256;
     size_t smem = 0;
+    bool cached_index = false;
     double jit_ms = 0;
     void* thread_kernel = nullptr;
     DeviceLayout dl;

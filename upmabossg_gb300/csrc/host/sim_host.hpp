@@ -28,7 +28,7 @@ struct DeviceLayout {
     std::vector<uint8_t> pidx;
     std::vector<uint64_t> palette;
     std::vector<uint32_t> dep_off;
-    std::vector<uint16_t> deps;
+    std::vector<uint32_t> deps;  // (d << 16) | (k_d << 8) | position of the source node (0xFF: itself)
     std::vector<uint16_t> out_nodes;
     std::vector<int16_t> out_pos;
     std::vector<uint32_t> istate_thr;
@@ -36,6 +36,10 @@ struct DeviceLayout {
 };
 
 DeviceLayout layout_model(const CompiledModel& cm);
+// Model-dependent SimParams fields (sizes, clock, rate scale).
+void set_model_constants(SimParams& prm, const CompiledModel& cm);
+// Throws if a run of n_traj trajectories of cm exceeds the result representation.
+void check_model_limits(const CompiledModel& cm, uint64_t n_traj);
 
 // NVRTC source of the thread-per-trajectory kernel `mbg_sim_thread` specialised to one model.
 std::string generate_thread_model(const CompiledModel& cm, const DeviceLayout& dl);
