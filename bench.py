@@ -165,6 +165,83 @@ def run_reference(args):
     return 0
 
 
+SWEEP_DESC = ("256 instances, 50..2000 nodes (log-uniform), 2-3 regulators per node, rates lognormal(0,0.5), "
+              "8 outputs, 1e4..1e5 trajectories (log-uniform), max_time 30, tick 0.5")
+
+
+def sweep_models(n_instances=256):
+    import upmabossg_gb300 as mbg
+    from upmabossg_gb300 import synth
+    nets = synth.sweep(n_instances)
+    return nets, [mbg.Model.from_strings(n.bnd(), n.cfg()) for n in nets]
+
+
+def measure_sweep(steps, warmup, local=0, autotune=True):
+    """Plain batched simulation of the sweep: every instance simulated in one graph launch.
+    Returns sweep points (instances) per second and transitions per second."""
+    import upmabossg_gb300 as mbg
+    nets, models = sweep_models()
+    batch = mbg.Batch(models, device=local, autotune=autotune)
+    for _ in range(max(1, warmup)):
+        batch.run()
+    ms = []
+    for _ in range(steps):
+        batch.run()
+        ms.append(batch.summary()["sim_ms"])
+    s = batch.summary()
+    step_ms = statistics.mean(ms)
+    return {"metric": "sweep points/s (plain batched simulation)", "value": len(models) / (step_ms * 1e-3),
+            "unit": "points/s", "ms_per_step": step_ms, "transitions_per_s": s["transitions"] / (step_ms * 1e-3),
+            "kernel_ms": s["kernel_ms"], "trajectories": s["trajectories"], "instances": len(models),
+            "shape": batch.shape(), "workload": SWEEP_DESC}
+
+
+SURROGATE_DESC = ("200-node network (2-3 regulators, rates 1) with 32 rate blocks scaled log-uniform in [0.1, 10], "
+                  "8 outputs, final window of max_time 100 / tick 1; MLP 32-512-512-512-256 (BF16, FP32 accumulate), "
+                  "ensemble of 4; 20000 training points x 1e4 trajectories; 1e6 candidates")
+
+
+def measure_surrogate(n_train=20000, n_traj=10000, n_cand=1_000_000, epochs=60, seed=7):
+    """Sweep points/s of surrogate-screened versus plain batched simulation, with the TV error of
+    the surrogate against re-simulation of every reported point."""
+    import numpy as np
+
+    import upmabossg_gb300 as mbg
+    from upmabossg_gb300 import screen, synth
+    space = synth.surrogate_space()
+    base = mbg.Model.from_strings(space.base.bnd(), space.base.cfg())
+    sim = screen.PointSimulator(base, space.blocks, n_traj=n_traj, chunk=1024)
+    rng = np.random.default_rng(seed)
+    train = space.sample(rng, n_train)
+    t0 = time.perf_counter()
+    y = sim.final_window(train).astype(np.float32)
+    data_s = time.perf_counter() - t0
+    plain = sim.stats.points / sim.stats.seconds
+    plain_transitions = sim.stats.transitions / sim.stats.seconds
+    s = mbg.Surrogate(32, 256, hidden=512, hidden_layers=3, ensemble=4, seed=seed)
+    t1 = time.perf_counter()
+    loss = s.train(screen.encode(train), y, epochs=epochs, batch=256, lr=1e-3, seed=seed)
+    train_s = time.perf_counter() - t1
+    held = space.sample(rng, 1000)
+    y_held = sim.final_window(held, ids=np.arange(n_train, n_train + 1000))
+    p_held, spread_held = s.predict(screen.encode(held))
+    tv_held = screen.total_variation(p_held, y_held)
+    target = int(np.argmax(y.var(axis=0)))
+    cands = space.sample(rng, n_cand)
+    rep = screen.screen(s, sim, cands, target, threshold=0.9, spread_cut=0.1, plain_points_per_s=plain,
+                        max_report=1000)
+    return {
+        "metric": "sweep points/s, surrogate-screened vs plain batched simulation", "value": rep.screened_points_per_s,
+        "unit": "points/s", "plain_points_per_s": plain, "speedup": rep.speedup,
+        "plain_transitions_per_s": plain_transitions,
+        "tv_reported": {"mean": rep.tv_mean, "max": rep.tv_max, "share_le_0.01": rep.tv_frac_ok, "n": rep.reported},
+        "tv_held_out": {"mean": float(tv_held.mean()), "median": float(np.median(tv_held)),
+                        "share_le_0.01": float((tv_held <= 0.01).mean()), "n": len(held)},
+        "resimulated": rep.resimulated, "uncertain": rep.uncertain, "candidates": rep.candidates,
+        "predict_s": rep.predict_s, "resim_s": rep.resim_s, "train_s": train_s, "train_loss": loss,
+        "training_data_s": data_s, "workload": SURROGATE_DESC}
+
+
 def run_ours(args):
     ws, rank, local = dist_env()
     import upmabossg_gb300 as mbg
@@ -286,7 +363,7 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="medium", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="medium", choices=sorted(WORKLOADS) + ["sweep", "surrogate"])
     ap.add_argument("--layout", type=int, default=0)
     ap.add_argument("--cpu-seconds", type=float, default=CPU_SAMPLE_SECONDS)
     ap.add_argument("--no-cpu", action="store_true")
@@ -294,6 +371,23 @@ def main():
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "surrogate":
+        import upmabossg_gb300 as mbg
+        if mbg.device_count() < 1:
+            raise SystemExit("bench: no CUDA device")
+        line = measure_surrogate()
+        line.update({"n_gpus": 1, "higher_is_better": True, "data": "synthetic", "dtype": "bf16"})
+        print(json.dumps(line), flush=True)
+        return 0
+    if args.workload == "sweep":
+        import upmabossg_gb300 as mbg
+        if mbg.device_count() < 1:
+            raise SystemExit("bench: no CUDA device")
+        line = measure_sweep(args.steps, args.warmup)
+        line.update({"n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+                     "data": "synthetic", "dtype": "u64"})
+        print(json.dumps(line), flush=True)
+        return 0
     return run_ours(args)
 
 

@@ -111,6 +111,14 @@ int32_t mbg_model_outputs(const mbg_model* m, int32_t* idx, int32_t cap);
 mbg_status mbg_model_rate(const mbg_model* m, int32_t node, const uint8_t* state, uint64_t* fixed_rate,
                           double* rate);
 
+/* A copy of `base` whose node i has its up rates multiplied by up_scale[i] and its down rates by
+ * down_scale[i] (NULL: 1), re-quantized as if the cfg had carried the scaled values. For
+ * parameter sweeps: no re-parse, no re-tabulation. Models with multi-valued rates are refused.
+ * The copy has no expression trees (mbg_model_rate and the simulation work; nothing else needs
+ * them). */
+mbg_status mbg_model_with_rate_scales(const mbg_model* base, const double* up_scale, const double* down_scale,
+                                      mbg_model** out);
+
 /* Generates the model's thread-per-trajectory kernel and compiles it with NVRTC for sm_103a
  * without loading it (needs no GPU). */
 mbg_status mbg_model_jit_check(const mbg_model* m, double* compile_ms);
@@ -140,6 +148,62 @@ mbg_status mbg_write_probtraj_csv(mbg_sim* s, const char* prefix);
 mbg_status mbg_write_fp_csv(mbg_sim* s, const char* prefix);
 /* The reference's stdout report (final points, fixed points, windows) to a file path or "-". */
 mbg_status mbg_print_results(mbg_sim* s, const char* path);
+
+/* ---- Batched parameter sweeps --------------------------------------------------------------
+ * Many independent simulations ("instances": any models, trajectory counts and seeds) in one
+ * persistent warp-per-trajectory launch, captured once into a CUDA graph and replayed by every
+ * mbg_batch_run. Replaces one reference CLI run per instance (src/main.cpp:101-169), each of which
+ * recompiles its kernels with NVRTC. Results per instance are the same as a single simulation's. */
+typedef struct mbg_batch mbg_batch;
+
+typedef struct {
+    int32_t device;        /* CUDA device ordinal */
+    uint32_t max_steps;    /* per-trajectory step cap; 0: none */
+    int32_t block_size;    /* threads per block (multiple of 32, <= 256); 0: default or autotuned */
+    int32_t blocks_per_sm; /* 0: occupancy limit */
+    int32_t autotune;      /* 1: time the launch shapes on the first run and keep the fastest */
+} mbg_batch_opts;
+
+void mbg_batch_opts_default(mbg_batch_opts* o);
+/* n_traj and seeds may be NULL: each instance then uses its cfg sample_count / seed_pseudorandom. */
+mbg_status mbg_batch_create(const mbg_model* const* models, int32_t n_models, const uint64_t* n_traj,
+                            const uint64_t* seeds, const mbg_batch_opts* o, mbg_batch** out);
+void mbg_batch_destroy(mbg_batch* b);
+/* Runs every instance on `stream` (NULL: an internal stream) and waits. */
+mbg_status mbg_batch_run(mbg_batch* b, void* stream);
+/* Totals over the batch (sim_ms: the whole graph, kernel_ms: the simulation kernel). */
+mbg_status mbg_batch_summary(const mbg_batch* b, mbg_run_summary* out);
+mbg_status mbg_batch_instance_summary(const mbg_batch* b, int32_t i, mbg_run_summary* out);
+mbg_status mbg_batch_probtraj(mbg_batch* b, int32_t i, double* probs, double* tr_entropy);
+mbg_status mbg_batch_probtraj_raw(mbg_batch* b, int32_t i, uint64_t* sums, uint64_t* th_sums);
+mbg_status mbg_batch_final_states(mbg_batch* b, int32_t i, double* probs);
+mbg_status mbg_batch_fixed_points(mbg_batch* b, int32_t i, uint32_t* states, double* probs, size_t cap,
+                                  size_t* count);
+/* Launch shape in use: threads per block, shared-memory index cache (0/1), blocks. */
+mbg_status mbg_batch_shape(const mbg_batch* b, int32_t* block_size, int32_t* cached_index, int32_t* grid);
+
+/* ---- Learned surrogate for sweep screening ---------------------------------------------------
+ * No counterpart in the reference. An ensemble of MLPs (BF16 weights, FP32 accumulation, ReLU
+ * hidden layers, softmax output) trained on simulated (parameters -> output-state distribution)
+ * pairs; screening uses the ensemble mean and its spread (largest total-variation distance of a
+ * member from the mean). Parameters are flattened per layer as W [in][out] row-major, then b. */
+typedef struct mbg_surrogate mbg_surrogate;
+
+mbg_status mbg_surrogate_create(int32_t in_dim, int32_t hidden, int32_t hidden_layers, int32_t out_dim,
+                                int32_t ensemble, uint64_t seed, int32_t device, mbg_surrogate** out);
+void mbg_surrogate_destroy(mbg_surrogate* s);
+/* Trains every member for `epochs` passes over (x: n x in_dim, y: n x out_dim distributions) with
+ * Adam; *last_loss gets the mean cross-entropy of the last epoch. */
+mbg_status mbg_surrogate_train(mbg_surrogate* s, const float* x, const float* y, int64_t n, int32_t epochs,
+                               int32_t batch, float lr, uint64_t seed, float* last_loss);
+/* probs: n x out_dim ensemble-mean distributions; spread: n values (either may be NULL). */
+mbg_status mbg_surrogate_predict(mbg_surrogate* s, const float* x, int64_t n, float* probs, float* spread);
+int64_t mbg_surrogate_param_count(const mbg_surrogate* s);
+mbg_status mbg_surrogate_get_params(mbg_surrogate* s, int32_t member, float* params);
+mbg_status mbg_surrogate_set_params(mbg_surrogate* s, int32_t member, const float* params);
+/* Mean cross-entropy of member `member` on (x, y) and its gradient (param_count floats). */
+mbg_status mbg_surrogate_gradients(mbg_surrogate* s, int32_t member, const float* x, const float* y,
+                                   int32_t rows, float* loss, float* grads);
 
 /* No counterpart in the reference. Fixed-point aggregation for callers that must not allocate
  * device memory (a host that owns every allocation through its own pool, a latency-critical loop

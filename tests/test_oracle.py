@@ -116,3 +116,29 @@ def test_oracle_matches_reference_goldens(name, n):
         th = r.th[w] / scale
         assert abs(th - wg["th"]) <= 0.05 + 0.05 * wg["th"], f"{name} window {w} TH {th} vs {wg['th']}"
     print(f"{name}: worst deviation {worst:.2f} sigma")
+
+
+def test_mlp_oracle_gradient_matches_finite_differences():
+    from oracle import mlp
+    rng = np.random.default_rng(3)
+    dims = [5, 7, 6, 4]
+    p = mlp.init_params(dims, rng).astype(np.float64)
+    x = rng.normal(size=(9, 5))
+    y = rng.dirichlet(np.ones(4), size=9)
+    loss, g = mlp.loss_and_grad(p, dims, x, y, bf16=False)
+    eps = 1e-6
+    for i in rng.choice(len(p), 25, replace=False):
+        q = p.copy()
+        q[i] += eps
+        lp, _ = mlp.loss_and_grad(q, dims, x, y, bf16=False)
+        q[i] -= 2 * eps
+        lm, _ = mlp.loss_and_grad(q, dims, x, y, bf16=False)
+        assert abs((lp - lm) / (2 * eps) - g[i]) <= 1e-6 + 1e-5 * abs(g[i])
+
+
+def test_bf16_rounding_is_nearest_even():
+    from oracle import mlp
+    assert mlp.bf16_round(np.float32(1.0)) == 1.0
+    assert mlp.bf16_round(np.float32(1.0 + 2 ** -8)) == 1.0          # tie -> even
+    assert mlp.bf16_round(np.float32(1.0 + 3 * 2 ** -8)) == 1.0 + 2 ** -6
+    assert mlp.bf16_round(np.float32(-2.5)) == -2.5

@@ -23,12 +23,23 @@ STATUS = {0: "OK", 1: "ARG", 2: "IO", 3: "PARSE", 4: "MODEL", 5: "CUDA", 6: "JIT
 EXPORTS = (
     "mbg_last_error", "mbg_version", "mbg_device_count", "mbg_model_parse_files", "mbg_model_parse_strings",
     "mbg_model_destroy", "mbg_model_info_get", "mbg_model_node_name", "mbg_model_outputs", "mbg_model_rate",
+    "mbg_model_with_rate_scales",
     "mbg_model_jit_check",
     "mbg_sim_opts_default", "mbg_sim_create", "mbg_sim_destroy", "mbg_sim_run", "mbg_sim_summary",
     "mbg_sim_probtraj", "mbg_sim_probtraj_raw", "mbg_sim_final_states", "mbg_sim_fixed_points",
     "mbg_sim_trajectories", "mbg_write_probtraj_csv", "mbg_write_fp_csv", "mbg_print_results",
     "mbg_fixed_points_aggregate_noalloc",
+    "mbg_batch_opts_default", "mbg_batch_create", "mbg_batch_destroy", "mbg_batch_run", "mbg_batch_summary",
+    "mbg_batch_instance_summary", "mbg_batch_probtraj", "mbg_batch_probtraj_raw", "mbg_batch_final_states",
+    "mbg_batch_fixed_points", "mbg_batch_shape",
+    "mbg_surrogate_create", "mbg_surrogate_destroy", "mbg_surrogate_train", "mbg_surrogate_predict",
+    "mbg_surrogate_param_count", "mbg_surrogate_get_params", "mbg_surrogate_set_params", "mbg_surrogate_gradients",
 )
+
+
+class BatchOpts(ctypes.Structure):
+    _fields_ = [("device", ctypes.c_int32), ("max_steps", ctypes.c_uint32), ("block_size", ctypes.c_int32),
+                ("blocks_per_sm", ctypes.c_int32), ("autotune", ctypes.c_int32)]
 
 
 class MbgError(RuntimeError):
@@ -89,6 +100,7 @@ def lib():
             "mbg_model_outputs": (i32, [vp, dp, i32]),
             "mbg_model_rate": (ctypes.c_int, [vp, i32, dp, ctypes.POINTER(u64), ctypes.POINTER(ctypes.c_double)]),
             "mbg_model_jit_check": (ctypes.c_int, [vp, ctypes.POINTER(ctypes.c_double)]),
+            "mbg_model_with_rate_scales": (ctypes.c_int, [vp, dp, dp, ctypes.POINTER(vp)]),
             "mbg_sim_opts_default": (None, [ctypes.POINTER(SimOpts)]),
             "mbg_sim_create": (ctypes.c_int, [vp, ctypes.POINTER(SimOpts), ctypes.POINTER(vp)]),
             "mbg_sim_destroy": (None, [vp]),
@@ -103,6 +115,27 @@ def lib():
             "mbg_write_fp_csv": (ctypes.c_int, [vp, ctypes.c_char_p]),
             "mbg_print_results": (ctypes.c_int, [vp, ctypes.c_char_p]),
             "mbg_fixed_points_aggregate_noalloc": (ctypes.c_int, [vp, ctypes.c_uint32, i32, vp, vp, vp, vp]),
+            "mbg_batch_opts_default": (None, [ctypes.POINTER(BatchOpts)]),
+            "mbg_batch_create": (ctypes.c_int, [dp, i32, dp, dp, ctypes.POINTER(BatchOpts), ctypes.POINTER(vp)]),
+            "mbg_batch_destroy": (None, [vp]),
+            "mbg_batch_run": (ctypes.c_int, [vp, vp]),
+            "mbg_batch_summary": (ctypes.c_int, [vp, ctypes.POINTER(RunSummary)]),
+            "mbg_batch_instance_summary": (ctypes.c_int, [vp, i32, ctypes.POINTER(RunSummary)]),
+            "mbg_batch_probtraj": (ctypes.c_int, [vp, i32, dp, dp]),
+            "mbg_batch_probtraj_raw": (ctypes.c_int, [vp, i32, dp, dp]),
+            "mbg_batch_final_states": (ctypes.c_int, [vp, i32, dp]),
+            "mbg_batch_fixed_points": (ctypes.c_int, [vp, i32, dp, dp, ctypes.c_size_t,
+                                                      ctypes.POINTER(ctypes.c_size_t)]),
+            "mbg_batch_shape": (ctypes.c_int, [vp, ctypes.POINTER(i32), ctypes.POINTER(i32), ctypes.POINTER(i32)]),
+            "mbg_surrogate_create": (ctypes.c_int, [i32, i32, i32, i32, i32, u64, i32, ctypes.POINTER(vp)]),
+            "mbg_surrogate_destroy": (None, [vp]),
+            "mbg_surrogate_train": (ctypes.c_int, [vp, dp, dp, ctypes.c_int64, i32, i32, ctypes.c_float, u64,
+                                                   ctypes.POINTER(ctypes.c_float)]),
+            "mbg_surrogate_predict": (ctypes.c_int, [vp, dp, ctypes.c_int64, dp, dp]),
+            "mbg_surrogate_param_count": (ctypes.c_int64, [vp]),
+            "mbg_surrogate_get_params": (ctypes.c_int, [vp, i32, dp]),
+            "mbg_surrogate_set_params": (ctypes.c_int, [vp, i32, dp]),
+            "mbg_surrogate_gradients": (ctypes.c_int, [vp, i32, dp, dp, i32, ctypes.POINTER(ctypes.c_float), dp]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -160,6 +193,17 @@ class Model:
         r = ctypes.c_double()
         _check(lib().mbg_model_rate(self._h, int(node), _p(st), ctypes.byref(q), ctypes.byref(r)))
         return q.value, r.value
+
+    def with_rate_scales(self, up=None, down=None) -> "Model":
+        """Copy with node i's up rates times up[i] and down rates times down[i] (no re-parse)."""
+        u = None if up is None else np.ascontiguousarray(np.asarray(up, dtype=np.float64))
+        d = None if down is None else np.ascontiguousarray(np.asarray(down, dtype=np.float64))
+        for a in (u, d):
+            if a is not None and a.size != self.info.nodes:
+                raise ValueError("one scale per node")
+        h = ctypes.c_void_p()
+        _check(lib().mbg_model_with_rate_scales(self._h, _p(u), _p(d), ctypes.byref(h)))
+        return Model(h)
 
     def jit_check(self) -> float:
         ms = ctypes.c_double()
@@ -260,6 +304,140 @@ class Simulation:
     def close(self):
         if self._h:
             lib().mbg_sim_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Batch:
+    """Many instances (models, trajectory counts, seeds) run in one graph-captured launch."""
+
+    def __init__(self, models, n_traj=None, seeds=None, device=0, max_steps=0, block_size=0, blocks_per_sm=0,
+                 autotune=False):
+        o = BatchOpts()
+        lib().mbg_batch_opts_default(ctypes.byref(o))
+        o.device, o.max_steps, o.block_size, o.blocks_per_sm = device, max_steps, block_size, blocks_per_sm
+        o.autotune = 1 if autotune else 0
+        self.models = list(models)
+        handles = (ctypes.c_void_p * len(self.models))(*[m._h for m in self.models])
+        nt = None if n_traj is None else np.ascontiguousarray(np.asarray(n_traj, dtype=np.uint64))
+        sd = None if seeds is None else np.ascontiguousarray(np.asarray(seeds, dtype=np.uint64))
+        h = ctypes.c_void_p()
+        _check(lib().mbg_batch_create(ctypes.cast(handles, ctypes.c_void_p), len(self.models), _p(nt), _p(sd),
+                                      ctypes.byref(o), ctypes.byref(h)))
+        self._h = h
+        self.n_traj = [int(x) for x in nt] if nt is not None else [int(m.info.sample_count) for m in self.models]
+
+    def run(self, stream=None):
+        _check(lib().mbg_batch_run(self._h, ctypes.c_void_p(stream) if stream else None))
+        return self
+
+    def summary(self, instance=None) -> dict:
+        s = RunSummary()
+        if instance is None:
+            _check(lib().mbg_batch_summary(self._h, ctypes.byref(s)))
+        else:
+            _check(lib().mbg_batch_instance_summary(self._h, int(instance), ctypes.byref(s)))
+        return s.as_dict()
+
+    def shape(self):
+        b, c, g = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
+        _check(lib().mbg_batch_shape(self._h, ctypes.byref(b), ctypes.byref(c), ctypes.byref(g)))
+        return {"block_size": b.value, "cached_index": bool(c.value), "grid": g.value}
+
+    def probtraj(self, i):
+        info = self.models[i].info
+        P = np.zeros((info.windows, 1 << info.outputs), np.float64)
+        TH = np.zeros(info.windows, np.float64)
+        _check(lib().mbg_batch_probtraj(self._h, int(i), _p(P), _p(TH)))
+        return P, TH
+
+    def probtraj_raw(self, i):
+        info = self.models[i].info
+        P = np.zeros((info.windows, 1 << info.outputs), np.uint64)
+        TH = np.zeros(info.windows, np.uint64)
+        _check(lib().mbg_batch_probtraj_raw(self._h, int(i), _p(P), _p(TH)))
+        return P, TH
+
+    def final_states(self, i):
+        F = np.zeros(1 << self.models[i].info.outputs, np.float64)
+        _check(lib().mbg_batch_final_states(self._h, int(i), _p(F)))
+        return F
+
+    def fixed_points(self, i):
+        n = ctypes.c_size_t()
+        _check(lib().mbg_batch_fixed_points(self._h, int(i), None, None, 0, ctypes.byref(n)))
+        W = self.models[i].info.words
+        states = np.zeros((n.value, W), np.uint32)
+        probs = np.zeros(n.value, np.float64)
+        if n.value:
+            _check(lib().mbg_batch_fixed_points(self._h, int(i), _p(states), _p(probs), n.value, ctypes.byref(n)))
+        return states, probs
+
+    def close(self):
+        if self._h:
+            lib().mbg_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Surrogate:
+    """Ensemble of BF16 MLPs screening sweep points (mbg_surrogate_*)."""
+
+    def __init__(self, in_dim, out_dim, hidden=512, hidden_layers=3, ensemble=4, seed=0, device=0):
+        h = ctypes.c_void_p()
+        _check(lib().mbg_surrogate_create(in_dim, hidden, hidden_layers, out_dim, ensemble, seed, device,
+                                          ctypes.byref(h)))
+        self._h = h
+        self.in_dim, self.out_dim, self.hidden, self.hidden_layers = in_dim, out_dim, hidden, hidden_layers
+        self.ensemble = ensemble
+
+    def param_count(self):
+        return int(lib().mbg_surrogate_param_count(self._h))
+
+    def train(self, x, y, epochs=50, batch=256, lr=1e-3, seed=0):
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        y = np.ascontiguousarray(y, dtype=np.float32)
+        loss = ctypes.c_float()
+        _check(lib().mbg_surrogate_train(self._h, _p(x), _p(y), len(x), epochs, batch, lr, seed, ctypes.byref(loss)))
+        return loss.value
+
+    def predict(self, x):
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        probs = np.zeros((len(x), self.out_dim), np.float32)
+        spread = np.zeros(len(x), np.float32)
+        _check(lib().mbg_surrogate_predict(self._h, _p(x), len(x), _p(probs), _p(spread)))
+        return probs, spread
+
+    def params(self, member=0):
+        out = np.zeros(self.param_count(), np.float32)
+        _check(lib().mbg_surrogate_get_params(self._h, member, _p(out)))
+        return out
+
+    def set_params(self, member, params):
+        params = np.ascontiguousarray(params, dtype=np.float32)
+        _check(lib().mbg_surrogate_set_params(self._h, member, _p(params)))
+
+    def gradients(self, member, x, y):
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        y = np.ascontiguousarray(y, dtype=np.float32)
+        g = np.zeros(self.param_count(), np.float32)
+        loss = ctypes.c_float()
+        _check(lib().mbg_surrogate_gradients(self._h, member, _p(x), _p(y), len(x), ctypes.byref(loss), _p(g)))
+        return loss.value, g
+
+    def close(self):
+        if self._h:
+            lib().mbg_surrogate_destroy(self._h)
             self._h = None
 
     def __del__(self):

@@ -25,8 +25,9 @@ CUDA = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-HOST_SOURCES = ["parser.cpp", "model.cpp", "codegen.cpp", "jit.cpp", "sim.cpp", "output.cpp", "capi.cpp"]
-DEVICE_SOURCES = ["sim_aot.cu", "noalloc.cu"]
+HOST_SOURCES = ["parser.cpp", "model.cpp", "codegen.cpp", "jit.cpp", "sim.cpp", "batch.cpp", "surrogate.cpp",
+                "output.cpp", "capi.cpp"]
+DEVICE_SOURCES = ["sim_aot.cu", "noalloc.cu", "mlp.cu"]
 JIT_HEADERS = ["sim_types.h", "philox.h", "sim_core.cuh", "sim_thread.cuh"]
 
 

@@ -119,6 +119,7 @@ extern "C" mbg_status mbg_fixed_points_aggregate_noalloc(const uint32_t* states,
     if (words < 1 || !n_unique || (n_states > 0 && (!states || !unique_states || !counts)))
         return mbg::set_error(MBG_ERR_ARG, "mbg_fixed_points_aggregate_noalloc: null buffer or words < 1");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
+    cudaGetLastError();  // drop a stale non-sticky error of an earlier unrelated call
     unsigned* scratch = nullptr;
     cudaError_t e = scratch_for_current_device(&scratch);
     if (e == cudaSuccess) e = cudaMemsetAsync(scratch, 0xFF, sizeof(unsigned) * kNoallocSlots, st);

@@ -295,8 +295,26 @@ __device__ unsigned char warp_trajectory(const SimParams& p, const WarpSmem& m, 
             if (jj < 0) { status = TRAJ_ERROR; break; }
             g = tj * 32 + jj;
         }
-        int k;
-        {
+        int k = -1;
+        const unsigned aw = m.act[g];
+        if (!p.has_palette && __popc(aw) <= 4) {
+            // few active nodes in the group (the usual case once most nodes have frozen): walk
+            // them in node order; inactive nodes add nothing to the prefix
+            const unsigned sw = m.st[g];
+            unsigned rem = aw;
+            while (rem) {
+                const int b = __ffs(rem) - 1;
+                rem &= rem - 1u;
+                const int i = g * 32 + b;
+                const unsigned long long v = __ldg(&p.nodes[i].up + ((sw >> b) & 1u));
+                if (r < v) {
+                    k = i;
+                    break;
+                }
+                r -= v;
+            }
+            if (k < 0) { status = TRAJ_ERROR; break; }
+        } else {
             const int i = g * 32 + (int)lane;
             const int jj = warp_pick(i < p.n ? current_rate<IDX>(p, i, m) : 0ull, r, lane);
             if (jj < 0) { status = TRAJ_ERROR; break; }

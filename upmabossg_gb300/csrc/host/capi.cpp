@@ -4,12 +4,15 @@
 // (src/utils.cpp:3-30, src/kernel_compiler.cpp:10-31, src/parser/driver.cpp:54-60).
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstring>
 #include <fstream>
 #include <iostream>
 #include <memory>
 
+#include "batch.hpp"
 #include "sim.hpp"
+#include "surrogate.hpp"
 
 struct mbg_model {
     mbg::Model model;
@@ -19,6 +22,14 @@ struct mbg_model {
 
 struct mbg_sim {
     mbg::Sim sim;
+};
+
+struct mbg_batch {
+    mbg::Batch batch;
+};
+
+struct mbg_surrogate {
+    mbg::Surrogate s;
 };
 
 namespace {
@@ -180,6 +191,20 @@ mbg_status mbg_model_rate(const mbg_model* m, int32_t node, const uint8_t* state
     return MBG_OK;
 }
 
+mbg_status mbg_model_with_rate_scales(const mbg_model* base, const double* up_scale, const double* down_scale,
+                                      mbg_model** out) {
+    if (!base || !out) return fail(MBG_ERR_ARG, "null argument");
+    *out = nullptr;
+    std::unique_ptr<mbg_model> m(new mbg_model());
+    mbg_status st = guard([&] {
+        m->cm = mbg::rescale_model(base->cm, up_scale, down_scale);
+        m->names = base->names;
+    });
+    if (st != MBG_OK) return st;
+    *out = m.release();
+    return MBG_OK;
+}
+
 mbg_status mbg_model_jit_check(const mbg_model* m, double* compile_ms) {
     if (!m) return fail(MBG_ERR_ARG, "null model");
     return guard([&] {
@@ -313,6 +338,181 @@ mbg_status mbg_print_results(mbg_sim* s, const char* path) {
             mbg::print_results(s->sim, f);
         }
     });
+}
+
+
+void mbg_batch_opts_default(mbg_batch_opts* o) {
+    if (!o) return;
+    std::memset(o, 0, sizeof *o);
+}
+
+mbg_status mbg_batch_create(const mbg_model* const* models, int32_t n_models, const uint64_t* n_traj,
+                            const uint64_t* seeds, const mbg_batch_opts* o, mbg_batch** out) {
+    if (!models || n_models <= 0 || !out) return fail(MBG_ERR_ARG, "null or empty argument");
+    *out = nullptr;
+    mbg_batch_opts opts;
+    if (o) opts = *o;
+    else mbg_batch_opts_default(&opts);
+    std::vector<const mbg::CompiledModel*> cms;
+    for (int32_t i = 0; i < n_models; ++i) {
+        if (!models[i]) return fail(MBG_ERR_ARG, "null model in batch");
+        cms.push_back(&models[i]->cm);
+    }
+    std::vector<uint64_t> nt, sd;
+    if (n_traj) nt.assign(n_traj, n_traj + n_models);
+    if (seeds) sd.assign(seeds, seeds + n_models);
+    std::unique_ptr<mbg_batch> b(new mbg_batch());
+    mbg_status st = guard([&] { b->batch.create(cms, nt, sd, opts); });
+    if (st != MBG_OK) return st;
+    *out = b.release();
+    return MBG_OK;
+}
+
+void mbg_batch_destroy(mbg_batch* b) { delete b; }
+
+mbg_status mbg_batch_run(mbg_batch* b, void* stream) {
+    if (!b) return fail(MBG_ERR_ARG, "null batch");
+    return guard([&] { b->batch.run(static_cast<cudaStream_t>(stream)); });
+}
+
+mbg_status mbg_batch_summary(const mbg_batch* b, mbg_run_summary* out) {
+    if (!b || !out) return fail(MBG_ERR_ARG, "null argument");
+    if (!b->batch.ran) return fail(MBG_ERR_STATE, "summary requested before mbg_batch_run");
+    *out = b->batch.summary;
+    return MBG_OK;
+}
+
+mbg_status mbg_batch_instance_summary(const mbg_batch* b, int32_t i, mbg_run_summary* out) {
+    if (!b || !out) return fail(MBG_ERR_ARG, "null argument");
+    if (!b->batch.ran) return fail(MBG_ERR_STATE, "summary requested before mbg_batch_run");
+    if (i < 0 || i >= (int32_t)b->batch.inst.size()) return fail(MBG_ERR_ARG, "instance index out of range");
+    *out = b->batch.inst[i].summary;
+    return MBG_OK;
+}
+
+mbg_status mbg_batch_probtraj(mbg_batch* b, int32_t i, double* probs, double* tr_entropy) {
+    if (!b) return fail(MBG_ERR_ARG, "null batch");
+    return guard([&] {
+        b->batch.fetch(i);
+        const mbg::Batch::Inst& x = b->batch.inst[i];
+        const double n = (double)x.n_traj;
+        const double tick = x.cm.tick;
+        for (size_t k = 0; probs && k < x.hist.size(); ++k)
+            probs[k] = x.cm.discrete ? (double)x.hist[k] / n : ((double)x.hist[k] / 4294967296.0) / (n * tick);
+        for (int w = 0; tr_entropy && w < x.cm.windows; ++w) {
+            double v = ((double)x.th[w] / 4294967296.0) / n;
+            tr_entropy[w] = x.cm.discrete ? v : v / tick;
+        }
+    });
+}
+
+mbg_status mbg_batch_probtraj_raw(mbg_batch* b, int32_t i, uint64_t* sums, uint64_t* th_sums) {
+    if (!b) return fail(MBG_ERR_ARG, "null batch");
+    return guard([&] {
+        b->batch.fetch(i);
+        const mbg::Batch::Inst& x = b->batch.inst[i];
+        if (sums) std::memcpy(sums, x.hist.data(), x.hist.size() * 8);
+        if (th_sums) std::memcpy(th_sums, x.th.data(), x.th.size() * 8);
+    });
+}
+
+mbg_status mbg_batch_final_states(mbg_batch* b, int32_t i, double* probs) {
+    if (!b || !probs) return fail(MBG_ERR_ARG, "null argument");
+    return guard([&] {
+        b->batch.fetch(i);
+        const mbg::Batch::Inst& x = b->batch.inst[i];
+        for (size_t k = 0; k < x.fin.size(); ++k) probs[k] = (double)x.fin[k] / (double)x.n_traj;
+    });
+}
+
+mbg_status mbg_batch_fixed_points(mbg_batch* b, int32_t i, uint32_t* states, double* probs, size_t cap,
+                                  size_t* count) {
+    if (!b) return fail(MBG_ERR_ARG, "null batch");
+    return guard([&] {
+        b->batch.fetch(i);
+        const mbg::Batch::Inst& x = b->batch.inst[i];
+        const size_t W = (size_t)x.cm.words, nu = x.fp_cnt.size();
+        // reference order: highest state word first (state.h:38-45)
+        std::vector<size_t> order(nu);
+        for (size_t k = 0; k < nu; ++k) order[k] = k;
+        std::sort(order.begin(), order.end(), [&](size_t a, size_t c) {
+            for (size_t w = W; w-- > 0;)
+                if (x.fp_words[a * W + w] != x.fp_words[c * W + w]) return x.fp_words[a * W + w] < x.fp_words[c * W + w];
+            return false;
+        });
+        if (count) *count = nu;
+        for (size_t k = 0; k < nu && k < cap; ++k) {
+            if (states) std::memcpy(states + k * W, x.fp_words.data() + order[k] * W, W * 4);
+            if (probs) probs[k] = (double)x.fp_cnt[order[k]] / (double)x.n_traj;
+        }
+    });
+}
+
+mbg_status mbg_surrogate_create(int32_t in_dim, int32_t hidden, int32_t hidden_layers, int32_t out_dim,
+                                int32_t ensemble, uint64_t seed, int32_t device, mbg_surrogate** out) {
+    if (!out) return fail(MBG_ERR_ARG, "null output pointer");
+    *out = nullptr;
+    std::unique_ptr<mbg_surrogate> s(new mbg_surrogate());
+    mbg_status st = guard([&] {
+        int n = 0;
+        if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
+            cudaGetLastError();
+            throw mbg::CudaError("no CUDA device available");
+        }
+        if (device < 0 || device >= n) throw mbg::ArgError("device ordinal out of range");
+        s->s.create(in_dim, hidden, hidden_layers, out_dim, ensemble, seed, device);
+    });
+    if (st != MBG_OK) return st;
+    *out = s.release();
+    return MBG_OK;
+}
+
+void mbg_surrogate_destroy(mbg_surrogate* s) { delete s; }
+
+mbg_status mbg_surrogate_train(mbg_surrogate* s, const float* x, const float* y, int64_t n, int32_t epochs,
+                               int32_t batch, float lr, uint64_t seed, float* last_loss) {
+    if (!s || !x || !y) return fail(MBG_ERR_ARG, "null argument");
+    return guard([&] {
+        float l = s->s.train(x, y, n, epochs, batch, lr, seed);
+        if (last_loss) *last_loss = l;
+    });
+}
+
+mbg_status mbg_surrogate_predict(mbg_surrogate* s, const float* x, int64_t n, float* probs, float* spread) {
+    if (!s || !x) return fail(MBG_ERR_ARG, "null argument");
+    return guard([&] { s->s.predict(x, n, probs, spread); });
+}
+
+int64_t mbg_surrogate_param_count(const mbg_surrogate* s) { return s ? s->s.param_count() : -1; }
+
+mbg_status mbg_surrogate_get_params(mbg_surrogate* s, int32_t member, float* params) {
+    if (!s || !params) return fail(MBG_ERR_ARG, "null argument");
+    if (member < 0 || member >= s->s.ensemble) return fail(MBG_ERR_ARG, "ensemble member out of range");
+    return guard([&] { s->s.get_params(member, params, false); });
+}
+
+mbg_status mbg_surrogate_set_params(mbg_surrogate* s, int32_t member, const float* params) {
+    if (!s || !params) return fail(MBG_ERR_ARG, "null argument");
+    if (member < 0 || member >= s->s.ensemble) return fail(MBG_ERR_ARG, "ensemble member out of range");
+    return guard([&] { s->s.set_params(member, params); });
+}
+
+mbg_status mbg_surrogate_gradients(mbg_surrogate* s, int32_t member, const float* x, const float* y,
+                                   int32_t rows, float* loss, float* grads) {
+    if (!s || !x || !y || rows < 1) return fail(MBG_ERR_ARG, "null or empty argument");
+    return guard([&] {
+        float l = s->s.gradients(member, x, y, rows);
+        if (loss) *loss = l;
+        if (grads) s->s.get_params(member, grads, true);
+    });
+}
+
+mbg_status mbg_batch_shape(const mbg_batch* b, int32_t* block_size, int32_t* cached_index, int32_t* grid) {
+    if (!b) return fail(MBG_ERR_ARG, "null batch");
+    if (block_size) *block_size = b->batch.block;
+    if (cached_index) *cached_index = b->batch.cached_index ? 1 : 0;
+    if (grid) *grid = b->batch.grid;
+    return MBG_OK;
 }
 
 }  // extern "C"

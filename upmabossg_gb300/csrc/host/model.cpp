@@ -254,6 +254,34 @@ uint64_t quantize_rate(double r, int frac_bits) {
     return v;
 }
 
+static int frac_bits_for(double sum_max) {
+    // fixed-point scale: the sum of every node's largest rate stays below 2^61
+    int fb = 40;
+    if (sum_max > 0) fb = std::min(40, (int)std::floor(61.0 - std::log2(sum_max)));
+    if (fb < 8) throw Error("rates too large for the fixed-point representation");
+    return fb;
+}
+
+CompiledModel rescale_model(const CompiledModel& src, const double* up_scale, const double* down_scale) {
+    CompiledModel cm = src;
+    double sum_max = 0;
+    for (int i = 0; i < cm.n; ++i) {
+        CompiledNode& cn = cm.nodes[i];
+        if (cn.kind != NODE_BINARY) throw Error("rate scaling of multi-valued rates is not supported");
+        const double su = up_scale ? up_scale[i] : 1.0, sd = down_scale ? down_scale[i] : 1.0;
+        if (!(su >= 0) || !(sd >= 0) || std::isinf(su) || std::isinf(sd)) throw Error("invalid rate scale");
+        cn.up_real *= su;
+        cn.down_real *= sd;
+        sum_max += std::max(cn.up_real, cn.down_real);
+    }
+    cm.frac_bits = frac_bits_for(sum_max);
+    for (auto& cn : cm.nodes) {
+        cn.up = quantize_rate(cn.up_real, cm.frac_bits);
+        cn.down = quantize_rate(cn.down_real, cm.frac_bits);
+    }
+    return cm;
+}
+
 CompiledModel compile_model(const Model& m) {
     CompiledModel cm;
     cm.n = (int)m.nodes.size();
@@ -321,10 +349,7 @@ CompiledModel compile_model(const Model& m) {
         sum_max += mx;
     }
 
-    // Fixed-point scale: the sum of every node's largest rate stays below 2^61.
-    int fb = 40;
-    if (sum_max > 0) fb = std::min(40, (int)std::floor(61.0 - std::log2(sum_max)));
-    if (fb < 8) throw Error("rates too large for the fixed-point representation");
+    const int fb = frac_bits_for(sum_max);
     cm.frac_bits = fb;
 
     for (int i = 0; i < cm.n; ++i) {

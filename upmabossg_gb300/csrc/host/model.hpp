@@ -113,6 +113,9 @@ constexpr int kMaxPaletteRegs = 12;  // 2^13 palette indices per node at most
 constexpr int kMaxNodes = 65535;     // regulator indices are stored as uint16
 
 CompiledModel compile_model(const Model& m);
+// Copy of cm with node i's up rates times up_scale[i] and down rates times down_scale[i] (null:
+// 1), fixed-point scale and quantisation redone by compile_model's rule. Throws for palette nodes.
+CompiledModel rescale_model(const CompiledModel& cm, const double* up_scale, const double* down_scale);
 uint64_t quantize_rate(double r, int frac_bits);  // round-to-nearest, throws on overflow
 
 }  // namespace mbg

@@ -233,6 +233,7 @@ void Sim::create(const CompiledModel& model, const std::vector<std::string>& nod
 
 void Sim::run(cudaStream_t stream) {
     ck(cudaSetDevice(device), "cudaSetDevice");
+    cudaGetLastError();  // drop a stale non-sticky error of an earlier unrelated call
     const uint64_t S = 1ull << cm.n_out;
     ck(cudaEventRecord(ev0, stream), "cudaEventRecord");
     ck(cudaMemsetAsync(prm.hist, 0, cm.windows * S * 8, stream), "cudaMemsetAsync");
@@ -261,8 +262,8 @@ void Sim::run(cudaStream_t stream) {
        "cudaMemcpyAsync");
     ck(cudaStreamSynchronize(stream), "simulation kernel");
     float ms = 0, kms = 0;
-    cudaEventElapsedTime(&ms, ev0, ev1);
-    cudaEventElapsedTime(&kms, evk0, evk1);
+    ck(cudaEventElapsedTime(&ms, ev0, ev1), "cudaEventElapsedTime");
+    ck(cudaEventElapsedTime(&kms, evk0, evk1), "cudaEventElapsedTime");
     summary = mbg_run_summary{};
     summary.trajectories = n_traj;
     summary.transitions = hc[CNT_TRANSITIONS];

@@ -1,0 +1,318 @@
+// Learned surrogate for sweep screening: an ensemble of BF16 MLPs (FP32 accumulation and FP32
+// master weights) mapping a sweep point's parameters to an output-state distribution. Training
+// (softmax cross-entropy against simulated distributions, Adam) and inference run on the project's
+// own kernels (device/mlp.cu). The reference has no surrogate; this is an addition on top of the
+// simulator, which stays the judge: every point a screen reports is re-simulated.
+#include "surrogate.hpp"
+
+#include <cmath>
+#include <cstring>
+#include <numeric>
+#include <random>
+
+namespace mbg {
+
+namespace {
+
+void ck(cudaError_t e, const char* what) {
+    if (e != cudaSuccess) throw CudaError(std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+}  // namespace
+
+template <class T>
+T* Surrogate::alloc(size_t n) {
+    void* p = nullptr;
+    cudaError_t e = cudaMalloc(&p, (n ? n : 1) * sizeof(T));
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        throw NoMemError(std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    }
+    owned.push_back(p);
+    return static_cast<T*>(p);
+}
+
+Surrogate::~Surrogate() {
+    for (void* p : owned) cudaFree(p);
+    if (stream) cudaStreamDestroy(stream);
+}
+
+void Surrogate::create(int in, int hid, int n_hidden, int out, int ens, uint64_t seed, int dev) {
+    if (in < 1 || hid < 1 || n_hidden < 1 || out < 2 || out > 1024 || ens < 1 || ens > 16)
+        throw ArgError("surrogate dimensions out of range");
+    in_dim = in;
+    hidden = hid;
+    hidden_layers = n_hidden;
+    out_dim = out;
+    ensemble = ens;
+    device = dev;
+    ck(cudaSetDevice(device), "cudaSetDevice");
+    ck(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "cudaStreamCreate");
+    std::mt19937_64 rng(seed);
+    members.resize(ens);
+    for (int e = 0; e < ens; ++e) {
+        Member& mb = members[e];
+        for (int l = 0; l <= n_hidden; ++l) {
+            Layer L;
+            L.in = l == 0 ? in : hid;
+            L.out = l == n_hidden ? out : hid;
+            const size_t nw = (size_t)L.in * L.out;
+            L.w = alloc<float>(nw);
+            L.b = alloc<float>(L.out);
+            L.wb = alloc<__nv_bfloat16>(nw);
+            L.gw = alloc<float>(nw);
+            L.gb = alloc<float>(L.out);
+            L.mw = alloc<float>(nw);
+            L.vw = alloc<float>(nw);
+            L.mb = alloc<float>(L.out);
+            L.vb = alloc<float>(L.out);
+            // He initialisation for the ReLU layers, Glorot-like for the output layer
+            const double sd = l == n_hidden ? std::sqrt(1.0 / L.in) : std::sqrt(2.0 / L.in);
+            std::normal_distribution<double> nd(0.0, sd);
+            std::vector<float> hw(nw), hb(L.out, 0.f);
+            for (auto& x : hw) x = (float)nd(rng);
+            ck(cudaMemcpy(L.w, hw.data(), nw * 4, cudaMemcpyHostToDevice), "cudaMemcpy H2D");
+            ck(cudaMemcpy(L.b, hb.data(), L.out * 4, cudaMemcpyHostToDevice), "cudaMemcpy H2D");
+            ck(cudaMemset(L.mw, 0, nw * 4), "cudaMemset");
+            ck(cudaMemset(L.vw, 0, nw * 4), "cudaMemset");
+            ck(cudaMemset(L.mb, 0, L.out * 4), "cudaMemset");
+            ck(cudaMemset(L.vb, 0, L.out * 4), "cudaMemset");
+            ck(mlp_to_bf16(L.w, L.wb, (long long)nw, stream), "mlp_to_bf16");
+            mb.layers.push_back(L);
+        }
+    }
+    ck(cudaStreamSynchronize(stream), "surrogate init");
+}
+
+void Surrogate::ensure_batch(int rows) {
+    if (rows <= cap_rows) return;
+    cap_rows = rows;
+    xb = alloc<__nv_bfloat16>((size_t)rows * in_dim);
+    xf = alloc<float>((size_t)rows * in_dim);
+    yt = alloc<float>((size_t)rows * out_dim);
+    acts.clear();
+    for (int l = 0; l < hidden_layers; ++l) acts.push_back(alloc<__nv_bfloat16>((size_t)rows * hidden));
+    logits = alloc<float>((size_t)rows * out_dim);
+    probs = alloc<float>((size_t)rows * out_dim * ensemble);
+    dlogits = alloc<__nv_bfloat16>((size_t)rows * out_dim);
+    da = alloc<float>((size_t)rows * hidden);
+    dh = alloc<__nv_bfloat16>((size_t)rows * hidden);
+    dh2 = alloc<__nv_bfloat16>((size_t)rows * hidden);
+    mean = alloc<float>((size_t)rows * out_dim);
+    spread = alloc<float>((size_t)rows);
+    loss = alloc<float>(1);
+}
+
+// logits = MLP(xb) for `rows` rows of member e; hidden activations kept for the backward pass.
+void Surrogate::forward(int e, int rows) {
+    Member& mb = members[e];
+    const __nv_bfloat16* a = xb;
+    int a_cols = in_dim;
+    for (int l = 0; l <= hidden_layers; ++l) {
+        const Layer& L = mb.layers[l];
+        GemmArgs g;
+        g.M = rows;
+        g.N = L.out;
+        g.K = L.in;
+        g.A = a;
+        g.a_m = a_cols;
+        g.a_k = 1;
+        g.B = L.wb;
+        g.b_k = L.out;
+        g.b_n = 1;
+        g.bias = L.b;
+        if (l < hidden_layers) {
+            g.relu = 1;
+            g.Cb = acts[l];
+            g.ldcb = L.out;
+        } else {
+            g.C = logits;
+            g.ldc = L.out;
+        }
+        ck(mlp_gemm(g, stream), "mlp_gemm forward");
+        if (l < hidden_layers) {
+            a = acts[l];
+            a_cols = L.out;
+        }
+    }
+}
+
+// Gradients of the mean cross-entropy of member e on `rows` rows (targets in yt) into gw, gb;
+// the summed loss is added to *loss.
+void Surrogate::backward(int e, int rows) {
+    Member& mb = members[e];
+    ck(mlp_softmax_xent(logits, rows, out_dim, yt, 1.f / (float)rows, nullptr, dlogits, loss, stream),
+       "mlp_softmax_xent");
+    const __nv_bfloat16* d = dlogits;  // gradient w.r.t. the current layer's output
+    int d_cols = out_dim;
+    __nv_bfloat16* bufs[2] = {dh, dh2};
+    for (int l = hidden_layers; l >= 0; --l) {
+        Layer& L = mb.layers[l];
+        const __nv_bfloat16* a_in = l == 0 ? xb : acts[l - 1];
+        // dW = a_in^T . d
+        GemmArgs gw;
+        gw.M = L.in;
+        gw.N = L.out;
+        gw.K = rows;
+        gw.A = a_in;
+        gw.a_m = 1;
+        gw.a_k = L.in;
+        gw.B = d;
+        gw.b_k = d_cols;
+        gw.b_n = 1;
+        gw.C = L.gw;
+        gw.ldc = L.out;
+        ck(mlp_gemm(gw, stream), "mlp_gemm weight gradient");
+        ck(mlp_bias_grad(d, rows, L.out, L.gb, stream), "mlp_bias_grad");
+        if (l > 0) {
+            // da = d . W^T, then through the ReLU of the layer below
+            GemmArgs gd;
+            gd.M = rows;
+            gd.N = L.in;
+            gd.K = L.out;
+            gd.A = d;
+            gd.a_m = d_cols;
+            gd.a_k = 1;
+            gd.B = L.wb;
+            gd.b_k = 1;
+            gd.b_n = L.out;
+            gd.C = da;
+            gd.ldc = L.in;
+            ck(mlp_gemm(gd, stream), "mlp_gemm data gradient");
+            __nv_bfloat16* next = bufs[l & 1];
+            ck(mlp_relu_backward(da, acts[l - 1], next, (long long)rows * L.in, stream), "mlp_relu_backward");
+            d = next;
+            d_cols = L.in;
+        }
+    }
+}
+
+void Surrogate::adam_step(int e, float lr) {
+    Member& mb = members[e];
+    ++mb.step;
+    for (Layer& L : mb.layers) {
+        ck(mlp_adam(L.w, L.gw, L.mw, L.vw, L.wb, (long long)L.in * L.out, lr, 0.9f, 0.999f, 1e-8f, mb.step, stream),
+           "mlp_adam");
+        ck(mlp_adam(L.b, L.gb, L.mb, L.vb, nullptr, L.out, lr, 0.9f, 0.999f, 1e-8f, mb.step, stream), "mlp_adam");
+    }
+}
+
+float Surrogate::train(const float* x, const float* y, int64_t n, int epochs, int batch, float lr, uint64_t seed) {
+    if (n < 1 || batch < 1 || epochs < 1) throw ArgError("empty training set or batch");
+    ck(cudaSetDevice(device), "cudaSetDevice");
+    batch = (int)std::min<int64_t>(batch, n);
+    ensure_batch(batch);
+    float* dx = alloc<float>((size_t)n * in_dim);
+    float* dy = alloc<float>((size_t)n * out_dim);
+    int* didx = alloc<int>((size_t)n);
+    ck(cudaMemcpy(dx, x, (size_t)n * in_dim * 4, cudaMemcpyHostToDevice), "cudaMemcpy H2D");
+    ck(cudaMemcpy(dy, y, (size_t)n * out_dim * 4, cudaMemcpyHostToDevice), "cudaMemcpy H2D");
+    std::mt19937_64 rng(seed);
+    std::vector<int> perm(n);
+    const int steps = (int)(n / batch);
+    float last = 0.f;
+    for (int e = 0; e < ensemble; ++e) {
+        for (int ep = 0; ep < epochs; ++ep) {
+            std::iota(perm.begin(), perm.end(), 0);
+            std::shuffle(perm.begin(), perm.end(), rng);
+            ck(cudaMemcpyAsync(didx, perm.data(), (size_t)n * 4, cudaMemcpyHostToDevice, stream), "cudaMemcpyAsync");
+            ck(cudaMemsetAsync(loss, 0, 4, stream), "cudaMemsetAsync");
+            for (int s = 0; s < steps; ++s) {
+                ck(mlp_gather_rows(dx, didx + (size_t)s * batch, batch, in_dim, nullptr, xb, stream), "gather x");
+                ck(mlp_gather_rows(dy, didx + (size_t)s * batch, batch, out_dim, yt, nullptr, stream), "gather y");
+                forward(e, batch);
+                backward(e, batch);
+                adam_step(e, lr);
+            }
+            if (ep == epochs - 1) {
+                float h = 0.f;
+                ck(cudaMemcpyAsync(&h, loss, 4, cudaMemcpyDeviceToHost, stream), "cudaMemcpyAsync");
+                ck(cudaStreamSynchronize(stream), "training");
+                last += h / (float)(steps * batch) / (float)ensemble;
+            }
+        }
+    }
+    ck(cudaStreamSynchronize(stream), "training");
+    // the training set buffers are only needed during this call
+    for (void* p : {(void*)dx, (void*)dy, (void*)didx}) {
+        cudaFree(p);
+        owned.erase(std::find(owned.begin(), owned.end(), p));
+    }
+    return last;
+}
+
+void Surrogate::predict(const float* x, int64_t n, float* out_probs, float* out_spread, int chunk) {
+    ck(cudaSetDevice(device), "cudaSetDevice");
+    chunk = (int)std::max<int64_t>(1, std::min<int64_t>(chunk, n));
+    ensure_batch(chunk);
+    for (int64_t r0 = 0; r0 < n; r0 += chunk) {
+        const int rows = (int)std::min<int64_t>(chunk, n - r0);
+        ck(cudaMemcpyAsync(xf, x + r0 * in_dim, (size_t)rows * in_dim * 4, cudaMemcpyHostToDevice, stream),
+           "cudaMemcpyAsync");
+        ck(mlp_to_bf16(xf, xb, (long long)rows * in_dim, stream), "mlp_to_bf16");
+        for (int e = 0; e < ensemble; ++e) {
+            forward(e, rows);
+            ck(mlp_softmax_xent(logits, rows, out_dim, nullptr, 0.f, probs + (size_t)e * rows * out_dim, nullptr,
+                                nullptr, stream),
+               "mlp_softmax");
+        }
+        ck(mlp_ensemble_stats(probs, ensemble, rows, out_dim, mean, spread, stream), "mlp_ensemble_stats");
+        if (out_probs)
+            ck(cudaMemcpyAsync(out_probs + r0 * out_dim, mean, (size_t)rows * out_dim * 4, cudaMemcpyDeviceToHost,
+                               stream),
+               "cudaMemcpyAsync");
+        if (out_spread)
+            ck(cudaMemcpyAsync(out_spread + r0, spread, (size_t)rows * 4, cudaMemcpyDeviceToHost, stream),
+               "cudaMemcpyAsync");
+        ck(cudaStreamSynchronize(stream), "prediction");
+    }
+}
+
+int64_t Surrogate::param_count() const {
+    int64_t c = 0;
+    for (const Layer& L : members[0].layers) c += (int64_t)L.in * L.out + L.out;
+    return c;
+}
+
+void Surrogate::get_params(int e, float* dst, bool grads) {
+    ck(cudaSetDevice(device), "cudaSetDevice");
+    ck(cudaStreamSynchronize(stream), "surrogate");
+    for (const Layer& L : members.at(e).layers) {
+        const size_t nw = (size_t)L.in * L.out;
+        ck(cudaMemcpy(dst, grads ? L.gw : L.w, nw * 4, cudaMemcpyDeviceToHost), "cudaMemcpy D2H");
+        dst += nw;
+        ck(cudaMemcpy(dst, grads ? L.gb : L.b, L.out * 4, cudaMemcpyDeviceToHost), "cudaMemcpy D2H");
+        dst += L.out;
+    }
+}
+
+void Surrogate::set_params(int e, const float* src) {
+    ck(cudaSetDevice(device), "cudaSetDevice");
+    for (Layer& L : members.at(e).layers) {
+        const size_t nw = (size_t)L.in * L.out;
+        ck(cudaMemcpy(L.w, src, nw * 4, cudaMemcpyHostToDevice), "cudaMemcpy H2D");
+        src += nw;
+        ck(cudaMemcpy(L.b, src, L.out * 4, cudaMemcpyHostToDevice), "cudaMemcpy H2D");
+        src += L.out;
+        ck(mlp_to_bf16(L.w, L.wb, (long long)nw, stream), "mlp_to_bf16");
+    }
+    ck(cudaStreamSynchronize(stream), "surrogate");
+}
+
+float Surrogate::gradients(int e, const float* x, const float* y, int rows) {
+    ck(cudaSetDevice(device), "cudaSetDevice");
+    if (e < 0 || e >= ensemble) throw ArgError("ensemble member out of range");
+    ensure_batch(rows);
+    ck(cudaMemcpyAsync(xf, x, (size_t)rows * in_dim * 4, cudaMemcpyHostToDevice, stream), "cudaMemcpyAsync");
+    ck(mlp_to_bf16(xf, xb, (long long)rows * in_dim, stream), "mlp_to_bf16");
+    ck(cudaMemcpyAsync(yt, y, (size_t)rows * out_dim * 4, cudaMemcpyHostToDevice, stream), "cudaMemcpyAsync");
+    ck(cudaMemsetAsync(loss, 0, 4, stream), "cudaMemsetAsync");
+    forward(e, rows);
+    backward(e, rows);
+    float h = 0.f;
+    ck(cudaMemcpyAsync(&h, loss, 4, cudaMemcpyDeviceToHost, stream), "cudaMemcpyAsync");
+    ck(cudaStreamSynchronize(stream), "gradients");
+    return h / (float)rows;
+}
+
+}  // namespace mbg

@@ -1,0 +1,67 @@
+// Ensemble of BF16 MLPs used to screen sweep points (surrogate.cpp).
+#pragma once
+
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdint>
+#include <vector>
+
+#include "../device/mlp.h"
+#include "sim_host.hpp"
+
+namespace mbg {
+
+class Surrogate {
+public:
+    struct Layer {
+        int in = 0, out = 0;
+        float *w = nullptr, *b = nullptr;  // FP32 master weights, W row-major [in][out]
+        __nv_bfloat16* wb = nullptr;       // BF16 copy used by the GEMMs
+        float *gw = nullptr, *gb = nullptr;
+        float *mw = nullptr, *vw = nullptr, *mb = nullptr, *vb = nullptr;  // Adam moments
+    };
+    struct Member {
+        std::vector<Layer> layers;
+        int step = 0;
+    };
+
+    ~Surrogate();
+    void create(int in_dim, int hidden, int hidden_layers, int out_dim, int ensemble, uint64_t seed, int device);
+    float train(const float* x, const float* y, int64_t n, int epochs, int batch, float lr, uint64_t seed);
+    void predict(const float* x, int64_t n, float* probs, float* spread, int chunk = 8192);
+    float gradients(int member, const float* x, const float* y, int rows);
+    int64_t param_count() const;
+    void get_params(int member, float* dst, bool grads);
+    void set_params(int member, const float* src);
+
+    int in_dim = 0, hidden = 0, hidden_layers = 0, out_dim = 0, ensemble = 0, device = 0;
+    std::vector<Member> members;
+
+private:
+    template <class T>
+    T* alloc(size_t n);
+    void ensure_batch(int rows);
+    void forward(int member, int rows);
+    void backward(int member, int rows);
+    void adam_step(int member, float lr);
+
+    cudaStream_t stream = nullptr;
+    int cap_rows = 0;
+    __nv_bfloat16* xb = nullptr;
+    float* xf = nullptr;
+    float* yt = nullptr;
+    std::vector<__nv_bfloat16*> acts;
+    float* logits = nullptr;
+    float* probs = nullptr;
+    __nv_bfloat16* dlogits = nullptr;
+    float* da = nullptr;
+    __nv_bfloat16 *dh = nullptr, *dh2 = nullptr;
+    float* mean = nullptr;
+    float* spread = nullptr;
+    float* loss = nullptr;
+    std::vector<void*> owned;
+};
+
+}  // namespace mbg
