@@ -254,8 +254,7 @@ def run_ours(args):
         dist.init_process_group("nccl")
     net = make_network(args.workload)
     n_total = args.n_traj or net.sample_count
-    n_rank = n_total // ws
-    base = rank * n_rank
+    base, n_rank = mbg.shard_range(n_total, rank, ws)
     bnd, cfg = net.bnd(), net.cfg()
     model = mbg.Model.from_strings(bnd, cfg)
     sim = mbg.Simulation(model, n_traj=n_rank, traj_base=base, device=local, layout=args.layout)

@@ -445,3 +445,12 @@ class Surrogate:
             self.close()
         except Exception:
             pass
+
+
+def shard_range(n_traj: int, rank: int, world: int):
+    """(first trajectory id, count) of `rank`'s share of n_traj trajectories over `world` ranks.
+    Trajectories are keyed by id, so the union of the shards equals one run over all ids."""
+    if world < 1 or not 0 <= rank < world:
+        raise ValueError("rank outside the world")
+    q, r = divmod(int(n_traj), world)
+    return rank * q + min(rank, r), q + (1 if rank < r else 0)

@@ -11,6 +11,8 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <map>
+#include <mutex>
 
 #include "../device/kernels.h"
 
@@ -203,17 +205,81 @@ void Sim::create(const CompiledModel& model, const std::vector<std::string>& nod
     ck(cudaEventCreate(&evk0), "cudaEventCreate");
     ck(cudaEventCreate(&evk1), "cudaEventCreate");
 
-    // layout
-    int cutoff = o.thread_cutoff > 0 ? o.thread_cutoff : 96;
-    layout = o.layout;
-    if (layout == MBG_LAYOUT_AUTO) layout = cm.n <= cutoff ? MBG_LAYOUT_THREAD : MBG_LAYOUT_WARP;
-    if (layout == MBG_LAYOUT_THREAD && cm.words > 16) throw ModelError("thread layout supports at most 512 nodes");
-    if (layout == MBG_LAYOUT_WARP && cm.n_out > 32) throw ModelError("warp layout supports at most 32 outputs");
-    block = o.block_size > 0 ? o.block_size : 256;
-    if (block % 32 != 0 || block > 256) throw ArgError("block_size must be a multiple of 32, at most 256");
+    if (o.block_size && (o.block_size % 32 != 0 || o.block_size > 256))
+        throw ArgError("block_size must be a multiple of 32, at most 256");
+    if (o.layout == MBG_LAYOUT_THREAD && cm.words > 16) throw ModelError("thread layout supports at most 512 nodes");
+    if (o.layout == MBG_LAYOUT_WARP && cm.n_out > 32) throw ModelError("warp layout supports at most 32 outputs");
+    if (o.layout != MBG_LAYOUT_AUTO) {
+        setup_layout(o.layout, o.block_size > 0 ? o.block_size : 256);
+    } else if (o.thread_cutoff > 0 || cm.words > 16 || cm.n_out > 32) {
+        const int lay = cm.words <= 16 && (cm.n <= o.thread_cutoff || cm.n_out > 32) ? MBG_LAYOUT_THREAD
+                                                                                     : MBG_LAYOUT_WARP;
+        setup_layout(lay, o.block_size > 0 ? o.block_size : 256);
+    } else {
+        autotune();
+    }
+}
+
+namespace {
+// Autotuned launch shapes per (model size class ceil(log2 N), pilot size class ceil(log2 pilot)),
+// shared by all simulations of the process: layout and threads per block.
+std::mutex g_tune_mu;
+std::map<std::pair<int, int>, std::pair<int, int>> g_tuned;
+
+int ceil_log2(uint64_t x) {
+    int c = 0;
+    while ((1ull << c) < x) ++c;
+    return c;
+}
+}  // namespace
+
+void Sim::autotune() {
+    // the pilot is large enough to fill the GPU in either layout (or the whole run when smaller),
+    // so that the choice reflects occupancy as well as per-transition cost
+    const uint64_t pilot = std::min<uint64_t>(n_traj, 1u << 17);
+    const std::pair<int, int> cls{ceil_log2((uint64_t)cm.n), ceil_log2(pilot)};
+    {
+        std::lock_guard<std::mutex> lock(g_tune_mu);
+        auto it = g_tuned.find(cls);
+        if (it != g_tuned.end()) {
+            setup_layout(it->second.first, opts.block_size > 0 ? opts.block_size : it->second.second);
+            return;
+        }
+    }
+    // time both layouts and two block sizes on the pilot
+    const uint64_t saved_n = prm.n_traj;
+    prm.n_traj = pilot;
+    double best = -1;
+    int best_layout = MBG_LAYOUT_WARP, best_block = 256;
+    for (int lay : {MBG_LAYOUT_THREAD, MBG_LAYOUT_WARP}) {
+        for (int blk : {128, 256}) {
+            if (opts.block_size > 0 && blk != opts.block_size) continue;
+            setup_layout(lay, blk);
+            run(nullptr);  // warm-up (and JIT load)
+            run(nullptr);
+            const double rate = (double)summary.transitions / std::max(summary.kernel_ms, 1e-3);
+            if (rate > best) {
+                best = rate;
+                best_layout = lay;
+                best_block = blk;
+            }
+        }
+    }
+    prm.n_traj = saved_n;
+    ran = false;
+    setup_layout(best_layout, best_block);
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    g_tuned[cls] = {best_layout, best_block};
+}
+
+void Sim::setup_layout(int lay, int blk) {
+    layout = lay;
+    block = blk;
     int bps = 0;
     if (layout == MBG_LAYOUT_THREAD) {
-        thread_kernel = jit_thread_kernel(generate_thread_model(cm, dl), jit_ms);
+        double ms = 0;
+        thread_kernel = jit_thread_kernel(generate_thread_model(cm, dl), ms);
+        jit_ms += ms;
         smem = 0;
         ck(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, (const void*)thread_kernel, block, 0),
            "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
@@ -227,7 +293,7 @@ void Sim::create(const CompiledModel& model, const std::vector<std::string>& nod
         ck(sim_warp_occupancy(cached_index, block, smem, &bps), "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
     }
     if (bps < 1) throw CudaError("kernel cannot be resident with this block size");
-    if (o.blocks_per_sm > 0) bps = std::min(bps, (int)o.blocks_per_sm);
+    if (opts.blocks_per_sm > 0) bps = std::min(bps, (int)opts.blocks_per_sm);
     grid = sms * bps;
 }
 

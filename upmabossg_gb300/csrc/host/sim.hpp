@@ -23,6 +23,10 @@ public:
     void create(const CompiledModel& cm, const std::vector<std::string>& names, const mbg_sim_opts& o);
     void run(cudaStream_t stream);
     void fetch();  // copies results to the host vectors below
+    // Chooses kernel, block size, shared memory and grid for a layout.
+    void setup_layout(int layout, int block);
+    // AUTO layout: times both layouts on a pilot subset once per model size class.
+    void autotune();
 
     CompiledModel cm;
     std::vector<std::string> names;
