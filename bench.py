@@ -335,7 +335,7 @@ def run_ours(args):
         "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "u64", "data": "synthetic",
         "config": {"workload": WORKLOADS[args.workload], "trajectories": n_total,
-                   "transitions_per_step": trans_step * ws, "layout": ["", "thread", "warp"][summary["layout"]],
+                   "transitions_per_step": trans_step * ws, "layout": ["", "thread", "warp", "lane"][summary["layout"]],
                    "l2": "flushed between steps (256 MiB write)", "wall_s": wall},
         "e2e": {"value": e2e_value, "unit": "transitions/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "ms_per_step": statistics.mean(e2e_ms),

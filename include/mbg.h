@@ -62,9 +62,11 @@ typedef struct {
     uint64_t sample_count, seed;
 } mbg_model_info;
 
-/* Trajectory layout: 0 auto (autotuned cutoff), 1 thread per trajectory (NVRTC-compiled
- * evaluator), 2 warp per trajectory (table driven). */
-enum { MBG_LAYOUT_AUTO = 0, MBG_LAYOUT_THREAD = 1, MBG_LAYOUT_WARP = 2 };
+/* Trajectory layout: 0 auto (timed on a pilot, once per model size class), 1 thread per
+ * trajectory (NVRTC-compiled evaluator, state in registers, every rate re-evaluated per step),
+ * 2 warp per trajectory (table driven), 3 lane: thread per trajectory, table driven, state in
+ * shared memory, rates updated incrementally. All four give identical results. */
+enum { MBG_LAYOUT_AUTO = 0, MBG_LAYOUT_THREAD = 1, MBG_LAYOUT_WARP = 2, MBG_LAYOUT_LANE = 3 };
 
 typedef struct {
     uint64_t n_traj;           /* 0: cfg sample_count */
@@ -77,7 +79,10 @@ typedef struct {
     uint32_t max_steps;        /* per-trajectory step cap; 0: none */
     int32_t block_size;        /* threads per block; 0: default */
     int32_t blocks_per_sm;     /* 0: occupancy limit */
-    int32_t thread_cutoff;     /* AUTO: largest N run thread per trajectory; 0: default */
+    int32_t thread_cutoff;     /* AUTO: > 0 runs N <= cutoff thread per trajectory and the rest warp
+                                  per trajectory without timing; 0: autotune */
+    int32_t lane_update;       /* LANE: readers of a flipped node updated 0: warp-cooperatively
+                                  (default), 1: by their own lane; AUTO times both */
 } mbg_sim_opts;
 
 typedef struct {

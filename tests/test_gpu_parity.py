@@ -17,64 +17,80 @@ from helpers import compare_histograms, compare_trajectories, golden_model, run_
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("layout", [mbg.LAYOUT_THREAD, mbg.LAYOUT_WARP])
+ALL_LAYOUTS = [mbg.LAYOUT_THREAD, mbg.LAYOUT_WARP, mbg.LAYOUT_LANE, "lane-serial"]
+
+
+def layout_kw(layout):
+    """Simulation keyword arguments for a layout id; "lane-serial" is the lane layout with each
+    lane updating its own readers."""
+    if layout == "lane-serial":
+        return {"layout": mbg.LAYOUT_LANE, "lane_update": 1}
+    return {"layout": layout}
+
+
+@pytest.mark.parametrize("layout", ALL_LAYOUTS)
 def test_small_network_parity(layout):
     net = synth.small()
     bnd, cfg = net.bnd(), net.cfg()
     n = 4000
-    model, sim = run_device(bnd, cfg, n, layout=layout)
+    model, sim = run_device(bnd, cfg, n, **layout_kw(layout))
     orc = run_oracle(bnd, cfg, model, n)
     s = sim.summary()
-    assert s["layout"] == layout
+    assert s["layout"] == layout_kw(layout)["layout"]
     assert s["transitions"] == orc.counters["transitions"] or orc.counters["time_ties"] > 0
     compare_trajectories(sim, orc)
     compare_histograms(model, sim, orc, n)
 
 
-def test_medium_network_parity():
+@pytest.mark.parametrize("layout", [mbg.LAYOUT_WARP, mbg.LAYOUT_LANE, "lane-serial"])
+def test_medium_network_parity(layout):
     net = synth.medium()
     bnd, cfg = net.bnd(), net.cfg(sample_count=192)
-    model, sim = run_device(bnd, cfg, 192, layout=mbg.LAYOUT_WARP)
+    model, sim = run_device(bnd, cfg, 192, **layout_kw(layout))
+    assert sim.summary()["layout"] == layout_kw(layout)["layout"]
     orc = run_oracle(bnd, cfg, model, 192)
     compare_trajectories(sim, orc)
     compare_histograms(model, sim, orc, 192)
 
 
-@pytest.mark.parametrize("layout", [mbg.LAYOUT_THREAD, mbg.LAYOUT_WARP])
+@pytest.mark.parametrize("layout", ALL_LAYOUTS)
 def test_mid_network_parity(layout):
     net = synth.sweep_instance(2)  # 268 nodes, 8 outputs, lognormal rates
     bnd, cfg = net.bnd(), net.cfg(sample_count=400)
-    model, sim = run_device(bnd, cfg, 400, layout=layout)
+    model, sim = run_device(bnd, cfg, 400, **layout_kw(layout))
     orc = run_oracle(bnd, cfg, model, 400)
     compare_trajectories(sim, orc)
     compare_histograms(model, sim, orc, 400)
 
 
-def test_large_network_parity():
+@pytest.mark.parametrize("layout", [mbg.LAYOUT_WARP, mbg.LAYOUT_LANE])
+def test_large_network_parity(layout):
     net = synth.large()
     bnd, cfg = net.bnd(), net.cfg(sample_count=24, max_time=5)
-    model, sim = run_device(bnd, cfg, 24, layout=mbg.LAYOUT_WARP)
+    model, sim = run_device(bnd, cfg, 24, layout=layout)
     orc = run_oracle(bnd, cfg, model, 24)
     compare_trajectories(sim, orc)
     compare_histograms(model, sim, orc, 24)
 
 
+@pytest.mark.parametrize("layout", [mbg.LAYOUT_AUTO, mbg.LAYOUT_WARP, mbg.LAYOUT_LANE, "lane-serial"])
 @pytest.mark.parametrize("name,n", [("cellcycle", 3000), ("metastasis", 300), ("sizek", 300), ("montagud", 200)])
-def test_reference_models_parity(name, n):
+def test_reference_models_parity(name, n, layout):
     bnd, cfg = golden_model(name)
-    model, sim = run_device(bnd, cfg, n)
+    model, sim = run_device(bnd, cfg, n, **layout_kw(layout))
     orc = run_oracle(bnd, cfg, model, n)
     compare_trajectories(sim, orc)
     compare_histograms(model, sim, orc, n)
 
 
-def test_thread_and_warp_layouts_agree():
-    """Both layouts run the same integer arithmetic and the same clock: identical window sums,
+@pytest.mark.parametrize("other", [mbg.LAYOUT_WARP, mbg.LAYOUT_LANE, "lane-serial"])
+def test_layouts_agree(other):
+    """Every layout runs the same integer arithmetic and the same clock: identical window sums,
     final states and fixed points."""
     net = synth.sweep_instance(2)
     bnd, cfg = net.bnd(), net.cfg(sample_count=3000)
     _, a = run_device(bnd, cfg, 3000, layout=mbg.LAYOUT_THREAD, record=False)
-    _, b = run_device(bnd, cfg, 3000, layout=mbg.LAYOUT_WARP, record=False)
+    _, b = run_device(bnd, cfg, 3000, record=False, **layout_kw(other))
     ra, _ = a.probtraj_raw()
     rb, _ = b.probtraj_raw()
     assert np.array_equal(ra, rb)
@@ -110,10 +126,11 @@ def test_trajectory_ids_are_partition_independent():
     assert np.array_equal(a, b + c)
 
 
-def test_step_limit_is_counted():
+@pytest.mark.parametrize("layout", [mbg.LAYOUT_WARP, mbg.LAYOUT_LANE, "lane-serial"])
+def test_step_limit_is_counted(layout):
     net = synth.medium()
     bnd, cfg = net.bnd(), net.cfg(sample_count=64)
-    model, sim = run_device(bnd, cfg, 64, max_steps=50)
+    model, sim = run_device(bnd, cfg, 64, max_steps=50, **layout_kw(layout))
     s = sim.summary()
     assert s["step_limited"] > 0
     assert s["step_limited"] + s["finished"] + s["fixed_points"] == 64

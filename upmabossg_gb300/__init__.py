@@ -15,7 +15,7 @@ PKG = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(PKG, "lib", "libmbg.so")
 CLI_PATH = os.path.join(PKG, "bin", "MaBoSSG")
 
-LAYOUT_AUTO, LAYOUT_THREAD, LAYOUT_WARP = 0, 1, 2
+LAYOUT_AUTO, LAYOUT_THREAD, LAYOUT_WARP, LAYOUT_LANE = 0, 1, 2, 3
 STATUS = {0: "OK", 1: "ARG", 2: "IO", 3: "PARSE", 4: "MODEL", 5: "CUDA", 6: "JIT", 7: "NOMEM", 8: "DEVICE",
           9: "STATE"}
 
@@ -62,7 +62,8 @@ class SimOpts(ctypes.Structure):
                 ("use_cfg_seed", ctypes.c_int32), ("layout", ctypes.c_int32),
                 ("record_trajectories", ctypes.c_int32), ("device", ctypes.c_int32),
                 ("max_steps", ctypes.c_uint32), ("block_size", ctypes.c_int32),
-                ("blocks_per_sm", ctypes.c_int32), ("thread_cutoff", ctypes.c_int32)]
+                ("blocks_per_sm", ctypes.c_int32), ("thread_cutoff", ctypes.c_int32),
+                ("lane_update", ctypes.c_int32)]
 
 
 class RunSummary(ctypes.Structure):
@@ -226,7 +227,8 @@ class Simulation:
     """One simulation handle: trajectories, seed, layout; results after run()."""
 
     def __init__(self, model: Model, n_traj=0, seed=None, layout=LAYOUT_AUTO, record_trajectories=False,
-                 max_steps=0, traj_base=0, device=0, block_size=0, blocks_per_sm=0, thread_cutoff=0):
+                 max_steps=0, traj_base=0, device=0, block_size=0, blocks_per_sm=0, thread_cutoff=0,
+                 lane_update=0):
         o = SimOpts()
         lib().mbg_sim_opts_default(ctypes.byref(o))
         o.n_traj = int(n_traj)
@@ -241,6 +243,7 @@ class Simulation:
         o.block_size = block_size
         o.blocks_per_sm = blocks_per_sm
         o.thread_cutoff = thread_cutoff
+        o.lane_update = lane_update
         self.model = model
         h = ctypes.c_void_p()
         _check(lib().mbg_sim_create(model._h, ctypes.byref(o), ctypes.byref(h)))

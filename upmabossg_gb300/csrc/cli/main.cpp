@@ -7,7 +7,7 @@
 // (main.cpp:148-152) is lifted to the library's own limits.
 //
 // Environment (the argument list stays the reference's): MBG_DEVICE (CUDA ordinal),
-// MBG_LAYOUT (auto | thread | warp), MBG_TIMINGS=1 (JSON run summary on stderr).
+// MBG_LAYOUT (auto | thread | warp | lane), MBG_TIMINGS=1 (JSON run summary on stderr).
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -47,6 +47,7 @@ int main(int argc, char** argv) {
     if (const char* l = std::getenv("MBG_LAYOUT")) {
         if (!std::strcmp(l, "thread")) opts.layout = MBG_LAYOUT_THREAD;
         else if (!std::strcmp(l, "warp")) opts.layout = MBG_LAYOUT_WARP;
+        else if (!std::strcmp(l, "lane")) opts.layout = MBG_LAYOUT_LANE;
     }
     mbg_sim* sim = nullptr;
     int rc = 0;

@@ -7,6 +7,7 @@
 #include "sim_types.h"
 #include "sim_core.cuh"
 #include "sim_warp.cuh"
+#include "sim_lane.cuh"
 #include "kernels.h"
 
 namespace mbg {
@@ -21,6 +22,18 @@ extern "C" __global__ void __launch_bounds__(256, 4) mbg_sim_warp(const SimParam
 extern "C" __global__ void __launch_bounds__(256) mbg_sim_warp_gather(const SimParams p) {
     extern __shared__ __align__(16) unsigned char smem[];
     sim_warp_body<false>(p, smem);
+}
+
+// One trajectory per lane, state in shared memory, incremental rates; the readers of a flipped
+// node are updated by their own lane, or dealt out over the warp (cooperative variant).
+extern "C" __global__ void __launch_bounds__(256, 3) mbg_sim_lane(const SimParams p) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    sim_lane_body<false>(p, smem);
+}
+
+extern "C" __global__ void __launch_bounds__(256, 3) mbg_sim_lane_coop(const SimParams p) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    sim_lane_body<true>(p, smem);
 }
 
 // Batched instances (parameter sweeps), both variants.
@@ -186,6 +199,21 @@ cudaError_t sim_warp_occupancy(bool cached_index, int block, size_t smem, int* b
                         : cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, mbg_sim_warp_gather, block,
                                                                         smem);
 }
+
+cudaError_t launch_sim_lane(const SimParams& p, bool coop, int grid, int block, size_t smem, cudaStream_t stream) {
+    if (coop) mbg_sim_lane_coop<<<grid, block, smem, stream>>>(p);
+    else mbg_sim_lane<<<grid, block, smem, stream>>>(p);
+    return cudaGetLastError();
+}
+
+cudaError_t sim_lane_configure(bool coop, size_t smem, int block, int* blocks_per_sm) {
+    const void* f = coop ? (const void*)mbg_sim_lane_coop : (const void*)mbg_sim_lane;
+    cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, f, block, smem);
+}
+
+unsigned sim_lane_smem_per_thread(int n) { return lane_smem_bytes(n); }
 
 cudaError_t launch_fp_aggregate(const unsigned* fp_states, const unsigned* fp_count, unsigned capacity, int words,
                                 unsigned* slot_rep, unsigned* slot_cnt, unsigned n_slots, unsigned* out_states,

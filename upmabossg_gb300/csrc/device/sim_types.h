@@ -47,9 +47,23 @@ struct DevNode {
     unsigned long long table;     // BINARY with k <= 5: the 2^(k+1) table bits
 };
 
+// The lane layout's per-node record, 32 bytes (one sector): everything a step reads about a
+// node whose rate is a two-valued table over at most 4 regulators. Other nodes carry a flag and
+// are read from their DevNode.
+constexpr unsigned kLaneWideTable = 1u;  // more than 4 regulators: table and regulators in DevNode
+constexpr unsigned kLanePalette = 2u;    // multi-valued rate: DevNode palette path
+struct LaneNode {
+    unsigned long long up, down;  // fixed-point rates (BINARY)
+    unsigned int table;           // k <= 4: the 2^(k+1) table bits
+    unsigned short r[4];          // the first min(k, 4) regulators
+    unsigned short k;             // number of regulators
+    unsigned short flags;         // kLaneWideTable | kLanePalette
+};
+
 struct SimParams {
     // model
     const DevNode* nodes;
+    const LaneNode* lnodes;
     const unsigned short* regs;
     const unsigned int* tabs;
     const unsigned char* pidx;

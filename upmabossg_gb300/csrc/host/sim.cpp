@@ -10,6 +10,8 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <mutex>
@@ -83,6 +85,16 @@ DeviceLayout layout_model(const CompiledModel& cm) {
         }
         d.tab_off[i] = dn.tab_off;
         d.pal_off[i] = dn.pal_off;
+        LaneNode ln;
+        std::memset(&ln, 0, sizeof ln);
+        ln.up = dn.up;
+        ln.down = dn.down;
+        ln.k = dn.k;
+        for (size_t j = 0; j < cn.regs.size() && j < 4; ++j) ln.r[j] = (uint16_t)cn.regs[j];
+        if (cn.kind != NODE_BINARY) ln.flags = kLanePalette;
+        else if (cn.regs.size() > 4) ln.flags = kLaneWideTable;
+        else ln.table = cn.bits[0];
+        d.lnodes.push_back(ln);
     }
     d.dep_off.push_back(0);
     for (int i = 0; i < cm.n; ++i) {
@@ -163,6 +175,7 @@ void Sim::create(const CompiledModel& model, const std::vector<std::string>& nod
     // model arrays
     std::memset(&prm, 0, sizeof prm);
     prm.nodes = upload(dl.nodes, owned);
+    prm.lnodes = upload(dl.lnodes, owned);
     prm.regs = upload(dl.regs, owned);
     prm.tabs = upload(dl.tabs, owned);
     prm.pidx = upload(dl.pidx, owned);
@@ -207,13 +220,20 @@ void Sim::create(const CompiledModel& model, const std::vector<std::string>& nod
 
     if (o.block_size && (o.block_size % 32 != 0 || o.block_size > 256))
         throw ArgError("block_size must be a multiple of 32, at most 256");
+    if (o.layout < MBG_LAYOUT_AUTO || o.layout > MBG_LAYOUT_LANE) throw ArgError("unknown layout");
+    if (o.lane_update < 0 || o.lane_update > 1) throw ArgError("lane_update must be 0 or 1");
     if (o.layout == MBG_LAYOUT_THREAD && cm.words > 16) throw ModelError("thread layout supports at most 512 nodes");
-    if (o.layout == MBG_LAYOUT_WARP && cm.n_out > 32) throw ModelError("warp layout supports at most 32 outputs");
     if (o.layout != MBG_LAYOUT_AUTO) {
-        setup_layout(o.layout, o.block_size > 0 ? o.block_size : 256);
-    } else if (o.thread_cutoff > 0 || cm.words > 16 || cm.n_out > 32) {
-        const int lay = cm.words <= 16 && (cm.n <= o.thread_cutoff || cm.n_out > 32) ? MBG_LAYOUT_THREAD
-                                                                                     : MBG_LAYOUT_WARP;
+        int blk = o.block_size;
+        if (blk <= 0) {
+            // the lane layout's shared memory grows with N: the largest block that fits
+            blk = 256;
+            if (o.layout == MBG_LAYOUT_LANE)
+                while (blk > 32 && (size_t)blk * sim_lane_smem_per_thread(cm.n) > 227 * 1024) blk >>= 1;
+        }
+        setup_layout(o.layout, blk, o.lane_update != 1);
+    } else if (o.thread_cutoff > 0) {
+        const int lay = cm.words <= 16 && cm.n <= o.thread_cutoff ? MBG_LAYOUT_THREAD : MBG_LAYOUT_WARP;
         setup_layout(lay, o.block_size > 0 ? o.block_size : 256);
     } else {
         autotune();
@@ -224,7 +244,11 @@ namespace {
 // Autotuned launch shapes per (model size class ceil(log2 N), pilot size class ceil(log2 pilot)),
 // shared by all simulations of the process: layout and threads per block.
 std::mutex g_tune_mu;
-std::map<std::pair<int, int>, std::pair<int, int>> g_tuned;
+struct Shape {
+    int layout, block;
+    bool coop;
+};
+std::map<std::pair<int, int>, Shape> g_tuned;
 
 int ceil_log2(uint64_t x) {
     int c = 0;
@@ -234,7 +258,7 @@ int ceil_log2(uint64_t x) {
 }  // namespace
 
 void Sim::autotune() {
-    // the pilot is large enough to fill the GPU in either layout (or the whole run when smaller),
+    // the pilot is large enough to fill the GPU in every layout (or the whole run when smaller),
     // so that the choice reflects occupancy as well as per-transition cost
     const uint64_t pilot = std::min<uint64_t>(n_traj, 1u << 17);
     const std::pair<int, int> cls{ceil_log2((uint64_t)cm.n), ceil_log2(pilot)};
@@ -242,39 +266,49 @@ void Sim::autotune() {
         std::lock_guard<std::mutex> lock(g_tune_mu);
         auto it = g_tuned.find(cls);
         if (it != g_tuned.end()) {
-            setup_layout(it->second.first, opts.block_size > 0 ? opts.block_size : it->second.second);
+            setup_layout(it->second.layout, opts.block_size > 0 ? opts.block_size : it->second.block,
+                         it->second.coop);
             return;
         }
     }
-    // time both layouts and two block sizes on the pilot
+    // time every layout and block size on the pilot; all give identical results, so the kernel
+    // times compare the same work
     const uint64_t saved_n = prm.n_traj;
     prm.n_traj = pilot;
+    const bool log = std::getenv("MBG_AUTOTUNE_LOG") != nullptr;
     double best = -1;
-    int best_layout = MBG_LAYOUT_WARP, best_block = 256;
-    for (int lay : {MBG_LAYOUT_THREAD, MBG_LAYOUT_WARP}) {
-        for (int blk : {128, 256}) {
-            if (opts.block_size > 0 && blk != opts.block_size) continue;
-            setup_layout(lay, blk);
-            run(nullptr);  // warm-up (and JIT load)
-            run(nullptr);
-            const double rate = (double)summary.transitions / std::max(summary.kernel_ms, 1e-3);
-            if (rate > best) {
-                best = rate;
-                best_layout = lay;
-                best_block = blk;
+    Shape best_shape{MBG_LAYOUT_WARP, 256, false};
+    for (int lay : {MBG_LAYOUT_THREAD, MBG_LAYOUT_WARP, MBG_LAYOUT_LANE}) {
+        for (int blk : {64, 128, 256}) {
+            for (int coop = 0; coop < 2; ++coop) {
+                if (opts.block_size > 0 && blk != opts.block_size) continue;
+                if (lay != MBG_LAYOUT_LANE && (blk == 64 || coop)) continue;
+                if (lay == MBG_LAYOUT_THREAD && cm.words > 16) continue;
+                if (lay == MBG_LAYOUT_LANE && (size_t)blk * sim_lane_smem_per_thread(cm.n) > 227 * 1024) continue;
+                setup_layout(lay, blk, coop != 0);
+                run(nullptr);  // warm-up (and JIT load)
+                run(nullptr);
+                if (log)
+                    std::fprintf(stderr, "mbg autotune: n=%d pilot=%llu layout=%d block=%d coop=%d kernel_ms=%.3f\n",
+                                 cm.n, (unsigned long long)pilot, lay, blk, coop, summary.kernel_ms);
+                if (best < 0 || summary.kernel_ms < best) {
+                    best = summary.kernel_ms;
+                    best_shape = Shape{lay, blk, coop != 0};
+                }
             }
         }
     }
     prm.n_traj = saved_n;
     ran = false;
-    setup_layout(best_layout, best_block);
+    setup_layout(best_shape.layout, best_shape.block, best_shape.coop);
     std::lock_guard<std::mutex> lock(g_tune_mu);
-    g_tuned[cls] = {best_layout, best_block};
+    g_tuned[cls] = best_shape;
 }
 
-void Sim::setup_layout(int lay, int blk) {
+void Sim::setup_layout(int lay, int blk, bool coop) {
     layout = lay;
     block = blk;
+    lane_coop = coop;
     int bps = 0;
     if (layout == MBG_LAYOUT_THREAD) {
         double ms = 0;
@@ -283,6 +317,10 @@ void Sim::setup_layout(int lay, int blk) {
         smem = 0;
         ck(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, (const void*)thread_kernel, block, 0),
            "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
+    } else if (layout == MBG_LAYOUT_LANE) {
+        smem = (size_t)block * sim_lane_smem_per_thread(cm.n);
+        if (smem > 227 * 1024) throw ModelError("model too large for the lane layout's shared memory at this block size");
+        ck(sim_lane_configure(lane_coop, smem, block, &bps), "configuring mbg_sim_lane");
     } else {
         // keep every node's regulator index in shared memory while a block's share stays small
         // enough for several resident blocks per SM; otherwise re-gather it on each update
@@ -313,6 +351,8 @@ void Sim::run(cudaStream_t stream) {
         void* args[] = {(void*)&prm};
         ck(cudaLaunchKernel((const void*)thread_kernel, dim3(grid), dim3(block), args, 0, stream),
            "cudaLaunchKernel(mbg_sim_thread)");
+    } else if (layout == MBG_LAYOUT_LANE) {
+        ck(launch_sim_lane(prm, lane_coop, grid, block, smem, stream), "launch mbg_sim_lane");
     } else {
         ck(launch_sim_warp(prm, cached_index, grid, block, smem, stream), "launch mbg_sim_warp");
     }

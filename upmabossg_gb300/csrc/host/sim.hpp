@@ -23,9 +23,10 @@ public:
     void create(const CompiledModel& cm, const std::vector<std::string>& names, const mbg_sim_opts& o);
     void run(cudaStream_t stream);
     void fetch();  // copies results to the host vectors below
-    // Chooses kernel, block size, shared memory and grid for a layout.
-    void setup_layout(int layout, int block);
-    // AUTO layout: times both layouts on a pilot subset once per model size class.
+    // Chooses kernel, block size, shared memory and grid for a layout (coop: the lane layout's
+    // warp-cooperative reader update).
+    void setup_layout(int layout, int block, bool coop = true);
+    // AUTO layout: times every layout and shape on a pilot subset once per model size class.
     void autotune();
 
     CompiledModel cm;
@@ -35,6 +36,7 @@ public:
     int device = 0, sms = 0, layout = 0, grid = 0, block = 256;
     size_t smem = 0;
     bool cached_index = false;
+    bool lane_coop = true;
     double jit_ms = 0;
     void* thread_kernel = nullptr;
     DeviceLayout dl;

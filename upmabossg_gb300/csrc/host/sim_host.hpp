@@ -23,6 +23,7 @@ struct IoError : Error { using Error::Error; };
 // Device image of a compiled model: the arrays SimParams points at, before upload.
 struct DeviceLayout {
     std::vector<DevNode> nodes;
+    std::vector<LaneNode> lnodes;
     std::vector<uint16_t> regs;
     std::vector<uint32_t> tabs;
     std::vector<uint8_t> pidx;
