@@ -14,7 +14,7 @@ unsigned sim_warp_smem_per_warp(int n, bool cached_index);
 cudaError_t sim_warp_occupancy(bool cached_index, int block, size_t smem, int* blocks_per_sm);
 cudaError_t launch_sim_lane(const SimParams& p, bool coop, int grid, int block, size_t smem, cudaStream_t stream);
 cudaError_t sim_lane_configure(bool coop, size_t smem, int block, int* blocks_per_sm);
-unsigned sim_lane_smem_per_thread(int n);
+size_t sim_lane_smem(int n, int block);  // dynamic shared memory of a lane-layout block
 cudaError_t launch_sim_warp_batch(const BatchDesc& b, bool cached_index, int grid, int block, size_t smem,
                                   cudaStream_t stream);
 cudaError_t sim_warp_batch_configure(bool cached_index, size_t smem, int block, int* blocks_per_sm);

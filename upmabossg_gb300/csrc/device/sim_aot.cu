@@ -3,6 +3,8 @@
 // from the same headers (see jit.cpp).
 #include <cuda_runtime.h>
 
+#include <cmath>
+
 #include "philox.h"
 #include "sim_types.h"
 #include "sim_core.cuh"
@@ -209,11 +211,30 @@ cudaError_t launch_sim_lane(const SimParams& p, bool coop, int grid, int block, 
 cudaError_t sim_lane_configure(bool coop, size_t smem, int block, int* blocks_per_sm) {
     const void* f = coop ? (const void*)mbg_sim_lane_coop : (const void*)mbg_sim_lane;
     cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, f, block, smem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(f, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, f, block, smem);
+    if (e != cudaSuccess || *blocks_per_sm < 1) return e;
+    // the smallest shared-memory carve-out that keeps as many blocks resident leaves the rest of
+    // the SM's 256 KiB to L1, which caches the model tables every step reads
+    int dev = 0, per_sm = 0, reserved = 0;
+    e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev);
+    if (e != cudaSuccess || per_sm <= 0) return e;
+    // the driver rounds the percentage up to a supported carve-out: try the largest percentage at
+    // or below the need first, and step up if that carve-out holds fewer blocks
+    const int want = *blocks_per_sm;
+    const double need = (double)want * (double)(smem + (size_t)reserved);
+    const int lo = (int)std::floor(100.0 * need / per_sm), hi = (int)std::ceil(100.0 * need / per_sm);
+    for (int pct : {lo, hi, 100}) {
+        e = cudaFuncSetAttribute(f, cudaFuncAttributePreferredSharedMemoryCarveout, pct < 100 ? pct : 100);
+        if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, f, block, smem);
+        if (e != cudaSuccess || *blocks_per_sm >= want) return e;
+    }
+    return e;
 }
 
-unsigned sim_lane_smem_per_thread(int n) { return lane_smem_bytes(n); }
+size_t sim_lane_smem(int n, int block) { return (size_t)block * lane_smem_bytes(n) + lane_block_extra(block); }
 
 cudaError_t launch_fp_aggregate(const unsigned* fp_states, const unsigned* fp_count, unsigned capacity, int words,
                                 unsigned* slot_rep, unsigned* slot_cnt, unsigned n_slots, unsigned* out_states,

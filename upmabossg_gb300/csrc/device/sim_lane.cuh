@@ -4,49 +4,42 @@
 // The reference re-evaluates all N rates and scans them on every step
 // (src/jit_kernels/simulation.cu:9-21 and 77-164 with the generated compute_transition_rates of
 // src/generator.cpp:124-144). Here a lane keeps, for its trajectory:
-//   st[W]    state words,
-//   act[W]   active words (bit i: node i's rate is non-zero),
-//   gsum[G]  exact 64-bit fixed-point rate sum of each 32-node group (G = W),
-//   gact[GW] bit g: gsum[g] != 0,
+//   fen[G]  a Fenwick tree over the exact 64-bit fixed-point rate sums of the 32-node groups
+//           (G = W): entry i (1-based) holds the sum of groups (i - lowbit(i), i],
+//   st[W]   state words,
+//   act[W]  active words (bit i: node i's rate is non-zero),
 // in shared memory, in rows of blockDim.x entries (entry [row][thread]), so that the 32 lanes of a
-// warp always touch 32 distinct banks whatever rows they read. A step walks the non-empty groups in
-// node order, then the active nodes of the chosen group, which is the reference's first-prefix
-// pick restricted to the nodes that can contribute; a flip of node k re-evaluates only the nodes
-// whose rate reads k (the dependency CSR) and patches act, gsum, gact and the total. Every lane
-// runs its own trajectory, so the per-step work is not spread over a warp; a new trajectory is set
-// up by the whole warp at once (one node per lane), because that pass is O(N).
+// warp always touch 32 distinct banks whatever rows they read. A step descends the tree to the
+// group holding the target (log2 G loads, the same count on every lane), then walks the active
+// nodes of that group in node order: the reference's first-prefix pick, exactly. A flip of node k
+// re-evaluates only the nodes whose rate reads k (the dependency CSR) and adds each rate change
+// along its group's tree path. A new trajectory is set up by the whole warp at once (one node per
+// lane), because that pass is O(N).
 // Includes nothing: sim_types.h, philox.h, sim_core.cuh and sim_warp.cuh come first.
 #pragma once
 
 namespace mbg {
 
 __host__ __device__ __forceinline__ int lane_groups(int n) { return (n + 31) >> 5; }
-__host__ __device__ __forceinline__ int lane_gwords(int n) { return (lane_groups(n) + 31) >> 5; }
-// Shared-memory bytes per thread: group sums, the rate-change slot, state, active and
-// non-empty-group words, the output-touched slot.
-__host__ __device__ __forceinline__ unsigned lane_smem_bytes(int n) {
-    const int G = lane_groups(n);
-    return (unsigned)(8 * (G + 1) + 4 * (2 * G + lane_gwords(n) + 1));
-}
+// Shared-memory bytes per thread (plus lane_block_extra per block).
+__host__ __device__ __forceinline__ unsigned lane_smem_bytes(int n) { return 16u * (unsigned)lane_groups(n); }
+// Per block: one word per warp (lanes whose output-node rates changed in a cooperative update).
+__host__ __device__ __forceinline__ unsigned lane_block_extra(int block) { return 4u * (unsigned)((block + 31) / 32); }
 
 struct LaneSmem {
-    unsigned long long* gsum;    // [G][T]
-    unsigned long long* tdelta;  // [T]: rate change of the owner's total during a cooperative update
-    unsigned* st;                // [G][T]
-    unsigned* act;               // [G][T]
-    unsigned* gact;              // [GW][T]
-    unsigned* touched;           // [T]: an output node's rate changed
+    unsigned long long* fen;  // [G][T]
+    unsigned* st;             // [G][T]
+    unsigned* act;            // [G][T]
+    unsigned* wtouch;         // [T / 32]
 };
 
 __device__ __forceinline__ LaneSmem lane_smem_at(unsigned char* base, int n, int T) {
     const int G = lane_groups(n);
     LaneSmem m;
-    m.gsum = reinterpret_cast<unsigned long long*>(base);
-    m.tdelta = m.gsum + (size_t)G * T;
-    m.st = reinterpret_cast<unsigned*>(m.tdelta + T);
+    m.fen = reinterpret_cast<unsigned long long*>(base);
+    m.st = reinterpret_cast<unsigned*>(m.fen + (size_t)G * T);
     m.act = m.st + (size_t)G * T;
-    m.gact = m.act + (size_t)G * T;
-    m.touched = m.gact + (size_t)lane_gwords(n) * T;
+    m.wtouch = m.act + (size_t)G * T;
     return m;
 }
 
@@ -54,6 +47,37 @@ __device__ __forceinline__ LaneSmem lane_smem_at(unsigned char* base, int n, int
 // of row 0).
 __device__ __forceinline__ unsigned col_bit(const unsigned* col, int T, int i) {
     return (col[(i >> 5) * T] >> (i & 31)) & 1u;
+}
+
+// Fenwick tree of one trajectory (`col` points at its entry of row 0; tree index i is row i-1).
+__device__ __forceinline__ void fen_add(unsigned long long* col, int T, int G, int g, unsigned long long delta) {
+    for (int i = g + 1; i <= G; i += i & -i) col[(size_t)(i - 1) * T] += delta;
+}
+__device__ __forceinline__ void fen_add_atomic(unsigned long long* col, int T, int G, int g,
+                                               unsigned long long delta) {
+    for (int i = g + 1; i <= G; i += i & -i) atomicAdd(col + (size_t)(i - 1) * T, delta);
+}
+// Group holding target r (r < total): the largest g with sum(groups < g) <= r; r becomes relative
+// to that group. `top` is the largest power of two <= G.
+__device__ __forceinline__ int fen_find(const unsigned long long* col, int T, int G, int top,
+                                        unsigned long long& r) {
+    int pos = 0;
+    for (int step = top; step > 0; step >>= 1) {
+        const int nxt = pos + step;
+        if (nxt <= G) {
+            const unsigned long long v = col[(size_t)(nxt - 1) * T];
+            if (v <= r) {
+                pos = nxt;
+                r -= v;
+            }
+        }
+    }
+    return pos;
+}
+__device__ __forceinline__ unsigned long long fen_total(const unsigned long long* col, int T, int G) {
+    unsigned long long s = 0ull;
+    for (int i = G; i > 0; i -= i & -i) s += col[(size_t)(i - 1) * T];
+    return s;
 }
 
 // Regulator index of node i (k regulators) in the state column st.
@@ -77,6 +101,20 @@ __device__ __forceinline__ unsigned lane_idx4(const unsigned* st, int T, int k, 
     if (k > 2) idx |= col_bit(st, T, (int)(r23 & 0xffffu)) << 2;
     if (k > 3) idx |= col_bit(st, T, (int)(r23 >> 16)) << 3;
     return idx;
+}
+
+// Rate of node i in the state column st, evaluated from its tables.
+__device__ __forceinline__ unsigned long long lane_eval(const SimParams& p, int i, const unsigned* st, int T) {
+    const uint4* rec = reinterpret_cast<const uint4*>(p.lnodes + i);
+    const uint4 ra = __ldg(rec), rb = __ldg(rec + 1);
+    const unsigned self = col_bit(st, T, i);
+    if ((rb.w >> 16) == 0u) {
+        const int k = (int)(rb.w & 0xffffu);
+        if (!((rb.x >> ((self << k) | lane_idx4(st, T, k, rb.y, rb.z))) & 1u)) return 0ull;
+        return self ? (((unsigned long long)ra.w << 32) | ra.z) : (((unsigned long long)ra.y << 32) | ra.x);
+    }
+    const NodeHead h = load_head(p, i);
+    return rate_at(p, i, h, self, lane_gather(p, i, h.k, st, T));
 }
 
 // Current rate of node i from its active bit (BINARY) or its table (PALETTE).
@@ -114,11 +152,14 @@ __device__ __forceinline__ float lane_entropy(const SimParams& p, const unsigned
     return entropy_from_sums(R, c, p.to_real);
 }
 
-// The whole warp sets up the trajectory `traj` in column `c` (state, active bits, group sums,
-// non-empty-group bits); returns the total rate on every lane.
+// The whole warp sets up the trajectory `traj` in column `c` (state, active bits, Fenwick tree);
+// returns the total rate on every lane. Groups are processed 32 at a time (chunk): lane l holds
+// the sum of group 32 * chunk + l, a scan gives the prefixes, and tree entry
+// i = P(i) - P(i - lowbit(i)) (P(x) = sum of groups < x) takes P(i - lowbit(i)) from this chunk
+// or, at a multiple of 32, from the chunk boundaries kept one per lane.
 __device__ __forceinline__ unsigned long long lane_coop_init(const SimParams& p, const LaneSmem& m, int T, int c,
                                                              unsigned long long traj, unsigned lane) {
-    const int n = p.n, G = lane_groups(n), GW = lane_gwords(n);
+    const int n = p.n, G = lane_groups(n);
     unsigned* st = m.st + c;
     // state word w from Philox blocks 8w .. 8w+7 (4 nodes each), as the other layouts do
     for (int w = (int)lane; w < G; w += 32) {
@@ -137,63 +178,39 @@ __device__ __forceinline__ unsigned long long lane_coop_init(const SimParams& p,
         st[w * T] = word;
     }
     __syncwarp();
-    unsigned long long total = 0ull;
-    unsigned gbits = 0u;  // lane q collects bits of gact word q
-    for (int g = 0; g < G; ++g) {
-        const int i = g * 32 + (int)lane;
-        unsigned long long v = 0ull;
-        if (i < n) {
-            const uint4* rec = reinterpret_cast<const uint4*>(p.lnodes + i);
-            const uint4 ra = __ldg(rec), rb = __ldg(rec + 1);
-            const unsigned self = col_bit(st, T, i);
-            if ((rb.w >> 16) == 0u) {
-                const unsigned idx = lane_idx4(st, T, (int)(rb.w & 0xffffu), rb.y, rb.z);
-                const int k = (int)(rb.w & 0xffffu);
-                if ((rb.x >> ((self << k) | idx)) & 1u)
-                    v = self ? (((unsigned long long)ra.w << 32) | ra.z) : (((unsigned long long)ra.y << 32) | ra.x);
-            } else {
-                const NodeHead h = load_head(p, i);
-                v = rate_at(p, i, h, self, lane_gather(p, i, h.k, st, T));
-            }
+    unsigned long long carry = 0ull, bnd = 0ull;
+    for (int ch = 0; ch * 32 < G; ++ch) {
+        if ((int)lane == ch) bnd = carry;  // P(32 * ch)
+        unsigned long long mine = 0ull;
+        const int gend = min(G - ch * 32, 32);
+        for (int gg = 0; gg < gend; ++gg) {
+            const int g = ch * 32 + gg;
+            const int i = g * 32 + (int)lane;
+            const unsigned long long v = i < n ? lane_eval(p, i, st, T) : 0ull;
+            const unsigned a = __ballot_sync(MBG_FULL, v != 0ull);
+            const unsigned long long s = warp_sum_u64(v);
+            if (lane == 0u) m.act[(size_t)g * T + c] = a;
+            if ((int)lane == gg) mine = s;
         }
-        const unsigned a = __ballot_sync(MBG_FULL, v != 0ull);
-        const unsigned long long s = warp_sum_u64(v);
-        if (lane == 0u) {
-            m.act[g * T + c] = a;
-            m.gsum[(size_t)g * T + c] = s;
-        }
-        if (s != 0ull && (int)lane == (g >> 5)) gbits |= 1u << (g & 31);
-        total += s;
-    }
-    if ((int)lane < GW) m.gact[lane * T + c] = gbits;
-    if (lane == 0u) {
-        m.tdelta[c] = 0ull;
-        m.touched[c] = 0u;
+        const unsigned long long P = carry + warp_scan_u64(mine, lane);  // P(32 * ch + lane + 1)
+        const int idx = ch * 32 + (int)lane + 1;                        // tree index
+        const int j = idx - (idx & -idx);
+        const unsigned long long v_in = __shfl_sync(MBG_FULL, P, (j - 1 - ch * 32) & 31);
+        const unsigned long long v_bnd = __shfl_sync(MBG_FULL, bnd, (j >> 5) & 31);
+        const unsigned long long Pj = j > ch * 32 ? v_in : v_bnd;
+        if (idx <= G) m.fen[(size_t)(idx - 1) * T + c] = P - Pj;
+        carry = __shfl_sync(MBG_FULL, P, 31);
     }
     __syncwarp();
-    return total;
+    return carry;
 }
 
 // First node whose inclusive rate prefix exceeds r (r < total), or -1.
 __device__ __forceinline__ int lane_pick(const SimParams& p, const unsigned* st, const unsigned* act,
-                                         const unsigned long long* gs, const unsigned* ga, int T, int GW,
+                                         const unsigned long long* fen, int T, int G, int top,
                                          unsigned long long r) {
-    int g = -1;
-    for (int gw = 0; gw < GW && g < 0; ++gw) {
-        unsigned bits = ga[gw * T];
-        while (bits) {
-            const int b = __ffs(bits) - 1;
-            bits &= bits - 1u;
-            const int gg = gw * 32 + b;
-            const unsigned long long s = gs[(size_t)gg * T];
-            if (r < s) {
-                g = gg;
-                break;
-            }
-            r -= s;
-        }
-    }
-    if (g < 0) return -1;
+    const int g = fen_find(fen, T, G, top, r);
+    if (g >= G) return -1;
     unsigned aw = act[g * T];
     const unsigned sw = st[g * T];
     while (aw) {
@@ -209,12 +226,13 @@ __device__ __forceinline__ int lane_pick(const SimParams& p, const unsigned* st,
 }
 
 // Re-evaluates reader dn of a node that just flipped, in the trajectory whose entries start at
-// `col`: dependency entry e = (dn << 16) | (k_dn << 8) | pos (pos 0xFF: dn itself flipped). Patches
-// act, gsum and gact (with shared-memory atomics when several lanes may patch the same
-// trajectory), returns the rate change and sets `out` when dn is an output node whose rate changed.
+// `col`: dependency entry e = (dn << 16) | (k_dn << 8) | pos (pos 0xFF: dn itself flipped).
+// Patches the active bits and the Fenwick tree (with shared-memory atomics when several lanes may
+// patch the same trajectory), returns the rate change and sets `out` when dn is an output node
+// whose rate changed.
 template <bool ATOMIC>
 __device__ __forceinline__ unsigned long long lane_reader(const SimParams& p, unsigned e, const LaneSmem& m, int T,
-                                                          int col, bool& out) {
+                                                          int G, int col, bool& out) {
     const int dn = (int)(e >> 16);
     const int kd = (int)((e >> 8) & 0xffu);
     const unsigned pos = e & 0xffu;
@@ -249,28 +267,15 @@ __device__ __forceinline__ unsigned long long lane_reader(const SimParams& p, un
         a_old = r_old != 0ull;
     }
     const int g = dn >> 5;
-    unsigned* aw = m.act + (size_t)g * T + col;
-    unsigned long long* gw = m.gsum + (size_t)g * T + col;
-    unsigned* gaw = m.gact + (size_t)(g >> 5) * T + col;
     if (a_new != a_old) {
+        unsigned* aw = m.act + (size_t)g * T + col;
         if (ATOMIC) atomicXor(aw, 1u << (dn & 31));
         else *aw ^= 1u << (dn & 31);
     }
     const unsigned long long delta = r_new - r_old;
     if (delta != 0ull) {
-        // the non-empty bit follows every change of the sum; under atomics each update sees a
-        // consistent predecessor, so the toggles compose to (final sum != 0)
-        unsigned long long s_old;
-        if (ATOMIC) {
-            s_old = atomicAdd(gw, delta);
-        } else {
-            s_old = *gw;
-            *gw = s_old + delta;
-        }
-        if ((s_old == 0ull) != (s_old + delta == 0ull)) {
-            if (ATOMIC) atomicXor(gaw, 1u << (g & 31));
-            else *gaw ^= 1u << (g & 31);
-        }
+        if (ATOMIC) fen_add_atomic(m.fen + col, T, G, g, delta);
+        else fen_add(m.fen + col, T, G, g, delta);
         out |= __ldg(p.out_pos + dn) >= 0;
     }
     return delta;
@@ -278,19 +283,20 @@ __device__ __forceinline__ unsigned long long lane_reader(const SimParams& p, un
 
 // After node k flipped in this lane's trajectory: re-evaluates every node whose rate reads k (and
 // k itself) in turn. Returns whether an output node's rate changed.
-__device__ __forceinline__ bool lane_update(const SimParams& p, int k, const LaneSmem& m, int T, int col,
+__device__ __forceinline__ bool lane_update(const SimParams& p, int k, const LaneSmem& m, int T, int G, int col,
                                             unsigned long long& total) {
     const int d0 = (int)__ldg(p.dep_off + k), d1 = (int)__ldg(p.dep_off + k + 1);
     bool out = false;
-    for (int q = d0; q < d1; ++q) total += lane_reader<false>(p, __ldg(p.deps + q), m, T, col, out);
+    for (int q = d0; q < d1; ++q) total += lane_reader<false>(p, __ldg(p.deps + q), m, T, G, col, out);
     return out;
 }
 
 // Warp-cooperative form of lane_update for every lane at once (k < 0: nothing flipped): the
 // reader lists of the 32 flipped nodes are concatenated and dealt out one entry per lane, so a
 // step costs ceil(total length / 32) rounds instead of the longest list. Entries of one trajectory
-// patch its shared-memory rows with atomics and add their rate changes to its tdelta slot.
-__device__ __forceinline__ void lane_coop_update(const SimParams& p, const LaneSmem& m, int T, int wbase,
+// patch its shared-memory rows with atomics; lanes whose output-node rates changed are marked in
+// the warp's wtouch word. The owners read their new totals from their trees afterwards.
+__device__ __forceinline__ void lane_coop_update(const SimParams& p, const LaneSmem& m, int T, int G, int wbase,
                                                  unsigned lane, int k) {
     int d0 = 0, c = 0;
     if (k >= 0) {
@@ -306,6 +312,7 @@ __device__ __forceinline__ void lane_coop_update(const SimParams& p, const LaneS
     const int C = __shfl_sync(MBG_FULL, inc, 31);
     const int ex = inc - c;
     __syncwarp();  // every lane's flip is visible
+    unsigned touched = 0u;
     for (int base = 0; base < C; base += 32) {
         const int q = base + (int)lane;
         // owner: the first lane whose inclusive count exceeds q
@@ -317,14 +324,11 @@ __device__ __forceinline__ void lane_coop_update(const SimParams& p, const LaneS
         }
         const int o_ex = __shfl_sync(MBG_FULL, ex, o);
         const int o_d0 = __shfl_sync(MBG_FULL, d0, o);
-        if (q < C) {
-            const int col = wbase + o;
-            bool out = false;
-            const unsigned long long delta = lane_reader<true>(p, __ldg(p.deps + o_d0 + (q - o_ex)), m, T, col, out);
-            if (delta != 0ull) atomicAdd(m.tdelta + col, delta);
-            if (out) atomicOr(m.touched + col, 1u);
-        }
+        bool out = false;
+        if (q < C) lane_reader<true>(p, __ldg(p.deps + o_d0 + (q - o_ex)), m, T, G, wbase + o, out);
+        touched |= __reduce_or_sync(MBG_FULL, out ? 1u << o : 0u);
     }
+    if (lane == 0u) m.wtouch[wbase >> 5] = touched;
     __syncwarp();
 }
 
@@ -333,13 +337,13 @@ __device__ void sim_lane_body(const SimParams& p, unsigned char* smem) {
     const int T = (int)blockDim.x;
     const unsigned lane = threadIdx.x & 31u;
     const int wbase = (int)(threadIdx.x & ~31u);
-    const int GW = lane_gwords(p.n);
+    const int G = lane_groups(p.n);
+    const int top = 1 << (31 - __clz(G));
     const LaneSmem m = lane_smem_at(smem, p.n, T);
     const int col = (int)threadIdx.x;
     unsigned* st = m.st + col;
     const unsigned* act = m.act + col;
-    const unsigned long long* gs = m.gsum + col;
-    const unsigned* ga = m.gact + col;
+    const unsigned long long* fen = m.fen + col;
 
     unsigned long long j = 0, step = 0, t = 0, total = 0;
     unsigned trans = 0, so = 0;
@@ -404,27 +408,23 @@ __device__ void sim_lane_body(const SimParams& p, unsigned char* smem) {
                     t = p.max_time_fx;
                     status = TRAJ_FINISHED;
                 } else {
-                    k = lane_pick(p, st, act, gs, ga, T, GW, pick_target(d.y, d.z, total));
+                    k = lane_pick(p, st, act, fen, T, G, top, pick_target(d.y, d.z, total));
                     if (k < 0 || k >= p.n) {
                         k = -1;
                         status = TRAJ_ERROR;
                         atomicOr(p.error_flag, (unsigned)DEV_ERR_PICK);
                     } else {
                         st[(k >> 5) * T] ^= 1u << (k & 31);
-                        if (!COOP && lane_update(p, k, m, T, col, total)) h = lane_entropy(p, st, act, T);
+                        if (!COOP && lane_update(p, k, m, T, G, col, total)) h = lane_entropy(p, st, act, T);
                     }
                 }
             }
         }
         if (COOP) {
-            lane_coop_update(p, m, T, wbase, lane, k);
+            lane_coop_update(p, m, T, G, wbase, lane, k);
             if (k >= 0) {
-                total += m.tdelta[col];
-                m.tdelta[col] = 0ull;
-                if (m.touched[col]) {
-                    m.touched[col] = 0u;
-                    h = lane_entropy(p, st, act, T);
-                }
+                total = fen_total(fen, T, G);
+                if ((m.wtouch[wbase >> 5] >> lane) & 1u) h = lane_entropy(p, st, act, T);
             }
         }
         if (k >= 0) {
