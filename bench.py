@@ -99,6 +99,28 @@ class Clocks:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+MBG_LAYOUTS = {"thread": 1, "warp": 2, "lane": 3}
+
+
+def profile_figures(kernel, workload):
+    """Figures of the committed ncu summary profiles/<kernel>_<workload>.md: its `key: value`
+    lines (traffic_bytes_per_launch, issue_slot_utilisation)."""
+    path = os.path.join(ROOT, "profiles", f"{kernel}_{workload}.md")
+    out = {}
+    if not os.path.exists(path):
+        return out
+    out["file"] = os.path.relpath(path, ROOT)
+    with open(path) as f:
+        for line in f:
+            key, sep, val = line.strip().strip("`").partition(": ")
+            if sep and key in ("traffic_bytes_per_launch", "issue_slot_utilisation"):
+                try:
+                    out[key] = float(val) if "." in val else int(val)
+                except ValueError:
+                    pass
+    return out
+
+
 def load_peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -193,7 +215,7 @@ def measure_sweep(steps, warmup, local=0, autotune=True):
     return {"metric": "sweep points/s (plain batched simulation)", "value": len(models) / (step_ms * 1e-3),
             "unit": "points/s", "ms_per_step": step_ms, "transitions_per_s": s["transitions"] / (step_ms * 1e-3),
             "kernel_ms": s["kernel_ms"], "trajectories": s["trajectories"], "instances": len(models),
-            "shape": batch.shape(), "workload": SWEEP_DESC}
+            "classes": batch.classes(), "workload": SWEEP_DESC}
 
 
 SURROGATE_DESC = ("200-node network (2-3 regulators, rates 1) with 32 rate blocks scaled log-uniform in [0.1, 10], "
@@ -253,11 +275,14 @@ def run_ours(args):
         import torch.distributed as dist
         dist.init_process_group("nccl")
     net = make_network(args.workload)
-    n_total = args.n_traj or net.sample_count
-    base, n_rank = mbg.shard_range(n_total, rank, ws)
+    # weak scaling: every rank runs the workload's full trajectory count on its own id range
+    # (trajectories are keyed by id, so the union is one run of ws x n trajectories)
+    n_rank = args.n_traj or net.sample_count
+    base = rank * n_rank
     bnd, cfg = net.bnd(), net.cfg()
     model = mbg.Model.from_strings(bnd, cfg)
-    sim = mbg.Simulation(model, n_traj=n_rank, traj_base=base, device=local, layout=args.layout)
+    sim_kw = dict(layout=args.layout, block_size=args.block, lane_update=args.lane_update)
+    sim = mbg.Simulation(model, n_traj=n_rank, traj_base=base, device=local, **sim_kw)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{local}")
 
     def barrier():
@@ -283,12 +308,17 @@ def run_ours(args):
         barrier()
         wall = time.perf_counter() - t0
     step_ms = sum(sim_ms) / len(sim_ms)
+    trans_step = transitions[-1]  # every step runs the same trajectories: identical counts
     if ws > 1:
-        t = torch.tensor([step_ms], device=f"cuda:{local}")
+        t = torch.tensor([step_ms], device=f"cuda:{local}", dtype=torch.float64)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         step_ms = float(t.item())
-    trans_step = transitions[-1]
-    value = trans_step * ws / (step_ms * 1e-3)
+        c = torch.tensor([trans_step], device=f"cuda:{local}", dtype=torch.float64)
+        torch.distributed.all_reduce(c, op=torch.distributed.ReduceOp.SUM)
+        trans_all = float(c.item())
+    else:
+        trans_all = float(trans_step)
+    value = trans_all / (step_ms * 1e-3)
     summary = sim.summary()
 
     # end to end through the public API: parse + create (H2D of the model) + run + results (D2H)
@@ -297,7 +327,7 @@ def run_ours(args):
     for i in range(max(2, args.steps // 2) + 1):
         t1 = time.perf_counter()
         m2 = mbg.Model.from_strings(bnd, cfg)
-        s2 = mbg.Simulation(m2, n_traj=n_rank, traj_base=base, device=local, layout=args.layout)
+        s2 = mbg.Simulation(m2, n_traj=n_rank, traj_base=base, device=local, **sim_kw)
         s2.run()
         P, TH = s2.probtraj()
         F = s2.final_states()
@@ -311,7 +341,12 @@ def run_ours(args):
         d2h = P.size * 8 + TH.size * 8 + F.size * 4 + fs.nbytes + fp.size * 4
         s2.close()
         m2.close()
-    e2e_value = trans_step * ws / (statistics.mean(e2e_ms) * 1e-3)
+    e2e_step_ms = statistics.mean(e2e_ms)
+    if ws > 1:
+        t = torch.tensor([e2e_step_ms], device=f"cuda:{local}", dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_step_ms = float(t.item())
+    e2e_value = trans_all / (e2e_step_ms * 1e-3)
 
     peaks, peaks_kind = load_peaks()
     info = model.info
@@ -321,11 +356,9 @@ def run_ours(args):
     peak_ops = sms * 128 * clock
     kms = sum(kernel_ms) / len(kernel_ms)
     achieved = trans_step * w_tr / (kms * 1e-3)
-    traffic = None
-    tpath = os.path.join(ROOT, "profiles", f"traffic_{args.workload}.json")
-    if os.path.exists(tpath):
-        with open(tpath) as f:
-            traffic = json.load(f).get("dram_bytes_per_launch")
+    kernel = {MBG_LAYOUTS["thread"]: "mbg_sim_thread", MBG_LAYOUTS["warp"]: "mbg_sim_warp",
+              MBG_LAYOUTS["lane"]: "mbg_sim_lane"}[summary["layout"]]
+    prof = profile_figures(kernel, args.workload)
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu:
         cpu = cpu_reference(net, bnd, cfg, info.frac_bits, args.cpu_seconds)
@@ -334,16 +367,19 @@ def run_ours(args):
         "metric": "transitions/s", "value": value, "unit": "transitions/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "u64", "data": "synthetic",
-        "config": {"workload": WORKLOADS[args.workload], "trajectories": n_total,
-                   "transitions_per_step": trans_step * ws, "layout": ["", "thread", "warp", "lane"][summary["layout"]],
+        "config": {"workload": WORKLOADS[args.workload], "trajectories_per_gpu": n_rank,
+                   "transitions_per_step": trans_all, "layout": ["", "thread", "warp", "lane"][summary["layout"]],
+                   "block_size": summary.get("block_size"),
                    "l2": "flushed between steps (256 MiB write)", "wall_s": wall},
         "e2e": {"value": e2e_value, "unit": "transitions/s", "h2d_bytes_per_step": h2d,
-                "d2h_bytes_per_step": d2h, "ms_per_step": statistics.mean(e2e_ms),
+                "d2h_bytes_per_step": d2h, "ms_per_step": e2e_step_ms,
                 "path": "mbg_model_parse_strings + mbg_sim_create + mbg_sim_run + probtraj/final/fixed-point reads"},
         "gpu_launches": 3 * args.steps,
         "roofline": {"bound": "issue", "achieved": achieved / 1e9, "peak": peak_ops / 1e9, "unit": "Gop/s",
-                     "frac": achieved / peak_ops, "traffic": traffic,
-                     "kernel_ms": kms, "ops_per_transition": w_tr,
+                     "frac": achieved / peak_ops, "traffic": prof.get("traffic_bytes_per_launch"),
+                     "kernel": kernel, "kernel_ms": kms, "ops_per_transition": w_tr,
+                     "issue_slot_utilisation_ncu": prof.get("issue_slot_utilisation"),
+                     "profile": prof.get("file"),
                      "peak_source": f"152 SMs x 128 lanes x {clock / 1e6:.0f} MHz ({peaks_kind} sm_max_mhz)"},
         "cpu_baseline": cpu,
         "clocks": clocks,
@@ -363,7 +399,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="medium", choices=sorted(WORKLOADS) + ["sweep", "surrogate"])
-    ap.add_argument("--layout", type=int, default=0)
+    ap.add_argument("--layout", type=int, default=0, help="0 autotuned, 1 thread, 2 warp, 3 lane")
+    ap.add_argument("--block", type=int, default=0, help="threads per block (0: the layout's default); profiling")
+    ap.add_argument("--lane-update", type=int, default=0, help="lane layout: 0 cooperative, 1 per lane; profiling")
     ap.add_argument("--cpu-seconds", type=float, default=CPU_SAMPLE_SECONDS)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--n-traj", type=int, default=0, help="trajectories (default: the workload's); profiling only")

@@ -96,6 +96,10 @@ typedef struct {
     double sim_ms;             /* device time of the last mbg_sim_run (CUDA events) */
     double kernel_ms;          /* device time of its simulation kernel alone */
     double jit_ms;             /* NVRTC compile time at create (0 if cached) */
+    int32_t block_size;        /* threads per block of the simulation kernel */
+    int32_t grid_size;         /* blocks of the simulation kernel */
+    int32_t lane_update;       /* LANE: 0 cooperative, 1 per-lane reader updates */
+    int32_t reserved;
 } mbg_run_summary;
 
 const char* mbg_last_error(void);
@@ -155,8 +159,10 @@ mbg_status mbg_write_fp_csv(mbg_sim* s, const char* prefix);
 mbg_status mbg_print_results(mbg_sim* s, const char* path);
 
 /* ---- Batched parameter sweeps --------------------------------------------------------------
- * Many independent simulations ("instances": any models, trajectory counts and seeds) in one
- * persistent warp-per-trajectory launch, captured once into a CUDA graph and replayed by every
+ * Many independent simulations ("instances": any models, trajectory counts and seeds) grouped by
+ * model size into classes (<= 32, 64, 128, ..., 4096 nodes, larger); each class is one persistent
+ * launch in the lane or the warp layout with its own block size, and all classes, the fixed-point
+ * aggregation and the counter read-back are captured once into a CUDA graph replayed by every
  * mbg_batch_run. Replaces one reference CLI run per instance (src/main.cpp:101-169), each of which
  * recompiles its kernels with NVRTC. Results per instance are the same as a single simulation's. */
 typedef struct mbg_batch mbg_batch;
@@ -166,8 +172,31 @@ typedef struct {
     uint32_t max_steps;    /* per-trajectory step cap; 0: none */
     int32_t block_size;    /* threads per block (multiple of 32, <= 256); 0: default or autotuned */
     int32_t blocks_per_sm; /* 0: occupancy limit */
-    int32_t autotune;      /* 1: time the launch shapes on the first run and keep the fastest */
+    int32_t autotune;      /* 1: on the first run, time every shape of every class on a pilot subset
+                              of its trajectories and keep the fastest per class */
+    int32_t layout;        /* 0: autotuned per class (without autotune: lane where it fits);
+                              MBG_LAYOUT_LANE or MBG_LAYOUT_WARP: that layout for every class */
 } mbg_batch_opts;
+
+/* One launch shape the autotuner timed for a class. */
+typedef struct {
+    int32_t layout;        /* MBG_LAYOUT_LANE or MBG_LAYOUT_WARP */
+    int32_t block_size;
+    int32_t variant;       /* lane: 1 cooperative reader update; warp: 1 regulator-index cache */
+    int32_t reserved;
+    double kernel_ms;      /* pilot kernel time */
+} mbg_batch_class_timing;
+
+/* A size class of a batch and the launch that runs it. */
+typedef struct {
+    int32_t max_nodes;     /* nodes of the largest member */
+    int32_t instances;
+    uint64_t trajectories;
+    int32_t layout, block_size, variant, grid;
+    double kernel_ms;      /* device time of the class launch in the last run */
+    int32_t timings;       /* shapes timed by the autotuner (mbg_batch_class_timings) */
+    int32_t reserved;
+} mbg_batch_class_info;
 
 void mbg_batch_opts_default(mbg_batch_opts* o);
 /* n_traj and seeds may be NULL: each instance then uses its cfg sample_count / seed_pseudorandom. */
@@ -184,8 +213,12 @@ mbg_status mbg_batch_probtraj_raw(mbg_batch* b, int32_t i, uint64_t* sums, uint6
 mbg_status mbg_batch_final_states(mbg_batch* b, int32_t i, double* probs);
 mbg_status mbg_batch_fixed_points(mbg_batch* b, int32_t i, uint32_t* states, double* probs, size_t cap,
                                   size_t* count);
-/* Launch shape in use: threads per block, shared-memory index cache (0/1), blocks. */
-mbg_status mbg_batch_shape(const mbg_batch* b, int32_t* block_size, int32_t* cached_index, int32_t* grid);
+/* Size classes (in increasing size) and their launch shapes. */
+mbg_status mbg_batch_class_count(const mbg_batch* b, int32_t* count);
+mbg_status mbg_batch_class(const mbg_batch* b, int32_t c, mbg_batch_class_info* out);
+/* The shapes the autotuner timed for class c: up to cap entries, *count gets their number. */
+mbg_status mbg_batch_class_timings(const mbg_batch* b, int32_t c, mbg_batch_class_timing* out, int32_t cap,
+                                   int32_t* count);
 
 /* ---- Learned surrogate for sweep screening ---------------------------------------------------
  * No counterpart in the reference. An ensemble of MLPs (BF16 weights, FP32 accumulation, ReLU

@@ -22,10 +22,18 @@ def instances():
     return texts
 
 
-def single(bnd, cfg, n, seed):
+def single(bnd, cfg, n, seed, layout=mbg.LAYOUT_WARP, lane_update=0):
     m = mbg.Model.from_strings(bnd, cfg)
-    s = mbg.Simulation(m, n_traj=n, seed=seed, layout=mbg.LAYOUT_WARP).run()
+    s = mbg.Simulation(m, n_traj=n, seed=seed, layout=layout, lane_update=lane_update).run()
     return s
+
+
+def single_like(batch, i, bnd, cfg, n, seed):
+    """The single simulation in the layout that ran instance i: window sums agree across layouts,
+    and the transition entropy (float arithmetic, evaluated per layout) agrees bit for bit within
+    one layout."""
+    s = batch.summary(i)
+    return single(bnd, cfg, n, seed, layout=s["layout"], lane_update=s["lane_update"])
 
 
 def check_same(batch, i, sim):
@@ -49,18 +57,41 @@ def test_batch_matches_single_runs():
     tot = batch.summary()
     assert tot["trajectories"] == sum(n) and tot["errors"] == 0
     for i, (b, c) in enumerate(texts):
-        check_same(batch, i, single(b, c, n[i], seeds[i]))
+        check_same(batch, i, single_like(batch, i, b, c, n[i], seeds[i]))
 
 
-@pytest.mark.parametrize("block", [64, 256])
-def test_batch_shape_does_not_change_results(block):
+@pytest.mark.parametrize("layout,block", [(mbg.LAYOUT_LANE, 64), (mbg.LAYOUT_LANE, 256), (mbg.LAYOUT_WARP, 64),
+                                          (mbg.LAYOUT_WARP, 256)])
+def test_batch_shape_does_not_change_results(layout, block):
     texts = instances()[:4]
     models = [mbg.Model.from_strings(b, c) for b, c in texts]
     ref = mbg.Batch(models, n_traj=[1500] * 4).run()
-    other = mbg.Batch(models, n_traj=[1500] * 4, block_size=block).run()
+    other = mbg.Batch(models, n_traj=[1500] * 4, block_size=block, layout=layout).run()
+    assert all(k["layout"] == {mbg.LAYOUT_LANE: "lane", mbg.LAYOUT_WARP: "warp"}[layout] and k["block_size"] == block
+               for k in other.classes())
     for i in range(4):
         assert np.array_equal(ref.probtraj_raw(i)[0], other.probtraj_raw(i)[0])
         assert np.array_equal(ref.final_states(i), other.final_states(i))
+        fa, pa = ref.fixed_points(i)
+        fb, pb = other.fixed_points(i)
+        assert np.array_equal(fa, fb) and np.array_equal(pa, pb)
+
+
+def test_size_classes():
+    """Instances are grouped by node count (<= 32, 64, ..., 4096, larger), one launch each."""
+    texts = instances()
+    models = [mbg.Model.from_strings(b, c) for b, c in texts]
+    batch = mbg.Batch(models, n_traj=[500] * len(models)).run()
+    classes = batch.classes()
+    bounds = [32 << c for c in range(7)] + [1 << 30]
+    sizes = sorted(m.info.nodes for m in models)
+    assert sum(k["instances"] for k in classes) == len(models)
+    assert sum(k["trajectories"] for k in classes) == 500 * len(models)
+    expect = sorted({next(c for c, b in enumerate(bounds) if n <= b) for n in sizes})
+    assert len(classes) == len(expect) >= 2
+    for k, c in zip(classes, expect):
+        assert k["max_nodes"] <= bounds[c] and (c == 0 or k["max_nodes"] > bounds[c - 1])
+        assert k["grid"] > 0 and k["kernel_ms"] > 0
 
 
 def test_graph_replay_and_autotune():
@@ -74,8 +105,11 @@ def test_graph_replay_and_autotune():
     for i in range(5):
         assert np.array_equal(first[i], batch.probtraj_raw(i)[0])
     assert batch.summary()["transitions"] == s1["transitions"]
-    shape = batch.shape()
-    assert shape["block_size"] in (64, 128, 256) and shape["grid"] > 0
+    for k in batch.classes():
+        # the autotuner timed lane and warp shapes and kept the fastest
+        assert {t["layout"] for t in k["timings"]} == {"lane", "warp"}
+        best = min(k["timings"], key=lambda t: t["kernel_ms"])
+        assert (k["layout"], k["block_size"], k["variant"]) == (best["layout"], best["block_size"], best["variant"])
 
 
 def test_batch_probabilities_are_normalised():

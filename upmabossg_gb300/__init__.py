@@ -31,7 +31,7 @@ EXPORTS = (
     "mbg_fixed_points_aggregate_noalloc",
     "mbg_batch_opts_default", "mbg_batch_create", "mbg_batch_destroy", "mbg_batch_run", "mbg_batch_summary",
     "mbg_batch_instance_summary", "mbg_batch_probtraj", "mbg_batch_probtraj_raw", "mbg_batch_final_states",
-    "mbg_batch_fixed_points", "mbg_batch_shape",
+    "mbg_batch_fixed_points", "mbg_batch_class_count", "mbg_batch_class", "mbg_batch_class_timings",
     "mbg_surrogate_create", "mbg_surrogate_destroy", "mbg_surrogate_train", "mbg_surrogate_predict",
     "mbg_surrogate_param_count", "mbg_surrogate_get_params", "mbg_surrogate_set_params", "mbg_surrogate_gradients",
 )
@@ -39,7 +39,19 @@ EXPORTS = (
 
 class BatchOpts(ctypes.Structure):
     _fields_ = [("device", ctypes.c_int32), ("max_steps", ctypes.c_uint32), ("block_size", ctypes.c_int32),
-                ("blocks_per_sm", ctypes.c_int32), ("autotune", ctypes.c_int32)]
+                ("blocks_per_sm", ctypes.c_int32), ("autotune", ctypes.c_int32), ("layout", ctypes.c_int32)]
+
+
+class BatchClassTiming(ctypes.Structure):
+    _fields_ = [("layout", ctypes.c_int32), ("block_size", ctypes.c_int32), ("variant", ctypes.c_int32),
+                ("reserved", ctypes.c_int32), ("kernel_ms", ctypes.c_double)]
+
+
+class BatchClassInfo(ctypes.Structure):
+    _fields_ = [("max_nodes", ctypes.c_int32), ("instances", ctypes.c_int32), ("trajectories", ctypes.c_uint64),
+                ("layout", ctypes.c_int32), ("block_size", ctypes.c_int32), ("variant", ctypes.c_int32),
+                ("grid", ctypes.c_int32), ("kernel_ms", ctypes.c_double), ("timings", ctypes.c_int32),
+                ("reserved", ctypes.c_int32)]
 
 
 class MbgError(RuntimeError):
@@ -72,7 +84,8 @@ class RunSummary(ctypes.Structure):
                 ("step_limited", ctypes.c_uint64), ("errors", ctypes.c_uint64),
                 ("fixed_point_states", ctypes.c_uint64), ("device_error", ctypes.c_uint32),
                 ("layout", ctypes.c_int32), ("sim_ms", ctypes.c_double), ("kernel_ms", ctypes.c_double),
-                ("jit_ms", ctypes.c_double)]
+                ("jit_ms", ctypes.c_double), ("block_size", ctypes.c_int32), ("grid_size", ctypes.c_int32),
+                ("lane_update", ctypes.c_int32), ("reserved", ctypes.c_int32)]
 
     def as_dict(self):
         return {name: getattr(self, name) for name, _ in self._fields_}
@@ -127,7 +140,10 @@ def lib():
             "mbg_batch_final_states": (ctypes.c_int, [vp, i32, dp]),
             "mbg_batch_fixed_points": (ctypes.c_int, [vp, i32, dp, dp, ctypes.c_size_t,
                                                       ctypes.POINTER(ctypes.c_size_t)]),
-            "mbg_batch_shape": (ctypes.c_int, [vp, ctypes.POINTER(i32), ctypes.POINTER(i32), ctypes.POINTER(i32)]),
+            "mbg_batch_class_count": (ctypes.c_int, [vp, ctypes.POINTER(i32)]),
+            "mbg_batch_class": (ctypes.c_int, [vp, i32, ctypes.POINTER(BatchClassInfo)]),
+            "mbg_batch_class_timings": (ctypes.c_int, [vp, i32, ctypes.POINTER(BatchClassTiming), i32,
+                                                       ctypes.POINTER(i32)]),
             "mbg_surrogate_create": (ctypes.c_int, [i32, i32, i32, i32, i32, u64, i32, ctypes.POINTER(vp)]),
             "mbg_surrogate_destroy": (None, [vp]),
             "mbg_surrogate_train": (ctypes.c_int, [vp, dp, dp, ctypes.c_int64, i32, i32, ctypes.c_float, u64,
@@ -320,11 +336,12 @@ class Batch:
     """Many instances (models, trajectory counts, seeds) run in one graph-captured launch."""
 
     def __init__(self, models, n_traj=None, seeds=None, device=0, max_steps=0, block_size=0, blocks_per_sm=0,
-                 autotune=False):
+                 autotune=False, layout=0):
         o = BatchOpts()
         lib().mbg_batch_opts_default(ctypes.byref(o))
         o.device, o.max_steps, o.block_size, o.blocks_per_sm = device, max_steps, block_size, blocks_per_sm
         o.autotune = 1 if autotune else 0
+        o.layout = layout
         self.models = list(models)
         handles = (ctypes.c_void_p * len(self.models))(*[m._h for m in self.models])
         nt = None if n_traj is None else np.ascontiguousarray(np.asarray(n_traj, dtype=np.uint64))
@@ -347,10 +364,25 @@ class Batch:
             _check(lib().mbg_batch_instance_summary(self._h, int(instance), ctypes.byref(s)))
         return s.as_dict()
 
-    def shape(self):
-        b, c, g = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
-        _check(lib().mbg_batch_shape(self._h, ctypes.byref(b), ctypes.byref(c), ctypes.byref(g)))
-        return {"block_size": b.value, "cached_index": bool(c.value), "grid": g.value}
+    def classes(self):
+        """Size classes with their launch shapes and, after an autotuned run, every timed shape."""
+        n = ctypes.c_int32()
+        _check(lib().mbg_batch_class_count(self._h, ctypes.byref(n)))
+        out = []
+        for c in range(n.value):
+            k = BatchClassInfo()
+            _check(lib().mbg_batch_class(self._h, c, ctypes.byref(k)))
+            t = (BatchClassTiming * max(1, k.timings))()
+            cnt = ctypes.c_int32()
+            _check(lib().mbg_batch_class_timings(self._h, c, t, k.timings, ctypes.byref(cnt)))
+            out.append({"max_nodes": k.max_nodes, "instances": k.instances, "trajectories": k.trajectories,
+                        "layout": {LAYOUT_LANE: "lane", LAYOUT_WARP: "warp"}.get(k.layout, k.layout),
+                        "block_size": k.block_size, "variant": k.variant, "grid": k.grid,
+                        "kernel_ms": k.kernel_ms,
+                        "timings": [{"layout": {LAYOUT_LANE: "lane", LAYOUT_WARP: "warp"}.get(x.layout, x.layout),
+                                     "block_size": x.block_size, "variant": x.variant, "kernel_ms": x.kernel_ms}
+                                    for x in t[:cnt.value]]})
+        return out
 
     def probtraj(self, i):
         info = self.models[i].info

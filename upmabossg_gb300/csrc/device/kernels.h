@@ -3,6 +3,8 @@
 
 #include <cuda_runtime.h>
 
+#include <mutex>
+
 #include "sim_types.h"
 
 namespace mbg {
@@ -15,6 +17,16 @@ cudaError_t sim_warp_occupancy(bool cached_index, int block, size_t smem, int* b
 cudaError_t launch_sim_lane(const SimParams& p, bool coop, int grid, int block, size_t smem, cudaStream_t stream);
 cudaError_t sim_lane_configure(bool coop, size_t smem, int block, int* blocks_per_sm);
 size_t sim_lane_smem(int n, int block);  // dynamic shared memory of a lane-layout block
+// Re-applies the attributes of a simulation kernel for the launch shapes that are about to use it
+// (kernel 0: mbg_sim_lane[_coop], 1: mbg_sim_lane_batch[_coop], 2: mbg_sim_warp_batch[_gather],
+// 3: mbg_sim_warp[_gather]; variant selects the second name): kernel attributes are process-wide,
+// so another handle may have changed them since this one was configured.
+cudaError_t sim_kernel_limits(int kernel, bool variant, const int* blocks, const size_t* smems, const int* want,
+                              int count);
+std::mutex& kernel_attr_mutex();
+cudaError_t launch_sim_lane_batch(const BatchDesc& b, bool coop, int grid, int block, size_t smem,
+                                  cudaStream_t stream);
+cudaError_t sim_lane_batch_configure(bool coop, size_t smem, int block, int* blocks_per_sm);
 cudaError_t launch_sim_warp_batch(const BatchDesc& b, bool cached_index, int grid, int block, size_t smem,
                                   cudaStream_t stream);
 cudaError_t sim_warp_batch_configure(bool cached_index, size_t smem, int block, int* blocks_per_sm);

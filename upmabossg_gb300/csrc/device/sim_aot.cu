@@ -38,7 +38,18 @@ extern "C" __global__ void __launch_bounds__(256, 3) mbg_sim_lane_coop(const Sim
     sim_lane_body<true>(p, smem);
 }
 
-// Batched instances (parameter sweeps), both variants.
+// Batched instances (parameter sweeps) in the lane layout, both reader-update variants.
+extern "C" __global__ void __launch_bounds__(256, 3) mbg_sim_lane_batch(const BatchDesc b) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    sim_lane_batch_body<false>(b, smem);
+}
+
+extern "C" __global__ void __launch_bounds__(256, 3) mbg_sim_lane_batch_coop(const BatchDesc b) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    sim_lane_batch_body<true>(b, smem);
+}
+
+// Batched instances (parameter sweeps) in the warp layout, both variants.
 extern "C" __global__ void __launch_bounds__(256, 4) mbg_sim_warp_batch(const BatchDesc b) {
     extern __shared__ __align__(16) unsigned char smem[];
     sim_warp_batch_body<true>(b, smem);
@@ -208,21 +219,22 @@ cudaError_t launch_sim_lane(const SimParams& p, bool coop, int grid, int block, 
     return cudaGetLastError();
 }
 
-cudaError_t sim_lane_configure(bool coop, size_t smem, int block, int* blocks_per_sm) {
-    const void* f = coop ? (const void*)mbg_sim_lane_coop : (const void*)mbg_sim_lane;
+namespace {
+
+// Occupancy of a lane-layout kernel with the smallest shared-memory carve-out that keeps as many
+// blocks resident: the rest of the SM's 256 KiB is L1, which caches the model tables every step
+// reads. The driver rounds the percentage up to a supported carve-out, so the largest percentage
+// at or below the need is tried first, then larger ones if that carve-out holds fewer blocks.
+cudaError_t lane_configure(const void* f, size_t smem, int block, int* blocks_per_sm) {
     cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e == cudaSuccess) e = cudaFuncSetAttribute(f, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
     if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, f, block, smem);
     if (e != cudaSuccess || *blocks_per_sm < 1) return e;
-    // the smallest shared-memory carve-out that keeps as many blocks resident leaves the rest of
-    // the SM's 256 KiB to L1, which caches the model tables every step reads
     int dev = 0, per_sm = 0, reserved = 0;
     e = cudaGetDevice(&dev);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev);
     if (e != cudaSuccess || per_sm <= 0) return e;
-    // the driver rounds the percentage up to a supported carve-out: try the largest percentage at
-    // or below the need first, and step up if that carve-out holds fewer blocks
     const int want = *blocks_per_sm;
     const double need = (double)want * (double)(smem + (size_t)reserved);
     const int lo = (int)std::floor(100.0 * need / per_sm), hi = (int)std::ceil(100.0 * need / per_sm);
@@ -232,6 +244,71 @@ cudaError_t sim_lane_configure(bool coop, size_t smem, int block, int* blocks_pe
         if (e != cudaSuccess || *blocks_per_sm >= want) return e;
     }
     return e;
+}
+
+// Attributes of one kernel shared by several launch shapes (blocks[i], smems[i], want[i] resident
+// blocks per SM): the largest dynamic shared memory of any shape and the smallest carve-out at
+// which every shape keeps its resident blocks.
+cudaError_t shared_limits(const void* f, const int* blocks, const size_t* smems, const int* want, int count) {
+    size_t max_smem = 0;
+    double need = 0;
+    int dev = 0, per_sm = 0, reserved = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev);
+    if (e != cudaSuccess || per_sm <= 0) return e;
+    for (int i = 0; i < count; ++i) {
+        max_smem = smems[i] > max_smem ? smems[i] : max_smem;
+        const double d = (double)want[i] * (double)(smems[i] + (size_t)reserved);
+        need = d > need ? d : need;
+    }
+    e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)max_smem);
+    if (e != cudaSuccess) return e;
+    const int lo = (int)std::floor(100.0 * need / per_sm), hi = (int)std::ceil(100.0 * need / per_sm);
+    for (int pct : {lo, hi, 100}) {
+        e = cudaFuncSetAttribute(f, cudaFuncAttributePreferredSharedMemoryCarveout, pct < 100 ? pct : 100);
+        if (e != cudaSuccess) return e;
+        bool ok = true;
+        for (int i = 0; i < count && ok; ++i) {
+            int bps = 0;
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, f, blocks[i], smems[i]);
+            if (e != cudaSuccess) return e;
+            ok = bps >= want[i];
+        }
+        if (ok) return cudaSuccess;
+    }
+    return cudaSuccess;
+}
+
+}  // namespace
+
+cudaError_t sim_kernel_limits(int kernel, bool variant, const int* blocks, const size_t* smems, const int* want,
+                              int count) {
+    const void* f = nullptr;
+    switch (kernel) {
+        case 0: f = variant ? (const void*)mbg_sim_lane_coop : (const void*)mbg_sim_lane; break;
+        case 1: f = variant ? (const void*)mbg_sim_lane_batch_coop : (const void*)mbg_sim_lane_batch; break;
+        case 2: f = variant ? (const void*)mbg_sim_warp_batch : (const void*)mbg_sim_warp_batch_gather; break;
+        default: f = variant ? (const void*)mbg_sim_warp : (const void*)mbg_sim_warp_gather; break;
+    }
+    return shared_limits(f, blocks, smems, want, count);
+}
+
+cudaError_t sim_lane_configure(bool coop, size_t smem, int block, int* blocks_per_sm) {
+    return lane_configure(coop ? (const void*)mbg_sim_lane_coop : (const void*)mbg_sim_lane, smem, block,
+                          blocks_per_sm);
+}
+
+cudaError_t launch_sim_lane_batch(const BatchDesc& b, bool coop, int grid, int block, size_t smem,
+                                  cudaStream_t stream) {
+    if (coop) mbg_sim_lane_batch_coop<<<grid, block, smem, stream>>>(b);
+    else mbg_sim_lane_batch<<<grid, block, smem, stream>>>(b);
+    return cudaGetLastError();
+}
+
+cudaError_t sim_lane_batch_configure(bool coop, size_t smem, int block, int* blocks_per_sm) {
+    return lane_configure(coop ? (const void*)mbg_sim_lane_batch_coop : (const void*)mbg_sim_lane_batch, smem,
+                          block, blocks_per_sm);
 }
 
 size_t sim_lane_smem(int n, int block) { return (size_t)block * lane_smem_bytes(n) + lane_block_extra(block); }

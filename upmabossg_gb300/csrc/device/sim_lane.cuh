@@ -33,8 +33,8 @@ struct LaneSmem {
     unsigned* wtouch;         // [T / 32]
 };
 
-__device__ __forceinline__ LaneSmem lane_smem_at(unsigned char* base, int n, int T) {
-    const int G = lane_groups(n);
+// `G` rows of T entries per array: the largest model's group count in a batched launch.
+__device__ __forceinline__ LaneSmem lane_smem_at(unsigned char* base, int G, int T) {
     LaneSmem m;
     m.fen = reinterpret_cast<unsigned long long*>(base);
     m.st = reinterpret_cast<unsigned*>(m.fen + (size_t)G * T);
@@ -232,7 +232,7 @@ __device__ __forceinline__ int lane_pick(const SimParams& p, const unsigned* st,
 // whose rate changed.
 template <bool ATOMIC>
 __device__ __forceinline__ unsigned long long lane_reader(const SimParams& p, unsigned e, const LaneSmem& m, int T,
-                                                          int G, int col, bool& out) {
+                                                          int col, bool& out) {
     const int dn = (int)(e >> 16);
     const int kd = (int)((e >> 8) & 0xffu);
     const unsigned pos = e & 0xffu;
@@ -274,6 +274,7 @@ __device__ __forceinline__ unsigned long long lane_reader(const SimParams& p, un
     }
     const unsigned long long delta = r_new - r_old;
     if (delta != 0ull) {
+        const int G = lane_groups(p.n);
         if (ATOMIC) fen_add_atomic(m.fen + col, T, G, g, delta);
         else fen_add(m.fen + col, T, G, g, delta);
         out |= __ldg(p.out_pos + dn) >= 0;
@@ -283,11 +284,11 @@ __device__ __forceinline__ unsigned long long lane_reader(const SimParams& p, un
 
 // After node k flipped in this lane's trajectory: re-evaluates every node whose rate reads k (and
 // k itself) in turn. Returns whether an output node's rate changed.
-__device__ __forceinline__ bool lane_update(const SimParams& p, int k, const LaneSmem& m, int T, int G, int col,
+__device__ __forceinline__ bool lane_update(const SimParams& p, int k, const LaneSmem& m, int T, int col,
                                             unsigned long long& total) {
     const int d0 = (int)__ldg(p.dep_off + k), d1 = (int)__ldg(p.dep_off + k + 1);
     bool out = false;
-    for (int q = d0; q < d1; ++q) total += lane_reader<false>(p, __ldg(p.deps + q), m, T, G, col, out);
+    for (int q = d0; q < d1; ++q) total += lane_reader<false>(p, __ldg(p.deps + q), m, T, col, out);
     return out;
 }
 
@@ -295,13 +296,14 @@ __device__ __forceinline__ bool lane_update(const SimParams& p, int k, const Lan
 // reader lists of the 32 flipped nodes are concatenated and dealt out one entry per lane, so a
 // step costs ceil(total length / 32) rounds instead of the longest list. Entries of one trajectory
 // patch its shared-memory rows with atomics; lanes whose output-node rates changed are marked in
-// the warp's wtouch word. The owners read their new totals from their trees afterwards.
-__device__ __forceinline__ void lane_coop_update(const SimParams& p, const LaneSmem& m, int T, int G, int wbase,
-                                                 unsigned lane, int k) {
+// the warp's wtouch word. `owner(o)` gives the model of lane o's trajectory (called by all lanes).
+template <class Owner>
+__device__ __forceinline__ void lane_coop_update(const SimParams& mine, Owner owner, const LaneSmem& m, int T,
+                                                 int wbase, unsigned lane, int k) {
     int d0 = 0, c = 0;
     if (k >= 0) {
-        d0 = (int)__ldg(p.dep_off + k);
-        c = (int)__ldg(p.dep_off + k + 1) - d0;
+        d0 = (int)__ldg(mine.dep_off + k);
+        c = (int)__ldg(mine.dep_off + k + 1) - d0;
     }
     int inc = c;
 #pragma unroll
@@ -324,153 +326,264 @@ __device__ __forceinline__ void lane_coop_update(const SimParams& p, const LaneS
         }
         const int o_ex = __shfl_sync(MBG_FULL, ex, o);
         const int o_d0 = __shfl_sync(MBG_FULL, d0, o);
+        const SimParams& po = owner(o);
         bool out = false;
-        if (q < C) lane_reader<true>(p, __ldg(p.deps + o_d0 + (q - o_ex)), m, T, G, wbase + o, out);
+        if (q < C) lane_reader<true>(po, __ldg(po.deps + o_d0 + (q - o_ex)), m, T, wbase + o, out);
         touched |= __reduce_or_sync(MBG_FULL, out ? 1u << o : 0u);
     }
     if (lane == 0u) m.wtouch[wbase >> 5] = touched;
     __syncwarp();
 }
 
+// Registers of the trajectory a lane is running.
+struct LaneTraj {
+    unsigned long long j = 0, step = 0, t = 0, t1 = 0, total = 0;
+    unsigned trans = 0, so = 0;
+    float h = 0.f;
+    unsigned char status = TRAJ_CONTINUE;
+    bool have = false, done = false;
+    WindowAcc acc;
+};
+
+// End-state counts of one lane (or warp) until they are added to a counter block.
+struct LaneCounts {
+    unsigned long long trans = 0, steps = 0;
+    unsigned fin = 0, fix = 0, lim = 0, err = 0;
+    __device__ __forceinline__ void flush(unsigned long long* counters) {
+        if (trans) atomicAdd(counters + CNT_TRANSITIONS, trans);
+        if (steps) atomicAdd(counters + CNT_STEPS, steps);
+        if (fin) atomicAdd(counters + CNT_FINISHED, (unsigned long long)fin);
+        if (fix) atomicAdd(counters + CNT_FIXED, (unsigned long long)fix);
+        if (lim) atomicAdd(counters + CNT_STEP_LIMIT, (unsigned long long)lim);
+        if (err) atomicAdd(counters + CNT_ERROR, (unsigned long long)err);
+        *this = LaneCounts();
+    }
+    // all lanes of the warp: one atomic per counter
+    __device__ __forceinline__ void flush_warp(unsigned long long* counters, unsigned lane) {
+        for (int o = 16; o > 0; o >>= 1) {
+            trans += __shfl_xor_sync(MBG_FULL, trans, o);
+            steps += __shfl_xor_sync(MBG_FULL, steps, o);
+        }
+        fin = __reduce_add_sync(MBG_FULL, fin);
+        fix = __reduce_add_sync(MBG_FULL, fix);
+        lim = __reduce_add_sync(MBG_FULL, lim);
+        err = __reduce_add_sync(MBG_FULL, err);
+        if (lane == 0u) flush(counters);
+    }
+};
+
+// A new trajectory's registers once its state is set up.
+__device__ __forceinline__ void lane_begin(const SimParams& p, const LaneSmem& m, int T, int col, LaneTraj& tr) {
+    tr.have = true;
+    tr.t = 0;
+    tr.step = 0;
+    tr.trans = 0;
+    tr.so = lane_out_index(p, m.st + col, T);
+    tr.h = lane_entropy(p, m.st + col, m.act + col, T);
+    win_begin(tr.acc, p, tr.so);
+}
+
+// One Gillespie step up to the flip (src/jit_kernels/simulation.cu:104-147): fixed point, step
+// cap, dt and window accumulation, end of time, pick and flip. Returns the flipped node or -1;
+// tr.status says whether the trajectory ended. Without `coop` the readers are updated here.
+__device__ __forceinline__ int lane_step_front(const SimParams& p, const LaneSmem& m, int T, int col, LaneTraj& tr,
+                                               bool coop) {
+    tr.status = TRAJ_CONTINUE;
+    if (tr.total == 0ull) {
+        if (p.discrete) win_discrete(p, tr.step, tr.so, 0.f, true);
+        else win_slice(tr.acc, p, tr.t, p.max_time_fx, tr.so, 0.f, true);
+        tr.t = p.max_time_fx;
+        tr.status = TRAJ_FIXED_POINT;
+        return -1;
+    }
+    if (tr.step >= p.max_steps) {
+        tr.status = TRAJ_STEP_LIMIT;
+        return -1;
+    }
+    const u32x4 d = philox_step(p.seed, p.traj_base + tr.j, tr.step);
+    tr.t1 = next_time(p, tr.t, tr.step, p.discrete ? 0.f : neg_log_u(d.x), tr.total);
+    if (p.discrete) win_discrete(p, tr.step, tr.so, tr.h, true);
+    else win_slice(tr.acc, p, tr.t, tr.t1, tr.so, tr.h, true);
+    ++tr.step;
+    if (tr.t1 >= p.max_time_fx) {
+        tr.t = p.max_time_fx;
+        tr.status = TRAJ_FINISHED;
+        return -1;
+    }
+    const int G = lane_groups(p.n);
+    unsigned* st = m.st + col;
+    const int k = lane_pick(p, st, m.act + col, m.fen + col, T, G, 1 << (31 - __clz(G)),
+                            pick_target(d.y, d.z, tr.total));
+    if (k < 0 || k >= p.n) {
+        tr.status = TRAJ_ERROR;
+        atomicOr(p.error_flag, (unsigned)DEV_ERR_PICK);
+        return -1;
+    }
+    st[(k >> 5) * T] ^= 1u << (k & 31);
+    if (!coop && lane_update(p, k, m, T, col, tr.total)) tr.h = lane_entropy(p, st, m.act + col, T);
+    return k;
+}
+
+// After the readers of k were updated cooperatively: the new total from the tree, the entropy
+// when an output node's rate changed.
+__device__ __forceinline__ void lane_after_coop(const SimParams& p, const LaneSmem& m, int T, int col, int wbase,
+                                                unsigned lane, LaneTraj& tr) {
+    tr.total = fen_total(m.fen + col, T, lane_groups(p.n));
+    if ((m.wtouch[wbase >> 5] >> lane) & 1u) tr.h = lane_entropy(p, m.st + col, m.act + col, T);
+}
+
+// Completes the step: output state, clock, transition count; at the end of the trajectory its
+// window run, final state, optional records, fixed point and counts.
+__device__ __forceinline__ void lane_step_back(const SimParams& p, const LaneSmem& m, int T, int col, LaneTraj& tr,
+                                               int k, LaneCounts& c) {
+    if (k >= 0) {
+        const short op = __ldg(p.out_pos + k);
+        if (op >= 0) tr.so ^= 1u << op;
+        tr.t = tr.t1;
+        ++tr.trans;
+    }
+    const unsigned char status = tr.status;
+    if (status == TRAJ_CONTINUE) return;
+    const unsigned* st = m.st + col;
+    if (!p.discrete && status != TRAJ_ERROR) win_end(tr.acc, p, tr.t, true);
+    c.trans += tr.trans;
+    c.steps += tr.step + (status == TRAJ_FIXED_POINT ? 1 : 0);
+    c.fin += status == TRAJ_FINISHED;
+    c.fix += status == TRAJ_FIXED_POINT;
+    c.lim += status == TRAJ_STEP_LIMIT;
+    c.err += status == TRAJ_ERROR;
+    record_end_scalar(p, tr.j, status, tr.t, tr.trans, tr.so);
+    if (p.traj_state)
+        for (int w = 0; w < p.words; ++w) p.traj_state[tr.j * p.words + w] = st[w * T];
+    if (status == TRAJ_FIXED_POINT) {
+        const unsigned slot = atomicAdd(p.fp_count, 1u);
+        if (slot < p.fp_capacity) {
+            for (int w = 0; w < p.words; ++w) p.fp_states[(unsigned long long)slot * p.words + w] = st[w * T];
+        } else {
+            atomicOr(p.error_flag, (unsigned)DEV_ERR_FP_OVERFLOW);
+        }
+    }
+    tr.have = false;
+}
+
+// One simulation: lanes take trajectory ids from the run's work counter.
 template <bool COOP>
 __device__ void sim_lane_body(const SimParams& p, unsigned char* smem) {
     const int T = (int)blockDim.x;
     const unsigned lane = threadIdx.x & 31u;
     const int wbase = (int)(threadIdx.x & ~31u);
-    const int G = lane_groups(p.n);
-    const int top = 1 << (31 - __clz(G));
-    const LaneSmem m = lane_smem_at(smem, p.n, T);
+    const LaneSmem m = lane_smem_at(smem, lane_groups(p.n), T);
     const int col = (int)threadIdx.x;
-    unsigned* st = m.st + col;
-    const unsigned* act = m.act + col;
-    const unsigned long long* fen = m.fen + col;
-
-    unsigned long long j = 0, step = 0, t = 0, total = 0;
-    unsigned trans = 0, so = 0;
-    float h = 0.f;
-    bool have = false, done = false;
-    WindowAcc acc;
-    unsigned long long c_trans = 0, c_steps = 0;
-    unsigned c_fin = 0, c_fix = 0, c_lim = 0, c_err = 0;
-
+    LaneTraj tr;
+    LaneCounts c;
     for (;;) {
-        const unsigned need = __ballot_sync(MBG_FULL, !have && !done);
+        const unsigned need = __ballot_sync(MBG_FULL, !tr.have && !tr.done);
         if (need) {
             unsigned long long base = 0;
             const int leader = __ffs(need) - 1;
             if ((int)lane == leader) base = atomicAdd(p.counters + CNT_WORK, (unsigned long long)__popc(need));
             base = __shfl_sync(MBG_FULL, base, leader);
             bool start = false;
-            if (!have && !done) {
-                j = base + __popc(need & ((1u << lane) - 1u));
-                if (j < p.n_traj) start = true;
-                else done = true;
+            if (!tr.have && !tr.done) {
+                tr.j = base + __popc(need & ((1u << lane) - 1u));
+                if (tr.j < p.n_traj) start = true;
+                else tr.done = true;
             }
             unsigned init = __ballot_sync(MBG_FULL, start);
             while (init) {
                 const int L = __ffs(init) - 1;
                 init &= init - 1u;
-                const unsigned long long jl = __shfl_sync(MBG_FULL, j, L);
+                const unsigned long long jl = __shfl_sync(MBG_FULL, tr.j, L);
                 const unsigned long long tot = lane_coop_init(p, m, T, wbase + L, p.traj_base + jl, lane);
-                if ((int)lane == L) total = tot;
+                if ((int)lane == L) tr.total = tot;
             }
-            if (start) {
-                have = true;
-                t = 0;
-                step = 0;
-                trans = 0;
-                so = lane_out_index(p, st, T);
-                h = lane_entropy(p, st, act, T);
-                win_begin(acc, p, so);
-            }
+            if (start) lane_begin(p, m, T, col, tr);
         }
-        if (__all_sync(MBG_FULL, done)) break;
-        if (!COOP && !have) continue;
-
-        unsigned char status = TRAJ_CONTINUE;
-        int k = -1;
-        unsigned long long t1 = 0;
-        if (have) {
-            if (total == 0ull) {
-                if (p.discrete) win_discrete(p, step, so, 0.f, true);
-                else win_slice(acc, p, t, p.max_time_fx, so, 0.f, true);
-                t = p.max_time_fx;
-                status = TRAJ_FIXED_POINT;
-            } else if (step >= p.max_steps) {
-                status = TRAJ_STEP_LIMIT;
-            } else {
-                const u32x4 d = philox_step(p.seed, p.traj_base + j, step);
-                t1 = next_time(p, t, step, p.discrete ? 0.f : neg_log_u(d.x), total);
-                if (p.discrete) win_discrete(p, step, so, h, true);
-                else win_slice(acc, p, t, t1, so, h, true);
-                ++step;
-                if (t1 >= p.max_time_fx) {
-                    t = p.max_time_fx;
-                    status = TRAJ_FINISHED;
-                } else {
-                    k = lane_pick(p, st, act, fen, T, G, top, pick_target(d.y, d.z, total));
-                    if (k < 0 || k >= p.n) {
-                        k = -1;
-                        status = TRAJ_ERROR;
-                        atomicOr(p.error_flag, (unsigned)DEV_ERR_PICK);
-                    } else {
-                        st[(k >> 5) * T] ^= 1u << (k & 31);
-                        if (!COOP && lane_update(p, k, m, T, G, col, total)) h = lane_entropy(p, st, act, T);
-                    }
-                }
-            }
-        }
+        if (__all_sync(MBG_FULL, tr.done)) break;
+        if (!COOP && !tr.have) continue;
+        const int k = tr.have ? lane_step_front(p, m, T, col, tr, COOP) : -1;
         if (COOP) {
-            lane_coop_update(p, m, T, G, wbase, lane, k);
-            if (k >= 0) {
-                total = fen_total(fen, T, G);
-                if ((m.wtouch[wbase >> 5] >> lane) & 1u) h = lane_entropy(p, st, act, T);
-            }
+            lane_coop_update(p, [&](int) -> const SimParams& { return p; }, m, T, wbase, lane, k);
+            if (k >= 0) lane_after_coop(p, m, T, col, wbase, lane, tr);
         }
-        if (k >= 0) {
-            const short op = __ldg(p.out_pos + k);
-            if (op >= 0) so ^= 1u << op;
-            t = t1;
-            ++trans;
-        }
-        if (status != TRAJ_CONTINUE) {
-            if (!p.discrete && status != TRAJ_ERROR) win_end(acc, p, t, true);
-            c_trans += trans;
-            c_steps += step + (status == TRAJ_FIXED_POINT ? 1 : 0);
-            c_fin += status == TRAJ_FINISHED;
-            c_fix += status == TRAJ_FIXED_POINT;
-            c_lim += status == TRAJ_STEP_LIMIT;
-            c_err += status == TRAJ_ERROR;
-            record_end_scalar(p, j, status, t, trans, so);
-            if (p.traj_state)
-                for (int w = 0; w < p.words; ++w) p.traj_state[j * p.words + w] = st[w * T];
-            if (status == TRAJ_FIXED_POINT) {
-                const unsigned slot = atomicAdd(p.fp_count, 1u);
-                if (slot < p.fp_capacity) {
-                    for (int w = 0; w < p.words; ++w) p.fp_states[(unsigned long long)slot * p.words + w] = st[w * T];
+        if (tr.have) lane_step_back(p, m, T, col, tr, k, c);
+    }
+    c.flush_warp(p.counters, lane);
+}
+
+// Many instances in one launch (batched sweeps): lanes take work items from one counter over the
+// instances' trajectory counts; each lane runs its item with its instance's model and adds its
+// counts to that instance's counters when it moves to another instance. Shared memory has rows
+// for the largest instance of the launch (b.rows groups).
+template <bool COOP>
+__device__ void sim_lane_batch_body(const BatchDesc& b, unsigned char* smem) {
+    const int T = (int)blockDim.x;
+    const unsigned lane = threadIdx.x & 31u;
+    const int wbase = (int)(threadIdx.x & ~31u);
+    const LaneSmem m = lane_smem_at(smem, b.rows, T);
+    const int col = (int)threadIdx.x;
+    const unsigned long long items = __ldg(b.prefix + b.n_inst);
+    const SimParams* pp = b.params;
+    int cur = -1;
+    LaneTraj tr;
+    LaneCounts c;
+    for (;;) {
+        const unsigned need = __ballot_sync(MBG_FULL, !tr.have && !tr.done);
+        if (need) {
+            unsigned long long base = 0;
+            const int leader = __ffs(need) - 1;
+            if ((int)lane == leader) base = atomicAdd(b.work, (unsigned long long)__popc(need));
+            base = __shfl_sync(MBG_FULL, base, leader);
+            bool start = false;
+            if (!tr.have && !tr.done) {
+                const unsigned long long w = base + __popc(need & ((1u << lane) - 1u));
+                if (w < items) {
+                    int lo = 0, hi = b.n_inst;  // prefix[lo] <= w < prefix[hi]
+                    while (hi - lo > 1) {
+                        const int mid = (lo + hi) >> 1;
+                        if (__ldg(b.prefix + mid) <= w) lo = mid;
+                        else hi = mid;
+                    }
+                    if (lo != cur) {
+                        if (cur >= 0) c.flush(b.params[cur].counters);
+                        cur = lo;
+                    }
+                    pp = b.params + lo;
+                    tr.j = w - __ldg(b.prefix + lo);
+                    start = true;
                 } else {
-                    atomicOr(p.error_flag, (unsigned)DEV_ERR_FP_OVERFLOW);
+                    tr.done = true;
                 }
             }
-            have = false;
+            unsigned init = __ballot_sync(MBG_FULL, start);
+            while (init) {
+                const int L = __ffs(init) - 1;
+                init &= init - 1u;
+                const SimParams* pl = reinterpret_cast<const SimParams*>(
+                    __shfl_sync(MBG_FULL, reinterpret_cast<unsigned long long>(pp), L));
+                const unsigned long long jl = __shfl_sync(MBG_FULL, tr.j, L);
+                const unsigned long long tot = lane_coop_init(*pl, m, T, wbase + L, pl->traj_base + jl, lane);
+                if ((int)lane == L) tr.total = tot;
+            }
+            if (start) lane_begin(*pp, m, T, col, tr);
         }
+        if (__all_sync(MBG_FULL, tr.done)) break;
+        if (!COOP && !tr.have) continue;
+        const SimParams& p = *pp;
+        const int k = tr.have ? lane_step_front(p, m, T, col, tr, COOP) : -1;
+        if (COOP) {
+            lane_coop_update(
+                p,
+                [&](int o) -> const SimParams& {
+                    return *reinterpret_cast<const SimParams*>(
+                        __shfl_sync(MBG_FULL, reinterpret_cast<unsigned long long>(pp), o));
+                },
+                m, T, wbase, lane, k);
+            if (k >= 0) lane_after_coop(p, m, T, col, wbase, lane, tr);
+        }
+        if (tr.have) lane_step_back(p, m, T, col, tr, k, c);
     }
-    for (int o = 16; o > 0; o >>= 1) {
-        c_trans += __shfl_xor_sync(MBG_FULL, c_trans, o);
-        c_steps += __shfl_xor_sync(MBG_FULL, c_steps, o);
-    }
-    c_fin = __reduce_add_sync(MBG_FULL, c_fin);
-    c_fix = __reduce_add_sync(MBG_FULL, c_fix);
-    c_lim = __reduce_add_sync(MBG_FULL, c_lim);
-    c_err = __reduce_add_sync(MBG_FULL, c_err);
-    if (lane == 0u) {
-        atomicAdd(p.counters + CNT_TRANSITIONS, c_trans);
-        atomicAdd(p.counters + CNT_STEPS, c_steps);
-        atomicAdd(p.counters + CNT_FINISHED, (unsigned long long)c_fin);
-        atomicAdd(p.counters + CNT_FIXED, (unsigned long long)c_fix);
-        atomicAdd(p.counters + CNT_STEP_LIMIT, (unsigned long long)c_lim);
-        atomicAdd(p.counters + CNT_ERROR, (unsigned long long)c_err);
-    }
+    if (cur >= 0) c.flush(b.params[cur].counters);
 }
 
 }  // namespace mbg

@@ -109,7 +109,8 @@ struct BatchDesc {
     const unsigned long long* prefix;  // n_inst + 1 cumulative trajectory counts
     int n_inst;
     unsigned long long* work;          // work-item counter
-    unsigned slice_bytes;              // per warp: SimParams copy (16-byte padded) + largest warp slice
+    unsigned slice_bytes;              // warp layout, per warp: SimParams copy (16-byte padded) + largest slice
+    int rows;                          // lane layout: shared-memory rows (groups of the largest instance)
 };
 
 // Fixed-point hash table and compacted output of one batched instance.

@@ -1,6 +1,7 @@
-// Batched parameter sweeps: every instance's model image and results live in a few arenas, all
-// instances run in one persistent launch of the warp-per-trajectory kernel, and the clearing,
-// simulation, fixed-point aggregation and counter read-back are captured once into a CUDA graph.
+// Batched parameter sweeps: every instance's model image and results live in a few arenas; the
+// instances are grouped by model size into classes, each class runs in one persistent launch of
+// the lane or the warp layout with its own launch shape, and the clearing, the class launches, the
+// fixed-point aggregation and the counter read-back are captured once into a CUDA graph.
 // The reference has no batching: a sweep is one CLI run per instance (src/main.cpp:101-169),
 // each with its own NVRTC compilation (src/kernel_compiler.cpp:61-164) and batch loop
 // (src/simulation_runner.cu:54-180).
@@ -46,15 +47,27 @@ void* dmalloc(size_t bytes, std::vector<void*>& owned) {
 }
 
 constexpr size_t kSmallPerInst = 96;  // 8 u64 counters, error word, unique fixed points
+constexpr int kClasses = 8;  // up to 32, 64, ..., 4096 nodes, larger
+constexpr size_t kSmemLimit = 227 * 1024;
 
 }  // namespace
+
+int batch_size_class(int n) {
+    const int g = (n + 31) / 32;  // 32-node groups
+    int c = 0;
+    while ((1 << c) < g && c < kClasses - 1) ++c;
+    return c;
+}
 
 Batch::~Batch() {
     if (exec) cudaGraphExecDestroy(exec);
     if (graph) cudaGraphDestroy(graph);
     if (capture_stream) cudaStreamDestroy(capture_stream);
-    for (cudaEvent_t e : {ev0, ev1, evk0, evk1})
+    for (cudaEvent_t e : {ev0, ev1})
         if (e) cudaEventDestroy(e);
+    for (Class& k : classes)
+        for (cudaEvent_t e : {k.e0, k.e1})
+            if (e) cudaEventDestroy(e);
     if (small_host) cudaFreeHost(small_host);
     for (void* p : owned) cudaFree(p);
 }
@@ -62,6 +75,10 @@ Batch::~Batch() {
 void Batch::create(const std::vector<const CompiledModel*>& models, const std::vector<uint64_t>& n_traj,
                    const std::vector<uint64_t>& seeds, const mbg_batch_opts& o) {
     if (models.empty()) throw ArgError("empty batch");
+    if (o.block_size && (o.block_size % 32 != 0 || o.block_size > 256))
+        throw ArgError("block_size must be a multiple of 32, at most 256");
+    if (o.layout != 0 && o.layout != MBG_LAYOUT_LANE && o.layout != MBG_LAYOUT_WARP)
+        throw ArgError("batch layout must be 0 (auto), MBG_LAYOUT_LANE or MBG_LAYOUT_WARP");
     opts = o;
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
@@ -75,6 +92,32 @@ void Batch::create(const std::vector<const CompiledModel*>& models, const std::v
 
     const size_t n = models.size();
     inst.resize(n);
+    // size classes; the class-ordered arrays (params, fixed-point slots) list class 0's members
+    // first, then class 1's, ...
+    std::vector<Class> all(kClasses);
+    for (size_t i = 0; i < n; ++i) {
+        Inst& x = inst[i];
+        x.cm = *models[i];
+        x.n_traj = n_traj.empty() || n_traj[i] == 0 ? x.cm.sample_count : n_traj[i];
+        x.seed = seeds.empty() ? x.cm.seed : seeds[i];
+        check_model_limits(x.cm, x.n_traj);
+        if (x.cm.n_out > 32) throw ModelError("batched instances support at most 32 outputs");
+        Class& k = all[batch_size_class(x.cm.n)];
+        k.members.push_back((int)i);
+        k.max_n = std::max(k.max_n, x.cm.n);
+        k.traj += x.n_traj;
+    }
+    for (Class& k : all)
+        if (!k.members.empty()) classes.push_back(std::move(k));
+    std::vector<int> order;  // class order -> instance
+    for (size_t c = 0; c < classes.size(); ++c) {
+        classes[c].first = order.size();
+        for (int i : classes[c].members) {
+            inst[i].cls = (int)c;
+            order.push_back(i);
+        }
+    }
+
     std::vector<DeviceLayout> dls(n);
     Layout ml, rl, pl, fl;
     struct Off {
@@ -82,17 +125,10 @@ void Batch::create(const std::vector<const CompiledModel*>& models, const std::v
         size_t hist, th, fin, fp_count, slot_cnt, rep, fp_states, out_states, out_cnt;
     };
     std::vector<Off> off(n);
-    std::vector<unsigned long long> prefix(n + 1, 0);
     for (size_t i = 0; i < n; ++i) {
         Inst& x = inst[i];
-        x.cm = *models[i];
         const CompiledModel& cm = x.cm;
-        x.n_traj = n_traj.empty() || n_traj[i] == 0 ? cm.sample_count : n_traj[i];
-        x.seed = seeds.empty() ? cm.seed : seeds[i];
-        check_model_limits(cm, x.n_traj);
-        if (cm.n_out > 32) throw ModelError("batched instances support at most 32 outputs");
-        max_n = std::max(max_n, cm.n);
-        prefix[i + 1] = prefix[i] + x.n_traj;
+        total_traj += x.n_traj;
         dls[i] = layout_model(cm);
         const DeviceLayout& d = dls[i];
         Off& f = off[i];
@@ -120,8 +156,7 @@ void Batch::create(const std::vector<const CompiledModel*>& models, const std::v
         f.out_states = fl.add((size_t)cap * cm.words * 4);
         f.out_cnt = fl.add((size_t)cap * 4);
     }
-    total_traj = prefix[n];
-    small_bytes = n * kSmallPerInst + 8;  // + the work counter
+    small_bytes = n * kSmallPerInst + 8 * classes.size();  // + one work counter per class
     const size_t small_off = rl.add(small_bytes);
 
     // model arena: one staging buffer, one copy
@@ -159,7 +194,8 @@ void Batch::create(const std::vector<const CompiledModel*>& models, const std::v
 
     std::vector<SimParams> prms(n);
     std::vector<FpSlots> fps(n);
-    for (size_t i = 0; i < n; ++i) {
+    for (size_t pos = 0; pos < n; ++pos) {
+        const size_t i = (size_t)order[pos];
         Inst& x = inst[i];
         const Off& f = off[i];
         SimParams& p = x.prm;
@@ -194,42 +230,84 @@ void Batch::create(const std::vector<const CompiledModel*>& models, const std::v
         x.fp.out_states = reinterpret_cast<unsigned*>(fpa + f.out_states);
         x.fp.out_cnt = reinterpret_cast<unsigned*>(fpa + f.out_cnt);
         x.fp.n_unique = reinterpret_cast<unsigned*>(small_dev + x.small_off + 8 * CNT_COUNT + 4);
-        prms[i] = p;
-        fps[i] = x.fp;
+        prms[pos] = p;
+        fps[pos] = x.fp;
     }
     d_params = static_cast<SimParams*>(dmalloc(n * sizeof(SimParams), owned));
     d_fps = static_cast<FpSlots*>(dmalloc(n * sizeof(FpSlots), owned));
-    d_prefix = static_cast<unsigned long long*>(dmalloc((n + 1) * 8, owned));
     ck(cudaMemcpy(d_params, prms.data(), n * sizeof(SimParams), cudaMemcpyHostToDevice), "cudaMemcpy H2D");
     ck(cudaMemcpy(d_fps, fps.data(), n * sizeof(FpSlots), cudaMemcpyHostToDevice), "cudaMemcpy H2D");
-    ck(cudaMemcpy(d_prefix, prefix.data(), (n + 1) * 8, cudaMemcpyHostToDevice), "cudaMemcpy H2D");
-    desc.params = d_params;
-    desc.prefix = d_prefix;
-    desc.n_inst = (int)n;
-    desc.work = reinterpret_cast<unsigned long long*>(small_dev + n * kSmallPerInst);
+
+    // per class: trajectory prefixes over its members, and a pilot of about 256k trajectories
+    // (every member keeps at least one) for timing launch shapes
+    for (size_t c = 0; c < classes.size(); ++c) {
+        Class& k = classes[c];
+        const size_t m = k.members.size();
+        std::vector<unsigned long long> prefix(m + 1, 0), pilot(m + 1, 0);
+        const double scale = std::min(1.0, 262144.0 / (double)k.traj);
+        for (size_t q = 0; q < m; ++q) {
+            const uint64_t nt = inst[k.members[q]].n_traj;
+            prefix[q + 1] = prefix[q] + nt;
+            pilot[q + 1] = pilot[q] + std::max<uint64_t>(1, (uint64_t)((double)nt * scale));
+        }
+        auto* dp = static_cast<unsigned long long*>(dmalloc((m + 1) * 8, owned));
+        auto* dq = static_cast<unsigned long long*>(dmalloc((m + 1) * 8, owned));
+        ck(cudaMemcpy(dp, prefix.data(), (m + 1) * 8, cudaMemcpyHostToDevice), "cudaMemcpy H2D");
+        ck(cudaMemcpy(dq, pilot.data(), (m + 1) * 8, cudaMemcpyHostToDevice), "cudaMemcpy H2D");
+        k.desc.params = d_params + k.first;
+        k.desc.prefix = dp;
+        k.desc.n_inst = (int)m;
+        k.desc.work = reinterpret_cast<unsigned long long*>(small_dev + n * kSmallPerInst + 8 * c);
+        k.desc.rows = (k.max_n + 31) / 32;
+        k.pilot = k.desc;
+        k.pilot.prefix = dq;
+        ck(cudaEventCreate(&k.e0), "cudaEventCreate");
+        ck(cudaEventCreate(&k.e1), "cudaEventCreate");
+    }
 
     ck(cudaStreamCreateWithFlags(&capture_stream, cudaStreamNonBlocking), "cudaStreamCreate");
-    for (cudaEvent_t* e : {&ev0, &ev1, &evk0, &evk1}) ck(cudaEventCreate(e), "cudaEventCreate");
-    const int blk = o.block_size > 0 ? o.block_size : 128;
-    if (blk % 32 != 0 || blk > 256) throw ArgError("block_size must be a multiple of 32, at most 256");
-    configure(blk, (size_t)(blk / 32) * sim_warp_batch_slice_bytes(max_n, true) <= 100 * 1024, o.blocks_per_sm);
+    for (cudaEvent_t* e : {&ev0, &ev1}) ck(cudaEventCreate(e), "cudaEventCreate");
+    // default shapes (the autotuner replaces them on the first run): the lane layout at 128
+    // threads per block where its shared memory fits, else the warp layout
+    for (size_t c = 0; c < classes.size(); ++c) {
+        Class& k = classes[c];
+        const int blk = o.block_size > 0 ? o.block_size : 128;
+        const bool lane_fits = sim_lane_smem(k.max_n, blk) <= kSmemLimit;
+        const int lay = o.layout ? o.layout : (lane_fits ? MBG_LAYOUT_LANE : MBG_LAYOUT_WARP);
+        const bool variant =
+            lay == MBG_LAYOUT_WARP && (size_t)(blk / 32) * sim_warp_batch_slice_bytes(k.max_n, true) <= 100 * 1024;
+        configure((int)c, lay, blk, variant);
+    }
+    build_graph();
 }
 
-void Batch::configure(int blk, bool cached, int blocks_per_sm) {
-    ck(cudaSetDevice(device), "cudaSetDevice");
-    slice_bytes = sim_warp_batch_slice_bytes(max_n, cached);
-    const size_t sm = (size_t)(blk / 32) * slice_bytes;
-    if (sm > 227 * 1024) throw ModelError("largest instance too large for the batched warp layout");
+void Batch::configure(int c, int lay, int blk, bool variant) {
+    Class& k = classes[c];
     int bps = 0;
-    ck(sim_warp_batch_configure(cached, sm, blk, &bps), "batched kernel occupancy");
+    size_t sm = 0;
+    if (lay == MBG_LAYOUT_LANE) {
+        sm = sim_lane_smem(k.max_n, blk);
+        if (sm > kSmemLimit) throw ModelError("largest instance of a size class too large for the batched lane layout");
+        ck(sim_lane_batch_configure(variant, sm, blk, &bps), "batched lane kernel occupancy");
+    } else {
+        const unsigned slice = sim_warp_batch_slice_bytes(k.max_n, variant);
+        sm = (size_t)(blk / 32) * slice;
+        if (sm > kSmemLimit) throw ModelError("largest instance of a size class too large for the batched warp layout");
+        ck(sim_warp_batch_configure(variant, sm, blk, &bps), "batched warp kernel occupancy");
+        k.desc.slice_bytes = k.pilot.slice_bytes = slice;
+    }
     if (bps < 1) throw CudaError("batched kernel cannot be resident with this block size");
-    if (blocks_per_sm > 0) bps = std::min(bps, blocks_per_sm);
-    block = blk;
-    cached_index = cached;
-    smem = sm;
-    grid = sms * bps;
-    desc.slice_bytes = slice_bytes;
-    build_graph();
+    if (opts.blocks_per_sm > 0) bps = std::min(bps, (int)opts.blocks_per_sm);
+    k.layout = lay;
+    k.block = blk;
+    k.variant = variant;
+    k.smem = sm;
+    k.grid = sms * bps;
+}
+
+cudaError_t Batch::launch_class(const Class& k, const BatchDesc& d, cudaStream_t s) const {
+    if (k.layout == MBG_LAYOUT_LANE) return launch_sim_lane_batch(d, k.variant, k.grid, k.block, k.smem, s);
+    return launch_sim_warp_batch(d, k.variant, k.grid, k.block, k.smem, s);
 }
 
 void Batch::build_graph() {
@@ -242,13 +320,17 @@ void Batch::build_graph() {
         graph = nullptr;
     }
     cudaStream_t s = capture_stream;
+    apply_limits();
     ck(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture");
     cudaError_t e = cudaMemsetAsync(result_arena, 0, result_bytes, s);
     if (e == cudaSuccess) e = cudaMemsetAsync(rep_arena, 0xFF, rep_bytes, s);
-    // external event-record nodes, so the kernel's own time can be read after each replay
-    if (e == cudaSuccess) e = cudaEventRecordWithFlags(evk0, s, cudaEventRecordExternal);
-    if (e == cudaSuccess) e = launch_sim_warp_batch(desc, cached_index, grid, block, smem, s);
-    if (e == cudaSuccess) e = cudaEventRecordWithFlags(evk1, s, cudaEventRecordExternal);
+    // one launch per size class, bracketed by external event-record nodes so that each class's
+    // kernel time can be read after every replay
+    for (const Class& k : classes) {
+        if (e == cudaSuccess) e = cudaEventRecordWithFlags(k.e0, s, cudaEventRecordExternal);
+        if (e == cudaSuccess) e = launch_class(k, k.desc, s);
+        if (e == cudaSuccess) e = cudaEventRecordWithFlags(k.e1, s, cudaEventRecordExternal);
+    }
     if (e == cudaSuccess) e = launch_fp_aggregate_batch(d_params, d_fps, (int)inst.size(), 8, s);
     if (e == cudaSuccess) e = cudaMemcpyAsync(small_host, small_dev, small_bytes, cudaMemcpyDeviceToHost, s);
     cudaGraph_t g = nullptr;
@@ -259,21 +341,99 @@ void Batch::build_graph() {
     ck(cudaGraphInstantiate(&exec, graph, 0), "cudaGraphInstantiate");
 }
 
+void Batch::autotune() {
+    // Per size class, every shape (lane layout: threads per block x reader-update variant; warp
+    // layout: threads per block x regulator-index cache) runs the class's pilot trajectories twice
+    // and the second run's kernel time decides. Pilot runs write into the result buffers, which
+    // the graph clears before every real run; a fixed-point buffer that fills up during the pilots
+    // only sets an error bit in those buffers.
+    cudaStream_t s = capture_stream;
+    for (size_t c = 0; c < classes.size(); ++c) {
+        Class& k = classes[c];
+        k.timings.clear();
+        double best = -1;
+        int best_lay = k.layout, best_blk = k.block;
+        bool best_var = k.variant;
+        for (int lay : {MBG_LAYOUT_LANE, MBG_LAYOUT_WARP}) {
+            if (opts.layout && lay != opts.layout) continue;
+            for (int blk : {64, 128, 256}) {
+                if (opts.block_size > 0 && blk != opts.block_size) continue;
+                for (int var = 0; var < 2; ++var) {
+                    if (lay == MBG_LAYOUT_LANE && sim_lane_smem(k.max_n, blk) > kSmemLimit) continue;
+                    if (lay == MBG_LAYOUT_WARP &&
+                        (size_t)(blk / 32) * sim_warp_batch_slice_bytes(k.max_n, var != 0) > 100 * 1024)
+                        continue;
+                    configure((int)c, lay, blk, var != 0);
+                    float ms = 0.f;
+                    for (int rep = 0; rep < 2; ++rep) {
+                        ck(cudaMemsetAsync(k.desc.work, 0, 8, s), "cudaMemsetAsync");
+                        ck(cudaEventRecord(ev0, s), "cudaEventRecord");
+                        ck(launch_class(k, k.pilot, s), "autotune launch");
+                        ck(cudaEventRecord(ev1, s), "cudaEventRecord");
+                        ck(cudaStreamSynchronize(s), "autotune run");
+                        ck(cudaEventElapsedTime(&ms, ev0, ev1), "cudaEventElapsedTime");
+                    }
+                    k.timings.push_back(mbg_batch_class_timing{lay, blk, var, 0, (double)ms});
+                    if (best < 0 || ms < best) {
+                        best = ms;
+                        best_lay = lay;
+                        best_blk = blk;
+                        best_var = var != 0;
+                    }
+                }
+            }
+        }
+        configure((int)c, best_lay, best_blk, best_var);
+    }
+    build_graph();
+    tuned = true;
+}
+
+void Batch::apply_limits() {
+    // classes that share a kernel need its largest shared-memory size and a carve-out that keeps
+    // every class's resident blocks; kernel attributes are process-wide, so they are re-applied
+    // before each launch of the graph
+    for (int kern : {1, 2}) {
+        for (int var = 0; var < 2; ++var) {
+            std::vector<int> blocks, want;
+            std::vector<size_t> smems;
+            for (const Class& k : classes) {
+                if ((k.layout == MBG_LAYOUT_LANE ? 1 : 2) != kern || (int)k.variant != var) continue;
+                blocks.push_back(k.block);
+                smems.push_back(k.smem);
+                want.push_back(std::max(1, k.grid / std::max(1, sms)));
+            }
+            if (!blocks.empty())
+                ck(sim_kernel_limits(kern, var != 0, blocks.data(), smems.data(), want.data(), (int)blocks.size()),
+                   "batched kernel attributes");
+        }
+    }
+}
+
 void Batch::run(cudaStream_t stream) {
     ck(cudaSetDevice(device), "cudaSetDevice");
     cudaGetLastError();  // drop a stale non-sticky error of an earlier unrelated call
-    if (opts.autotune && !ran) autotune();
+    std::unique_lock<std::mutex> lock(kernel_attr_mutex());
+    if (opts.autotune && !tuned) autotune();
     cudaStream_t s = stream ? stream : capture_stream;
+    apply_limits();
     ck(cudaEventRecord(ev0, s), "cudaEventRecord");
     ck(cudaGraphLaunch(exec, s), "cudaGraphLaunch");
+    lock.unlock();
     ck(cudaEventRecord(ev1, s), "cudaEventRecord");
     ck(cudaStreamSynchronize(s), "batched simulation");
-    float ms = 0, kms = 0;
+    float ms = 0;
     ck(cudaEventElapsedTime(&ms, ev0, ev1), "cudaEventElapsedTime");
-    ck(cudaEventElapsedTime(&kms, evk0, evk1), "cudaEventElapsedTime");
+    double kms = 0;
+    for (Class& k : classes) {
+        ck(cudaEventElapsedTime(&k.kernel_ms, k.e0, k.e1), "cudaEventElapsedTime");
+        kms += k.kernel_ms;
+    }
     summary = mbg_run_summary{};
     uint32_t err = 0;
+    int layouts = 0;
     for (Inst& x : inst) {
+        const Class& k = classes[x.cls];
         const unsigned long long* c = reinterpret_cast<const unsigned long long*>(small_host + x.small_off);
         uint32_t flags[2];
         std::memcpy(flags, small_host + x.small_off + 8 * CNT_COUNT, 8);
@@ -288,7 +448,11 @@ void Batch::run(cudaStream_t stream) {
         r.errors = c[CNT_ERROR];
         r.device_error = flags[0];
         r.fixed_point_states = flags[1];
-        r.layout = MBG_LAYOUT_WARP;
+        r.layout = k.layout;
+        r.block_size = k.block;
+        r.grid_size = k.grid;
+        r.lane_update = k.layout == MBG_LAYOUT_LANE && !k.variant ? 1 : 0;
+        r.kernel_ms = k.kernel_ms;
         summary.trajectories += r.trajectories;
         summary.transitions += r.transitions;
         summary.steps += r.steps;
@@ -298,45 +462,16 @@ void Batch::run(cudaStream_t stream) {
         summary.errors += r.errors;
         summary.fixed_point_states += r.fixed_point_states;
         err |= flags[0];
+        layouts |= 1 << k.layout;
         x.fetched = false;
     }
     summary.device_error = err;
-    summary.layout = MBG_LAYOUT_WARP;
+    // one layout for every class, or 0 when the classes differ
+    summary.layout = (layouts & (layouts - 1)) ? 0 : __builtin_ctz((unsigned)layouts);
     summary.sim_ms = ms;
     summary.kernel_ms = kms;
     ran = true;
     if (err) throw DeviceError("device error flags 0x" + std::to_string(err));
-}
-
-void Batch::autotune() {
-    // Warps per block (= trajectories resident per block) and the shared-memory index cache,
-    // timed on the full batch; the fastest shape is kept.
-    const int blocks[3] = {64, 128, 256};
-    double best = 1e30;
-    int best_b = block;
-    bool best_c = cached_index;
-    for (int bi = 0; bi < 3; ++bi) {
-        for (int c = 0; c < 2; ++c) {
-            const bool cached = c == 1;
-            tune_ms[bi][c] = -1;
-            if ((size_t)(blocks[bi] / 32) * sim_warp_batch_slice_bytes(max_n, cached) > 100 * 1024) continue;
-            configure(blocks[bi], cached, opts.blocks_per_sm);
-            ck(cudaGraphLaunch(exec, capture_stream), "cudaGraphLaunch");
-            ck(cudaEventRecord(ev0, capture_stream), "cudaEventRecord");
-            ck(cudaGraphLaunch(exec, capture_stream), "cudaGraphLaunch");
-            ck(cudaEventRecord(ev1, capture_stream), "cudaEventRecord");
-            ck(cudaStreamSynchronize(capture_stream), "autotune run");
-            float ms = 0;
-            ck(cudaEventElapsedTime(&ms, ev0, ev1), "cudaEventElapsedTime");
-            tune_ms[bi][c] = ms;
-            if (ms < best) {
-                best = ms;
-                best_b = blocks[bi];
-                best_c = cached;
-            }
-        }
-    }
-    configure(best_b, best_c, opts.blocks_per_sm);
 }
 
 void Batch::fetch(int i) {

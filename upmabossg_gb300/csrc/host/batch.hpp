@@ -1,4 +1,5 @@
-// Batched sweeps: many independent instances in one persistent launch, captured in a CUDA graph.
+// Batched sweeps: many independent instances, grouped by model size into classes; each class is one
+// persistent launch (lane or warp layout, its own shape), and the whole batch is one CUDA graph.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -16,6 +17,7 @@ public:
     struct Inst {
         CompiledModel cm;
         uint64_t n_traj = 0, seed = 0;
+        int cls = 0;           // size class
         SimParams prm{};
         FpSlots fp{};
         size_t small_off = 0;  // offset of this instance's counters in the small block
@@ -27,26 +29,40 @@ public:
         mbg_run_summary summary{};
     };
 
+    // Instances of one size class and the launch that runs them.
+    struct Class {
+        int max_n = 0;                      // nodes of the largest member
+        std::vector<int> members;           // instance indices, ascending
+        uint64_t traj = 0;                  // trajectories of all members
+        size_t first = 0;                   // position of the first member in the class-ordered arrays
+        BatchDesc desc{};                   // work over all members' trajectories
+        BatchDesc pilot{};                  // a subset of every member's trajectories, for timing shapes
+        int layout = MBG_LAYOUT_LANE;       // MBG_LAYOUT_LANE or MBG_LAYOUT_WARP
+        int block = 128;
+        bool variant = false;               // lane: cooperative reader update; warp: regulator index cache
+        size_t smem = 0;
+        int grid = 0;
+        cudaEvent_t e0 = nullptr, e1 = nullptr;
+        float kernel_ms = 0.f;
+        std::vector<mbg_batch_class_timing> timings;  // every shape the autotuner timed
+    };
+
     ~Batch();
     void create(const std::vector<const CompiledModel*>& models, const std::vector<uint64_t>& n_traj,
                 const std::vector<uint64_t>& seeds, const mbg_batch_opts& o);
-    // Launch shape; rebuilds the graph.
-    void configure(int block, bool cached_index, int blocks_per_sm);
+    // Launch shape of class c (no graph rebuild).
+    void configure(int c, int layout, int block, bool variant);
     void autotune();
     void run(cudaStream_t stream);
     void fetch(int i);
 
     std::vector<Inst> inst;
+    std::vector<Class> classes;
     mbg_batch_opts opts{};
-    int device = 0, sms = 0, block = 256, grid = 0, max_n = 0;
-    bool cached_index = true;
-    size_t smem = 0;
-    unsigned slice_bytes = 0;
+    int device = 0, sms = 0;
     uint64_t total_traj = 0;
-    BatchDesc desc{};
-    SimParams* d_params = nullptr;
-    FpSlots* d_fps = nullptr;
-    unsigned long long* d_prefix = nullptr;
+    SimParams* d_params = nullptr;  // class order
+    FpSlots* d_fps = nullptr;       // class order
     void* result_arena = nullptr;
     size_t result_bytes = 0;
     void* rep_arena = nullptr;
@@ -57,14 +73,20 @@ public:
     cudaStream_t capture_stream = nullptr;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
-    cudaEvent_t ev0 = nullptr, ev1 = nullptr, evk0 = nullptr, evk1 = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     std::vector<void*> owned;
-    bool ran = false;
+    bool ran = false, tuned = false;
     mbg_run_summary summary{};
-    double tune_ms[3][2] = {};
 
 private:
     void build_graph();
+    void apply_limits();
+    cudaError_t launch_class(const Class& k, const BatchDesc& d, cudaStream_t s) const;
 };
+
+// Size class of a model with n nodes: c = ceil(log2(ceil(n / 32))), so class c holds models of at
+// most 32 * 2^c nodes (c = 0 .. 6), class 7 everything larger than 4096 nodes. The lane layout's
+// shared memory grows with a class's largest model, so narrow classes keep occupancy up.
+int batch_size_class(int n);
 
 }  // namespace mbg

@@ -507,11 +507,36 @@ mbg_status mbg_surrogate_gradients(mbg_surrogate* s, int32_t member, const float
     });
 }
 
-mbg_status mbg_batch_shape(const mbg_batch* b, int32_t* block_size, int32_t* cached_index, int32_t* grid) {
-    if (!b) return fail(MBG_ERR_ARG, "null batch");
-    if (block_size) *block_size = b->batch.block;
-    if (cached_index) *cached_index = b->batch.cached_index ? 1 : 0;
-    if (grid) *grid = b->batch.grid;
+mbg_status mbg_batch_class_count(const mbg_batch* b, int32_t* count) {
+    if (!b || !count) return fail(MBG_ERR_ARG, "null argument");
+    *count = (int32_t)b->batch.classes.size();
+    return MBG_OK;
+}
+
+mbg_status mbg_batch_class(const mbg_batch* b, int32_t c, mbg_batch_class_info* out) {
+    if (!b || !out) return fail(MBG_ERR_ARG, "null argument");
+    if (c < 0 || c >= (int32_t)b->batch.classes.size()) return fail(MBG_ERR_ARG, "class index out of range");
+    const mbg::Batch::Class& k = b->batch.classes[c];
+    *out = mbg_batch_class_info{};
+    out->max_nodes = k.max_n;
+    out->instances = (int32_t)k.members.size();
+    out->trajectories = k.traj;
+    out->layout = k.layout;
+    out->block_size = k.block;
+    out->variant = k.variant ? 1 : 0;
+    out->grid = k.grid;
+    out->kernel_ms = k.kernel_ms;
+    out->timings = (int32_t)k.timings.size();
+    return MBG_OK;
+}
+
+mbg_status mbg_batch_class_timings(const mbg_batch* b, int32_t c, mbg_batch_class_timing* out, int32_t cap,
+                                   int32_t* count) {
+    if (!b || !count || (cap > 0 && !out)) return fail(MBG_ERR_ARG, "null argument");
+    if (c < 0 || c >= (int32_t)b->batch.classes.size()) return fail(MBG_ERR_ARG, "class index out of range");
+    const auto& t = b->batch.classes[c].timings;
+    *count = (int32_t)t.size();
+    for (int32_t i = 0; i < cap && i < (int32_t)t.size(); ++i) out[i] = t[i];
     return MBG_OK;
 }
 

@@ -335,6 +335,11 @@ void Sim::setup_layout(int lay, int blk, bool coop) {
     grid = sms * bps;
 }
 
+std::mutex& kernel_attr_mutex() {
+    static std::mutex m;
+    return m;
+}
+
 void Sim::run(cudaStream_t stream) {
     ck(cudaSetDevice(device), "cudaSetDevice");
     cudaGetLastError();  // drop a stale non-sticky error of an earlier unrelated call
@@ -351,10 +356,17 @@ void Sim::run(cudaStream_t stream) {
         void* args[] = {(void*)&prm};
         ck(cudaLaunchKernel((const void*)thread_kernel, dim3(grid), dim3(block), args, 0, stream),
            "cudaLaunchKernel(mbg_sim_thread)");
-    } else if (layout == MBG_LAYOUT_LANE) {
-        ck(launch_sim_lane(prm, lane_coop, grid, block, smem, stream), "launch mbg_sim_lane");
     } else {
-        ck(launch_sim_warp(prm, cached_index, grid, block, smem, stream), "launch mbg_sim_warp");
+        // kernel attributes are process-wide: re-apply this handle's before its launch
+        std::lock_guard<std::mutex> lock(kernel_attr_mutex());
+        const int want = std::max(1, grid / std::max(1, sms));
+        if (layout == MBG_LAYOUT_LANE) {
+            ck(sim_kernel_limits(0, lane_coop, &block, &smem, &want, 1), "mbg_sim_lane attributes");
+            ck(launch_sim_lane(prm, lane_coop, grid, block, smem, stream), "launch mbg_sim_lane");
+        } else {
+            ck(sim_kernel_limits(3, cached_index, &block, &smem, &want, 1), "mbg_sim_warp attributes");
+            ck(launch_sim_warp(prm, cached_index, grid, block, smem, stream), "launch mbg_sim_warp");
+        }
     }
     ck(cudaEventRecord(evk1, stream), "cudaEventRecord");
     ck(launch_fp_aggregate(prm.fp_states, prm.fp_count, fp_capacity, cm.words, slot_rep, slot_cnt, n_slots,
@@ -386,6 +398,9 @@ void Sim::run(cudaStream_t stream) {
     summary.sim_ms = ms;
     summary.kernel_ms = kms;
     summary.jit_ms = jit_ms;
+    summary.block_size = block;
+    summary.grid_size = grid;
+    summary.lane_update = layout == MBG_LAYOUT_LANE && !lane_coop ? 1 : 0;
     ran = true;
     fetched = false;
     if (summary.device_error) throw DeviceError("device error flags 0x" + std::to_string(summary.device_error));
