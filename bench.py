@@ -170,17 +170,21 @@ def run_reference(args):
     bnd, cfg = net.bnd(), net.cfg()
     import upmabossg_gb300 as mbg
     model = mbg.Model.from_strings(bnd, cfg)  # host-side parse only: the fixed-point scale
-    vals = []
+    vals, ms = [], []
     last = None
     for i in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
         last = cpu_reference(net, bnd, cfg, model.info.frac_bits, args.cpu_seconds / 2)
         if i >= args.warmup:
             vals.append(last["value"])
+            ms.append((time.perf_counter() - t0) * 1e3)
     value = statistics.mean(vals)
     line = {"impl": "reference", "metric": "transitions/s", "value": value, "unit": "transitions/s",
-            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": None,
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": statistics.mean(ms),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
-            "data": "synthetic", "config": {"workload": WORKLOADS[args.workload]},
+            "data": "synthetic",
+            "config": {"workload": WORKLOADS[args.workload], "trajectories_per_gpu": args.n_traj or net.sample_count,
+                       "step": "a bounded sample of the workload's trajectories per step (see cpu_baseline.sample)"},
             "cpu_baseline": dict(last, value=value),
             "e2e": {"value": value, "unit": "transitions/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)

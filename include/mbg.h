@@ -229,6 +229,10 @@ typedef struct mbg_surrogate mbg_surrogate;
 
 mbg_status mbg_surrogate_create(int32_t in_dim, int32_t hidden, int32_t hidden_layers, int32_t out_dim,
                                 int32_t ensemble, uint64_t seed, int32_t device, mbg_surrogate** out);
+/* Forward products (training and prediction) on the tcgen05 tensor cores (1, default: 128x128 tiles,
+ * FP32 accumulator in tensor memory) or on the mma.sync kernel (0); both compute the same BF16
+ * products with FP32 accumulation (summation order differs). */
+mbg_status mbg_surrogate_set_tensor_path(mbg_surrogate* s, int32_t tcgen05);
 void mbg_surrogate_destroy(mbg_surrogate* s);
 /* Trains every member for `epochs` passes over (x: n x in_dim, y: n x out_dim distributions) with
  * Adam; *last_loss gets the mean cross-entropy of the last epoch. */

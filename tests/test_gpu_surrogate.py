@@ -35,6 +35,25 @@ def test_forward_matches_reference():
     assert np.all(spread == 0.0)  # one member: no spread
 
 
+@pytest.mark.parametrize("dims,rows", [((32, 512, 512, 512, 256), 300), ((24, 136, 136, 100), 129)])
+def test_tcgen05_forward_matches_mma_sync(dims, rows):
+    """The tcgen05 GEMM (TMEM accumulator) and the mma.sync GEMM compute the same BF16 products with
+    FP32 accumulation; only the summation order differs. Odd sizes exercise the partial tiles (rows
+    and columns outside M and N, K not a multiple of the 16-wide MMA step)."""
+    rng = np.random.default_rng(3)
+    s = mbg.Surrogate(dims[0], dims[-1], hidden=dims[1], hidden_layers=len(dims) - 2, ensemble=1, seed=9)
+    p = mlp.init_params(list(dims), rng)
+    s.set_params(0, p)
+    x = rng.uniform(-1, 1, size=(rows, dims[0])).astype(np.float32)
+    s.set_tensor_path(True)
+    a, _ = s.predict(x)
+    s.set_tensor_path(False)
+    b, _ = s.predict(x)
+    assert np.abs(a - b).max() < 1e-4
+    z, _ = mlp.forward(p, list(dims), x)
+    assert np.abs(a - mlp.softmax(z)).max() < 2e-3
+
+
 def test_gradients_match_reference():
     rng = np.random.default_rng(1)
     s = make()

@@ -34,6 +34,7 @@ EXPORTS = (
     "mbg_batch_fixed_points", "mbg_batch_class_count", "mbg_batch_class", "mbg_batch_class_timings",
     "mbg_surrogate_create", "mbg_surrogate_destroy", "mbg_surrogate_train", "mbg_surrogate_predict",
     "mbg_surrogate_param_count", "mbg_surrogate_get_params", "mbg_surrogate_set_params", "mbg_surrogate_gradients",
+    "mbg_surrogate_set_tensor_path",
 )
 
 
@@ -153,6 +154,7 @@ def lib():
             "mbg_surrogate_get_params": (ctypes.c_int, [vp, i32, dp]),
             "mbg_surrogate_set_params": (ctypes.c_int, [vp, i32, dp]),
             "mbg_surrogate_gradients": (ctypes.c_int, [vp, i32, dp, dp, i32, ctypes.POINTER(ctypes.c_float), dp]),
+            "mbg_surrogate_set_tensor_path": (ctypes.c_int, [vp, i32]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -428,13 +430,19 @@ class Batch:
 class Surrogate:
     """Ensemble of BF16 MLPs screening sweep points (mbg_surrogate_*)."""
 
-    def __init__(self, in_dim, out_dim, hidden=512, hidden_layers=3, ensemble=4, seed=0, device=0):
+    def __init__(self, in_dim, out_dim, hidden=512, hidden_layers=3, ensemble=4, seed=0, device=0, tcgen05=True):
         h = ctypes.c_void_p()
         _check(lib().mbg_surrogate_create(in_dim, hidden, hidden_layers, out_dim, ensemble, seed, device,
                                           ctypes.byref(h)))
         self._h = h
+        self.set_tensor_path(tcgen05)
         self.in_dim, self.out_dim, self.hidden, self.hidden_layers = in_dim, out_dim, hidden, hidden_layers
         self.ensemble = ensemble
+
+    def set_tensor_path(self, tcgen05: bool):
+        """Forward products on the tcgen05 tensor cores (True) or on the mma.sync kernel (False)."""
+        _check(lib().mbg_surrogate_set_tensor_path(self._h, 1 if tcgen05 else 0))
+        self.tcgen05 = bool(tcgen05)
 
     def param_count(self):
         return int(lib().mbg_surrogate_param_count(self._h))

@@ -27,6 +27,13 @@ struct GemmArgs {
 };
 
 cudaError_t mlp_gemm(const GemmArgs& g, cudaStream_t s);
+// The same product on the tcgen05 tensor cores (mlp_tc.cu): requires a_k == 1 and b_k == 1 (B
+// given transposed, K-contiguous), K, a_m and b_n multiples of 8 and 16-byte aligned A and B
+// (mlp_gemm_tc_supported); sets *error_flag if a completion wait gave up.
+bool mlp_gemm_tc_supported(const GemmArgs& g);
+cudaError_t mlp_gemm_tc(const GemmArgs& g, unsigned* error_flag, cudaStream_t s);
+// y = x^T for a rows x cols BF16 matrix.
+cudaError_t mlp_transpose_bf16(const __nv_bfloat16* x, int rows, int cols, __nv_bfloat16* y, cudaStream_t s);
 
 // Softmax of logits [rows x cols] (cols <= 1024) into probs (FP32); with a target distribution:
 // dlogits = (softmax - target) * scale as BF16 and the summed cross-entropy added to *loss.

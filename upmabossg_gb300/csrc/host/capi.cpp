@@ -467,6 +467,12 @@ mbg_status mbg_surrogate_create(int32_t in_dim, int32_t hidden, int32_t hidden_l
     return MBG_OK;
 }
 
+mbg_status mbg_surrogate_set_tensor_path(mbg_surrogate* s, int32_t tcgen05) {
+    if (!s) return fail(MBG_ERR_ARG, "null surrogate");
+    s->s.tensor_tc = tcgen05 != 0;
+    return MBG_OK;
+}
+
 void mbg_surrogate_destroy(mbg_surrogate* s) { delete s; }
 
 mbg_status mbg_surrogate_train(mbg_surrogate* s, const float* x, const float* y, int64_t n, int32_t epochs,

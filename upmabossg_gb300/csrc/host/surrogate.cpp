@@ -48,8 +48,11 @@ void Surrogate::create(int in, int hid, int n_hidden, int out, int ens, uint64_t
     device = dev;
     ck(cudaSetDevice(device), "cudaSetDevice");
     ck(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "cudaStreamCreate");
+    tc_error = alloc<unsigned>(1);
+    ck(cudaMemset(tc_error, 0, 4), "cudaMemset");
     std::mt19937_64 rng(seed);
     members.resize(ens);
+    wt_stale.assign(ens, true);
     for (int e = 0; e < ens; ++e) {
         Member& mb = members[e];
         for (int l = 0; l <= n_hidden; ++l) {
@@ -60,6 +63,7 @@ void Surrogate::create(int in, int hid, int n_hidden, int out, int ens, uint64_t
             L.w = alloc<float>(nw);
             L.b = alloc<float>(L.out);
             L.wb = alloc<__nv_bfloat16>(nw);
+            L.wtb = alloc<__nv_bfloat16>(nw);
             L.gw = alloc<float>(nw);
             L.gb = alloc<float>(L.out);
             L.mw = alloc<float>(nw);
@@ -103,9 +107,23 @@ void Surrogate::ensure_batch(int rows) {
     loss = alloc<float>(1);
 }
 
+void Surrogate::refresh_transposed(int e) {
+    if (!wt_stale[e]) return;
+    for (const Layer& L : members[e].layers)
+        ck(mlp_transpose_bf16(L.wb, L.in, L.out, L.wtb, stream), "mlp_transpose_bf16");
+    wt_stale[e] = false;
+}
+
+void Surrogate::check_tc_error() {
+    unsigned flag = 0;
+    ck(cudaMemcpy(&flag, tc_error, 4, cudaMemcpyDeviceToHost), "cudaMemcpy D2H");
+    if (flag) throw DeviceError("tcgen05 GEMM: a tensor-core completion wait gave up");
+}
+
 // logits = MLP(xb) for `rows` rows of member e; hidden activations kept for the backward pass.
 void Surrogate::forward(int e, int rows) {
     Member& mb = members[e];
+    if (tensor_tc) refresh_transposed(e);
     const __nv_bfloat16* a = xb;
     int a_cols = in_dim;
     for (int l = 0; l <= hidden_layers; ++l) {
@@ -121,6 +139,10 @@ void Surrogate::forward(int e, int rows) {
         g.b_k = L.out;
         g.b_n = 1;
         g.bias = L.b;
+        GemmArgs gt = g;  // the tcgen05 form reads W^T
+        gt.B = L.wtb;
+        gt.b_k = 1;
+        gt.b_n = L.in;
         if (l < hidden_layers) {
             g.relu = 1;
             g.Cb = acts[l];
@@ -129,7 +151,13 @@ void Surrogate::forward(int e, int rows) {
             g.C = logits;
             g.ldc = L.out;
         }
-        ck(mlp_gemm(g, stream), "mlp_gemm forward");
+        gt.relu = g.relu;
+        gt.Cb = g.Cb;
+        gt.ldcb = g.ldcb;
+        gt.C = g.C;
+        gt.ldc = g.ldc;
+        if (tensor_tc && mlp_gemm_tc_supported(gt)) ck(mlp_gemm_tc(gt, tc_error, stream), "mlp_gemm_tc forward");
+        else ck(mlp_gemm(g, stream), "mlp_gemm forward");
         if (l < hidden_layers) {
             a = acts[l];
             a_cols = L.out;
@@ -190,6 +218,7 @@ void Surrogate::backward(int e, int rows) {
 void Surrogate::adam_step(int e, float lr) {
     Member& mb = members[e];
     ++mb.step;
+    wt_stale[e] = true;
     for (Layer& L : mb.layers) {
         ck(mlp_adam(L.w, L.gw, L.mw, L.vw, L.wb, (long long)L.in * L.out, lr, 0.9f, 0.999f, 1e-8f, mb.step, stream),
            "mlp_adam");
@@ -233,6 +262,7 @@ float Surrogate::train(const float* x, const float* y, int64_t n, int epochs, in
         }
     }
     ck(cudaStreamSynchronize(stream), "training");
+    check_tc_error();
     // the training set buffers are only needed during this call
     for (void* p : {(void*)dx, (void*)dy, (void*)didx}) {
         cudaFree(p);
@@ -266,6 +296,7 @@ void Surrogate::predict(const float* x, int64_t n, float* out_probs, float* out_
                "cudaMemcpyAsync");
         ck(cudaStreamSynchronize(stream), "prediction");
     }
+    check_tc_error();
 }
 
 int64_t Surrogate::param_count() const {
@@ -296,6 +327,7 @@ void Surrogate::set_params(int e, const float* src) {
         src += L.out;
         ck(mlp_to_bf16(L.w, L.wb, (long long)nw, stream), "mlp_to_bf16");
     }
+    wt_stale[e] = true;
     ck(cudaStreamSynchronize(stream), "surrogate");
 }
 

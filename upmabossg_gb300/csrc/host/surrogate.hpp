@@ -19,6 +19,7 @@ public:
         int in = 0, out = 0;
         float *w = nullptr, *b = nullptr;  // FP32 master weights, W row-major [in][out]
         __nv_bfloat16* wb = nullptr;       // BF16 copy used by the GEMMs
+        __nv_bfloat16* wtb = nullptr;      // BF16 W^T [out][in]: the K-major operand of the tcgen05 GEMM
         float *gw = nullptr, *gb = nullptr;
         float *mw = nullptr, *vw = nullptr, *mb = nullptr, *vb = nullptr;  // Adam moments
     };
@@ -37,6 +38,8 @@ public:
     void set_params(int member, const float* src);
 
     int in_dim = 0, hidden = 0, hidden_layers = 0, out_dim = 0, ensemble = 0, device = 0;
+    // forward products on the tcgen05 tensor cores (true) or on the mma.sync kernel
+    bool tensor_tc = true;
     std::vector<Member> members;
 
 private:
@@ -46,6 +49,8 @@ private:
     void forward(int member, int rows);
     void backward(int member, int rows);
     void adam_step(int member, float lr);
+    void refresh_transposed(int member);
+    void check_tc_error();
 
     cudaStream_t stream = nullptr;
     int cap_rows = 0;
@@ -61,6 +66,8 @@ private:
     float* mean = nullptr;
     float* spread = nullptr;
     float* loss = nullptr;
+    unsigned* tc_error = nullptr;   // set by a tcgen05 GEMM whose mbarrier wait gave up
+    std::vector<bool> wt_stale;     // per member: wtb behind wb
     std::vector<void*> owned;
 };
 
