@@ -256,6 +256,7 @@ def measure_surrogate(n_train=20000, n_traj=10000, n_cand=1_000_000, epochs=60, 
     cands = space.sample(rng, n_cand)
     rep = screen.screen(s, sim, cands, target, threshold=0.9, spread_cut=0.1, plain_points_per_s=plain,
                         max_report=1000)
+    gemm = measure_surrogate_gemm()
     return {
         "metric": "sweep points/s, surrogate-screened vs plain batched simulation", "value": rep.screened_points_per_s,
         "unit": "points/s", "plain_points_per_s": plain, "speedup": rep.speedup,
@@ -265,7 +266,27 @@ def measure_surrogate(n_train=20000, n_traj=10000, n_cand=1_000_000, epochs=60, 
                         "share_le_0.01": float((tv_held <= 0.01).mean()), "n": len(held)},
         "resimulated": rep.resimulated, "uncertain": rep.uncertain, "candidates": rep.candidates,
         "predict_s": rep.predict_s, "resim_s": rep.resim_s, "train_s": train_s, "train_loss": loss,
-        "training_data_s": data_s, "workload": SURROGATE_DESC}
+        "training_data_s": data_s, "gemm": gemm, "workload": SURROGATE_DESC}
+
+
+def measure_surrogate_gemm(rows=131072, reps=10):
+    """Tensor-core throughput of the surrogate's forward products (4 members of 32-512-512-512-256,
+    BF16 in, FP32 accumulate, bias/ReLU epilogues) on the tcgen05 kernel and on the mma.sync kernel,
+    against the measured cuBLAS BF16 peak."""
+    import upmabossg_gb300 as mbg
+    peaks, kind = load_peaks()
+    dims = [32, 512, 512, 512, 256]
+    flop = 2.0 * rows * 4 * sum(a * b for a, b in zip(dims[:-1], dims[1:]))
+    out = {"rows": rows, "members": 4, "flop_per_pass": flop}
+    for name, tc in (("tcgen05", True), ("mma_sync", False)):
+        s = mbg.Surrogate(32, 256, hidden=512, hidden_layers=3, ensemble=4, seed=11, tcgen05=tc)
+        ms = s.time_forward(rows, reps)
+        s.close()
+        tf = flop / (ms * 1e-3) / 1e12
+        out[name] = {"ms_per_pass": ms, "tflops": tf, "frac_of_bf16_peak": tf / peaks["bf16_tflops"]}
+    out["peak_tflops"] = peaks["bf16_tflops"]
+    out["peak_source"] = f"{kind} cuBLAS bf16 burst (MEASURED_PEAKS.json)" if kind == "measured" else kind
+    return out
 
 
 def run_ours(args):

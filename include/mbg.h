@@ -233,6 +233,10 @@ mbg_status mbg_surrogate_create(int32_t in_dim, int32_t hidden, int32_t hidden_l
  * FP32 accumulator in tensor memory) or on the mma.sync kernel (0); both compute the same BF16
  * products with FP32 accumulation (summation order differs). */
 mbg_status mbg_surrogate_set_tensor_path(mbg_surrogate* s, int32_t tcgen05);
+/* Device time of one forward pass of every ensemble member over `rows` rows (the GEMMs with their
+ * bias/ReLU epilogues), the mean over `reps` passes timed with CUDA events: the tensor-core
+ * throughput figure (2 * rows * members * sum of layer in x out FLOP per pass). */
+mbg_status mbg_surrogate_time_forward(mbg_surrogate* s, int32_t rows, int32_t reps, double* ms_per_pass);
 void mbg_surrogate_destroy(mbg_surrogate* s);
 /* Trains every member for `epochs` passes over (x: n x in_dim, y: n x out_dim distributions) with
  * Adam; *last_loss gets the mean cross-entropy of the last epoch. */

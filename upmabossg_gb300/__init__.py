@@ -34,7 +34,7 @@ EXPORTS = (
     "mbg_batch_fixed_points", "mbg_batch_class_count", "mbg_batch_class", "mbg_batch_class_timings",
     "mbg_surrogate_create", "mbg_surrogate_destroy", "mbg_surrogate_train", "mbg_surrogate_predict",
     "mbg_surrogate_param_count", "mbg_surrogate_get_params", "mbg_surrogate_set_params", "mbg_surrogate_gradients",
-    "mbg_surrogate_set_tensor_path",
+    "mbg_surrogate_set_tensor_path", "mbg_surrogate_time_forward",
 )
 
 
@@ -155,6 +155,7 @@ def lib():
             "mbg_surrogate_set_params": (ctypes.c_int, [vp, i32, dp]),
             "mbg_surrogate_gradients": (ctypes.c_int, [vp, i32, dp, dp, i32, ctypes.POINTER(ctypes.c_float), dp]),
             "mbg_surrogate_set_tensor_path": (ctypes.c_int, [vp, i32]),
+            "mbg_surrogate_time_forward": (ctypes.c_int, [vp, i32, i32, ctypes.POINTER(ctypes.c_double)]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -443,6 +444,12 @@ class Surrogate:
         """Forward products on the tcgen05 tensor cores (True) or on the mma.sync kernel (False)."""
         _check(lib().mbg_surrogate_set_tensor_path(self._h, 1 if tcgen05 else 0))
         self.tcgen05 = bool(tcgen05)
+
+    def time_forward(self, rows, reps=10):
+        """Device milliseconds of one forward pass of every member over `rows` rows."""
+        ms = ctypes.c_double()
+        _check(lib().mbg_surrogate_time_forward(self._h, int(rows), int(reps), ctypes.byref(ms)))
+        return ms.value
 
     def param_count(self):
         return int(lib().mbg_surrogate_param_count(self._h))

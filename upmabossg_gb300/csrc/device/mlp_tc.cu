@@ -1,15 +1,17 @@
 // Surrogate GEMM on the fifth-generation tensor cores (tcgen05, sm_103a):
 //   C[M x N] = alpha * A[M x K] . B[K x N] (+ bias[n]) (ReLU), A and B BF16, accumulation FP32 in
 //   tensor memory (TMEM).
-// One CTA (4 warps) computes a 128 x 128 tile. Per 64-wide K block, the 128 threads stage the A
-// and B tiles into shared memory in the canonical no-swizzle K-major layout (8 x 16-byte core
-// matrices; core matrix (row group r, k group q) at byte (r * 8 + q) * 128), two buffers deep, and
-// one thread issues four 128x128x16 tcgen05.mma instructions and a tcgen05.commit to the buffer's
-// mbarrier; the buffer is refilled once that mbarrier has flipped. The epilogue reads the 128 x 128
-// FP32 accumulator with tcgen05.ld (warp w owns TMEM lanes 32w .. 32w + 31 = tile rows) and applies
-// alpha, bias and ReLU. Requirements (checked by mlp_gemm_tc): A rows K-contiguous (a_k == 1),
-// B given transposed (element (k, n) at B[n * b_n + k], b_k == 1), K, a_m and b_n multiples of 8,
-// 16-byte aligned A and B.
+// One CTA (4 warps) computes a 128 x 128 tile. K is consumed in 64-wide blocks through a 3-stage
+// shared-memory ring: every thread copies its 16-byte chunks of the A and B tiles with cp.async
+// (zero-filled outside the matrices) into the canonical no-swizzle K-major layout (8 x 16-byte
+// core matrices; core matrix (row group r, k group q) at byte (r * 8 + q) * 128), so the copies of
+// the next two blocks are in flight while the tensor core works on the current one; one thread
+// issues four 128x128x16 tcgen05.mma instructions per block and a tcgen05.commit to the stage's
+// mbarrier, and a stage is refilled once its mbarrier has flipped. The epilogue reads the
+// accumulator with tcgen05.ld (warp w owns TMEM lanes 32w .. 32w + 31 = tile rows), applies alpha,
+// bias and ReLU and writes each thread's 32-column run with 16-byte stores. Requirements (checked
+// by mlp_gemm_tc_supported): A rows K-contiguous (a_k == 1), B given transposed (element (k, n) at
+// B[n * b_n + k], b_k == 1), K, a_m and b_n multiples of 8, 16-byte aligned A and B.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -21,10 +23,11 @@ namespace mbg {
 
 namespace {
 
-constexpr int TM = 128, TN = 128, TK = 64;
-constexpr int kTileBytes = TM * TK * 2;            // 16 KiB per operand tile
-constexpr int kSmemBytes = 4 * kTileBytes + 1024;  // A0 B0 A1 B1 + alignment slack
-constexpr unsigned kSpinLimit = 1u << 26;          // bounded mbarrier waits
+constexpr int TM = 128, TN = 128, TK = 64, kStages = 3;
+constexpr int kTileBytes = TM * TK * 2;                      // 16 KiB per operand tile
+constexpr int kStageBytes = 2 * kTileBytes;                  // A tile, then B tile
+constexpr int kSmemBytes = kStages * kStageBytes + 1024;     // + alignment slack
+constexpr unsigned kSpinLimit = 1u << 26;                    // bounded mbarrier waits
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -90,33 +93,43 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
     for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
 }
 
-// Stages rows r0 .. r0+127 (of `rows`), k0 .. k0+63 (of K) of a K-contiguous BF16 matrix (row
-// stride ld elements) into the core-matrix layout at dst: chunk c (16 bytes) of the tile is row
-// (c / 64) * 8 + c % 8, k group (c / 8) % 8, stored at byte 16 c. Out-of-range chunks are zero.
-__device__ __forceinline__ void stage_tile(unsigned char* dst, const __nv_bfloat16* src, long long ld, int r0,
-                                           int rows, int k0, int K) {
+// Starts the copies of rows r0 .. r0+127 (of `rows`), k0 .. k0+63 (of K) of a K-contiguous BF16
+// matrix (row stride ld elements) into the core-matrix layout at shared address dst: chunk c
+// (16 bytes) of the tile is row (c / 64) * 8 + c % 8, k group (c / 8) % 8, stored at byte 16 c, so
+// a warp's 32 chunks cover 8 rows x 64 contiguous bytes. Chunks outside the matrix are zero-filled.
+__device__ __forceinline__ void load_tile_async(uint32_t dst, const __nv_bfloat16* src, long long ld, int r0,
+                                                int rows, int k0, int K) {
 #pragma unroll
     for (int i = 0; i < (TM * TK / 8) / 128; ++i) {
         const int c = (int)threadIdx.x + 128 * i;
         const int r = (c >> 6) * 8 + (c & 7);
         const int kq = (c >> 3) & 7;
         const int gr = r0 + r, gk = k0 + kq * 8;
-        uint4 v = make_uint4(0u, 0u, 0u, 0u);
-        if (gr < rows && gk < K) v = __ldg(reinterpret_cast<const uint4*>(src + (long long)gr * ld + gk));
-        *reinterpret_cast<uint4*>(dst + 16 * c) = v;
+        const bool in = gr < rows && gk < K;
+        const __nv_bfloat16* p = in ? src + (long long)gr * ld + gk : src;
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst + 16u * c), "l"(p), "r"(in ? 16 : 0)
+                     : "memory");
     }
+}
+
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
 }
 
 }  // namespace
 
 __global__ void __launch_bounds__(128) mlp_gemm_tc_kernel(const GemmArgs g, unsigned* error_flag) {
     extern __shared__ unsigned char smem_raw[];
-    __shared__ __align__(8) uint64_t bar[2];
+    __shared__ __align__(8) uint64_t bar[kStages];
     __shared__ uint32_t tmem_slot;
     unsigned char* smem = reinterpret_cast<unsigned char*>(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    const uint32_t sbase = smem_u32(smem);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int m0 = blockIdx.y * TM, n0 = blockIdx.x * TN;
     const long long a_base = g.a_row_offset ? (long long)(*g.a_row_offset) * g.a_m : 0;
+    const __nv_bfloat16* A = g.A + a_base;
 
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_slot)),
@@ -125,9 +138,19 @@ __global__ void __launch_bounds__(128) mlp_gemm_tc_kernel(const GemmArgs g, unsi
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
     if (threadIdx.x == 0) {
-        mbar_init(&bar[0], 1);
-        mbar_init(&bar[1], 1);
+        for (int i = 0; i < kStages; ++i) mbar_init(&bar[i], 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    const int nk = (g.K + TK - 1) / TK;
+    // prologue: the first kStages - 1 blocks in flight (an empty group keeps the counting uniform)
+#pragma unroll
+    for (int st = 0; st < kStages - 1; ++st) {
+        if (st < nk) {
+            const uint32_t d = sbase + st * kStageBytes;
+            load_tile_async(d, A, g.a_m, m0, g.M, st * TK, g.K);
+            load_tile_async(d + kTileBytes, g.B, g.b_n, n0, g.N, st * TK, g.K);
+        }
+        cp_async_commit();
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
@@ -135,56 +158,91 @@ __global__ void __launch_bounds__(128) mlp_gemm_tc_kernel(const GemmArgs g, unsi
     const uint32_t tmem = tmem_slot;
 
     bool ok = true;
-    const int nk = (g.K + TK - 1) / TK;
     for (int kb = 0; kb < nk; ++kb) {
-        const int buf = kb & 1;
-        // the MMAs that last read this buffer (K block kb - 2) must be done before it is refilled
-        if (kb >= 2 && !mbar_wait(&bar[buf], (unsigned)(((kb - 2) >> 1) & 1))) ok = false;
-        const int k0 = kb * TK;
-        unsigned char* ta = smem + (2 * buf) * kTileBytes;  // buffer buf: A tile, then B tile
-        unsigned char* tb = ta + kTileBytes;
-        stage_tile(ta, g.A + a_base, g.a_m, m0, g.M, k0, g.K);
-        stage_tile(tb, g.B, g.b_n, n0, g.N, k0, g.K);
-        // generic-proxy stores -> visible to the tensor core's async proxy
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        const int stage = kb % kStages;
+        // this thread's copies of block kb have landed (the later kStages - 2 groups may be pending)
+        cp_async_wait<kStages - 2>();
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // -> visible to the tensor core
         __syncthreads();
         if (threadIdx.x == 0) {
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            const int steps = (min(TK, g.K - k0) + 15) / 16;
-            const uint32_t a_addr = smem_u32(ta), b_addr = smem_u32(tb);
+            const int steps = (min(TK, g.K - kb * TK) + 15) / 16;
+            const uint32_t a_addr = sbase + stage * kStageBytes, b_addr = a_addr + kTileBytes;
             for (int s = 0; s < steps; ++s) {
                 // K step s covers k groups 2s and 2s+1: 256 bytes further into each tile
                 const uint64_t ad = smem_desc(a_addr + 256u * s, 128u, 1024u);
                 const uint64_t bd = smem_desc(b_addr + 256u * s, 128u, 1024u);
                 mma_bf16_tc(tmem, ad, bd, (kb > 0 || s > 0) ? 1u : 0u);
             }
-            mma_commit(&bar[buf]);
+            mma_commit(&bar[stage]);
         }
+        // refill the stage of block kb - 1 with block kb + kStages - 1 once block kb - 1's MMAs are done
+        const int next = kb + kStages - 1;
+        if (next < nk) {
+            const int ns = next % kStages;
+            if (kb >= 1 && !mbar_wait(&bar[ns], (unsigned)(((kb - 1) / kStages) & 1))) ok = false;
+            const uint32_t d = sbase + ns * kStageBytes;
+            load_tile_async(d, A, g.a_m, m0, g.M, next * TK, g.K);
+            load_tile_async(d + kTileBytes, g.B, g.b_n, n0, g.N, next * TK, g.K);
+        }
+        cp_async_commit();
     }
     // every MMA of this thread is tracked by the last commit
-    if (nk > 0 && !mbar_wait(&bar[(nk - 1) & 1], (unsigned)(((nk - 1) >> 1) & 1))) ok = false;
+    if (nk > 0 && !mbar_wait(&bar[(nk - 1) % kStages], (unsigned)(((nk - 1) / kStages) & 1))) ok = false;
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     if (!ok && lane == 0) atomicOr(error_flag, 1u);
 
     const int row = m0 + warp * 32 + lane;
     const uint32_t lane_addr = tmem + ((uint32_t)(warp * 32) << 16);
+    // 16-byte stores need 16-byte aligned rows
+    const bool vec_b = g.Cb && (g.ldcb % 8) == 0 && ((uintptr_t)g.Cb & 15u) == 0;
+    const bool vec_f = g.C && !g.accumulate && (g.ldc % 4) == 0 && ((uintptr_t)g.C & 15u) == 0;
 #pragma unroll 1
     for (int c0 = 0; c0 < TN; c0 += 32) {
         float v[32];
+        __syncwarp();  // tcgen05.ld is warp-collective: reconverge after the previous chunk's exits
         tmem_ld32(lane_addr + (uint32_t)c0, v);
-        if (!ok || row >= g.M) continue;
+        const int col0 = n0 + c0;
+        if (!ok || row >= g.M || col0 >= g.N) continue;
 #pragma unroll
         for (int i = 0; i < 32; ++i) {
-            const int col = n0 + c0 + i;
-            if (col >= g.N) break;
             float x = g.alpha * (nk > 0 ? v[i] : 0.f);
-            if (g.bias) x += g.bias[col];
+            if (g.bias && col0 + i < g.N) x += __ldg(g.bias + col0 + i);
             if (g.relu) x = x > 0.f ? x : 0.f;
-            if (g.C) {
-                float* dst = g.C + (long long)row * g.ldc + col;
-                *dst = g.accumulate ? *dst + x : x;
+            v[i] = x;
+        }
+        const bool full = col0 + 32 <= g.N;
+        if (g.Cb) {
+            __nv_bfloat16* dst = g.Cb + (long long)row * g.ldcb + col0;
+            if (full && vec_b) {
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    uint4 w;
+                    unsigned* wp = reinterpret_cast<unsigned*>(&w);
+#pragma unroll
+                    for (int h = 0; h < 4; ++h) {
+                        const __nv_bfloat162 b2 = __floats2bfloat162_rn(v[8 * q + 2 * h], v[8 * q + 2 * h + 1]);
+                        wp[h] = *reinterpret_cast<const unsigned*>(&b2);
+                    }
+                    reinterpret_cast<uint4*>(dst)[q] = w;
+                }
+            } else {
+#pragma unroll
+                for (int i = 0; i < 32; ++i)
+                    if (col0 + i < g.N) dst[i] = __float2bfloat16(v[i]);
             }
-            if (g.Cb) g.Cb[(long long)row * g.ldcb + col] = __float2bfloat16(x);
+        }
+        if (g.C) {
+            float* dst = g.C + (long long)row * g.ldc + col0;
+            if (full && vec_f) {
+#pragma unroll
+                for (int q = 0; q < 8; ++q)
+                    reinterpret_cast<float4*>(dst)[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+            } else {
+#pragma unroll
+                for (int i = 0; i < 32; ++i)
+                    if (col0 + i < g.N) dst[i] = g.accumulate ? dst[i] + v[i] : v[i];
+            }
         }
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");

@@ -473,6 +473,11 @@ mbg_status mbg_surrogate_set_tensor_path(mbg_surrogate* s, int32_t tcgen05) {
     return MBG_OK;
 }
 
+mbg_status mbg_surrogate_time_forward(mbg_surrogate* s, int32_t rows, int32_t reps, double* ms_per_pass) {
+    if (!s || !ms_per_pass) return fail(MBG_ERR_ARG, "null argument");
+    return guard([&] { *ms_per_pass = s->s.time_forward(rows, reps); });
+}
+
 void mbg_surrogate_destroy(mbg_surrogate* s) { delete s; }
 
 mbg_status mbg_surrogate_train(mbg_surrogate* s, const float* x, const float* y, int64_t n, int32_t epochs,

@@ -299,6 +299,29 @@ void Surrogate::predict(const float* x, int64_t n, float* out_probs, float* out_
     check_tc_error();
 }
 
+double Surrogate::time_forward(int rows, int reps) {
+    ck(cudaSetDevice(device), "cudaSetDevice");
+    if (rows < 1 || reps < 1) throw ArgError("rows and reps must be positive");
+    ensure_batch(rows);
+    // inputs: whatever the last batch left (the products' cost does not depend on the values)
+    ck(cudaMemsetAsync(xb, 0, (size_t)rows * in_dim * sizeof(__nv_bfloat16), stream), "cudaMemsetAsync");
+    cudaEvent_t e0, e1;
+    ck(cudaEventCreate(&e0), "cudaEventCreate");
+    ck(cudaEventCreate(&e1), "cudaEventCreate");
+    for (int e = 0; e < ensemble; ++e) forward(e, rows);  // warm-up (and W^T refresh)
+    ck(cudaEventRecord(e0, stream), "cudaEventRecord");
+    for (int r = 0; r < reps; ++r)
+        for (int e = 0; e < ensemble; ++e) forward(e, rows);
+    ck(cudaEventRecord(e1, stream), "cudaEventRecord");
+    ck(cudaEventSynchronize(e1), "forward timing");
+    float ms = 0.f;
+    ck(cudaEventElapsedTime(&ms, e0, e1), "cudaEventElapsedTime");
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    check_tc_error();
+    return (double)ms / reps;
+}
+
 int64_t Surrogate::param_count() const {
     int64_t c = 0;
     for (const Layer& L : members[0].layers) c += (int64_t)L.in * L.out + L.out;

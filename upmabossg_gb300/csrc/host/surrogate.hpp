@@ -34,6 +34,8 @@ public:
     void predict(const float* x, int64_t n, float* probs, float* spread, int chunk = 8192);
     float gradients(int member, const float* x, const float* y, int rows);
     int64_t param_count() const;
+    // Device time (ms) of one forward pass of every member over `rows` rows, mean of `reps`.
+    double time_forward(int rows, int reps);
     void get_params(int member, float* dst, bool grads);
     void set_params(int member, const float* src);
 
