@@ -239,7 +239,8 @@ mbg_status mbg_surrogate_set_tensor_path(mbg_surrogate* s, int32_t tcgen05);
 mbg_status mbg_surrogate_time_forward(mbg_surrogate* s, int32_t rows, int32_t reps, double* ms_per_pass);
 void mbg_surrogate_destroy(mbg_surrogate* s);
 /* Trains every member for `epochs` passes over (x: n x in_dim, y: n x out_dim distributions) with
- * Adam; *last_loss gets the mean cross-entropy of the last epoch. */
+ * Adam, the learning rate decaying from lr along a half cosine (floored at lr / 100) over the call;
+ * *last_loss gets the mean cross-entropy of the last epoch. */
 mbg_status mbg_surrogate_train(mbg_surrogate* s, const float* x, const float* y, int64_t n, int32_t epochs,
                                int32_t batch, float lr, uint64_t seed, float* last_loss);
 /* probs: n x out_dim ensemble-mean distributions; spread: n values (either may be NULL). */

@@ -87,3 +87,54 @@ def compare_histograms(model, sim, orc, n_traj):
         orc_map = {tuple(s): int(c) for s, c in zip(uo, co)}
         assert dev_map == orc_map, "fixed points differ"
     return err
+
+
+def mixed_network(n=48, seed=3, outputs=6, max_time=20.0, tick=0.5, discrete=False):
+    """A random network exercising every rate form of the grammar: two-valued `@logic` rates,
+    multi-valued (palette) rates that read other nodes (arithmetic on node values, nested ternaries,
+    comparisons), XOR and NOT in the logic, constant nodes, and nodes with more than 12 regulators
+    (stored outside the inline records). Returns (bnd, cfg)."""
+    rng = np.random.default_rng(seed)
+    names = [f"M{i}" for i in range(n)]
+    lines = []
+    for i, nm in enumerate(names):
+        others = [x for x in names if x != nm]
+        kind = i % 6
+        if i == n - 1:  # a wide two-valued node: 14 regulators, beyond the 12 inline ones
+            kind = 0
+            regs = list(rng.choice(others, size=14, replace=False))
+            logic = " | ".join(f"({a} & !{b})" for a, b in zip(regs[0::2], regs[1::2]))
+        else:
+            k = int(rng.integers(1, 4))
+            regs = list(rng.choice(others, size=k, replace=False))
+            ops = [" & ", " | ", " ^ "]
+            logic = regs[0] if rng.random() < 0.5 else f"!{regs[0]}"
+            for r in regs[1:]:
+                logic = f"({logic}{ops[int(rng.integers(0, 3))]}{r})"
+        u = float(np.round(rng.lognormal(0.0, 0.5), 4))
+        d = float(np.round(rng.lognormal(0.0, 0.5), 4))
+        a, b, c = rng.choice(others, size=3, replace=False)
+        if kind == 0:
+            up, down = f"@logic ? {u} : 0", f"@logic ? 0 : {d}"
+        elif kind == 1:  # palette: the up rate scales with two other nodes
+            up, down = f"@logic ? {u} * (1 + {a} + 2 * {b}) : 0", f"@logic ? 0 : {d}"
+        elif kind == 2:  # palette: nested ternary on other nodes in the down rate
+            up, down = f"@logic ? {u} : 0", f"@logic ? 0 : ({a} ? {d} : ({b} ? {2 * d} : {0.5 * d}))"
+        elif kind == 3:  # palette: a comparison
+            up, down = f"@logic ? ({a} + {b} + {c} >= 2 ? {2 * u} : {u}) : 0", f"@logic ? 0 : {d}"
+        elif kind == 4 and i % 12 == 4:  # constant node (fixed points become common)
+            logic = "1" if rng.random() < 0.5 else "0"
+            up, down = f"@logic ? {u} : 0", f"@logic ? 0 : {d}"
+        elif kind == 4:
+            up, down = f"@logic ? {u} : 0", f"@logic ? 0 : {d}"
+        else:
+            up, down = f"@logic ? {u} : 0", f"@logic ? 0 : {d} * (2 - {a})"
+        lines.append(f"Node {nm} {{\n  logic = {logic};\n  rate_up = {up};\n  rate_down = {down};\n}}\n")
+    bnd = "".join(lines)
+    out = set(rng.choice(names, size=outputs, replace=False))
+    cfg = "".join(f"{nm}.is_internal = {0 if nm in out else 1};\n" for nm in names)
+    cfg += "".join(f"{nm}.istate = 0.5;\n" for nm in names)
+    cfg += f"max_time = {max_time};\ntime_tick = {tick};\nsample_count = 2000;\nseed_pseudorandom = 11;\n"
+    if discrete:
+        cfg += "discrete_time = 1;\n"
+    return bnd, cfg

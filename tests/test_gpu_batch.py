@@ -7,7 +7,7 @@ import pytest
 import upmabossg_gb300 as mbg
 from upmabossg_gb300 import synth
 
-from helpers import golden_model
+from helpers import golden_model, mixed_network
 
 pytestmark = pytest.mark.gpu
 
@@ -19,6 +19,7 @@ def instances():
         texts.append((net.bnd(), net.cfg(sample_count=min(net.sample_count, 3000))))
     texts.append(golden_model("montagud"))
     texts.append(golden_model("cellcycle"))
+    texts.append(mixed_network(seed=3))  # multi-valued rates and a 14-regulator node
     return texts
 
 

@@ -12,7 +12,7 @@ import pytest
 import upmabossg_gb300 as mbg
 from upmabossg_gb300 import synth
 
-from helpers import compare_histograms, compare_trajectories, golden_model, run_device, run_oracle
+from helpers import compare_histograms, compare_trajectories, golden_model, mixed_network, run_device, run_oracle
 
 pytestmark = pytest.mark.gpu
 
@@ -40,6 +40,19 @@ def test_small_network_parity(layout):
     assert s["transitions"] == orc.counters["transitions"] or orc.counters["time_ties"] > 0
     compare_trajectories(sim, orc)
     compare_histograms(model, sim, orc, n)
+
+
+@pytest.mark.parametrize("layout", ALL_LAYOUTS)
+@pytest.mark.parametrize("seed,discrete", [(3, False), (4, False), (3, True)])
+def test_mixed_rate_forms_parity(seed, discrete, layout):
+    """Multi-valued (palette) rates reading other nodes, XOR, nested ternaries, comparisons,
+    constant nodes and a 14-regulator node, in continuous and discrete time."""
+    bnd, cfg = mixed_network(seed=seed, discrete=discrete)
+    model, sim = run_device(bnd, cfg, 2000, **layout_kw(layout))
+    assert model.info.palette_nodes > 0 and model.info.max_regulators > 12
+    orc = run_oracle(bnd, cfg, model, 2000)
+    compare_trajectories(sim, orc)
+    compare_histograms(model, sim, orc, 2000)
 
 
 @pytest.mark.parametrize("layout", [mbg.LAYOUT_WARP, mbg.LAYOUT_LANE, "lane-serial"])

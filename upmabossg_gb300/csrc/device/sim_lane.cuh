@@ -231,16 +231,14 @@ __device__ __forceinline__ int lane_pick(const SimParams& p, const unsigned* st,
 // patch the same trajectory), returns the rate change and sets `out` when dn is an output node
 // whose rate changed.
 template <bool ATOMIC>
-__device__ __forceinline__ unsigned long long lane_reader(const SimParams& p, unsigned e, const LaneSmem& m, int T,
-                                                          int col, bool& out) {
+__device__ __forceinline__ unsigned long long lane_reader_rec(const SimParams& p, unsigned e, uint4 ra, uint4 rb,
+                                                              const LaneSmem& m, int T, int col, bool& out) {
     const int dn = (int)(e >> 16);
     const int kd = (int)((e >> 8) & 0xffu);
     const unsigned pos = e & 0xffu;
     const unsigned* st = m.st + col;
     const unsigned self = col_bit(st, T, dn);
     const unsigned self_old = pos == 0xffu ? self ^ 1u : self;
-    const uint4* rec = reinterpret_cast<const uint4*>(p.lnodes + dn);
-    const uint4 ra = __ldg(rec), rb = __ldg(rec + 1);
     const unsigned flags = rb.w >> 16;
     unsigned long long r_new, r_old;
     unsigned a_new, a_old;
@@ -282,13 +280,36 @@ __device__ __forceinline__ unsigned long long lane_reader(const SimParams& p, un
     return delta;
 }
 
+template <bool ATOMIC>
+__device__ __forceinline__ unsigned long long lane_reader(const SimParams& p, unsigned e, const LaneSmem& m, int T,
+                                                          int col, bool& out) {
+    const uint4* rec = reinterpret_cast<const uint4*>(p.lnodes + (e >> 16));
+    return lane_reader_rec<ATOMIC>(p, e, __ldg(rec), __ldg(rec + 1), m, T, col, out);
+}
+
 // After node k flipped in this lane's trajectory: re-evaluates every node whose rate reads k (and
 // k itself) in turn. Returns whether an output node's rate changed.
 __device__ __forceinline__ bool lane_update(const SimParams& p, int k, const LaneSmem& m, int T, int col,
                                             unsigned long long& total) {
     const int d0 = (int)__ldg(p.dep_off + k), d1 = (int)__ldg(p.dep_off + k + 1);
     bool out = false;
-    for (int q = d0; q < d1; ++q) total += lane_reader<false>(p, __ldg(p.deps + q), m, T, col, out);
+    // the next reader's dependency entry and record are fetched while this one is applied
+    unsigned e = __ldg(p.deps + d0);
+    uint4 ra = __ldg(reinterpret_cast<const uint4*>(p.lnodes + (e >> 16)));
+    uint4 rb = __ldg(reinterpret_cast<const uint4*>(p.lnodes + (e >> 16)) + 1);
+    for (int q = d0; q < d1; ++q) {
+        unsigned e2 = 0u;
+        uint4 ra2 = ra, rb2 = rb;
+        if (q + 1 < d1) {
+            e2 = __ldg(p.deps + q + 1);
+            ra2 = __ldg(reinterpret_cast<const uint4*>(p.lnodes + (e2 >> 16)));
+            rb2 = __ldg(reinterpret_cast<const uint4*>(p.lnodes + (e2 >> 16)) + 1);
+        }
+        total += lane_reader_rec<false>(p, e, ra, rb, m, T, col, out);
+        e = e2;
+        ra = ra2;
+        rb = rb2;
+    }
     return out;
 }
 

@@ -251,7 +251,10 @@ float Surrogate::train(const float* x, const float* y, int64_t n, int epochs, in
                 ck(mlp_gather_rows(dy, didx + (size_t)s * batch, batch, out_dim, yt, nullptr, stream), "gather y");
                 forward(e, batch);
                 backward(e, batch);
-                adam_step(e, lr);
+                // half-cosine decay of the learning rate over the call, floored at lr / 100
+                const double frac = (double)(ep * steps + s) / (double)((int64_t)epochs * steps);
+                const double f = std::max(0.01, 0.5 * (1.0 + std::cos(3.141592653589793 * frac)));
+                adam_step(e, (float)(lr * f));
             }
             if (ep == epochs - 1) {
                 float h = 0.f;

@@ -90,6 +90,9 @@ class ScreenReport:
     plain_points_per_s: float
     screened_points_per_s: float
     speedup: float
+    hits: np.ndarray = None          # indices of the reported candidates
+    hit_probs: np.ndarray = None     # their predicted distributions
+    hit_truth: np.ndarray = None     # their re-simulated distributions
 
 
 def screen(surrogate: mbg.Surrogate, sim: PointSimulator, candidates: np.ndarray, target_state: int,
@@ -117,4 +120,6 @@ def screen(surrogate: mbg.Surrogate, sim: PointSimulator, candidates: np.ndarray
         predict_s=predict_s, resim_s=resim_s, tv_mean=float(tv.mean()) if len(tv) else 0.0,
         tv_max=float(tv.max()) if len(tv) else 0.0, tv_frac_ok=float((tv <= 0.01).mean()) if len(tv) else 1.0,
         plain_points_per_s=plain_points_per_s, screened_points_per_s=screened,
-        speedup=screened / plain_points_per_s if plain_points_per_s > 0 else math.inf)
+        speedup=screened / plain_points_per_s if plain_points_per_s > 0 else math.inf,
+        hits=hits, hit_probs=probs[hits],
+        hit_truth=np.array([truth[pos[int(i)]] for i in hits]) if len(hits) else np.zeros((0, probs.shape[1])))
