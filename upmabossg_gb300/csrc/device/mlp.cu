@@ -177,9 +177,14 @@ cudaError_t mlp_bias_grad(const __nv_bfloat16* d, int rows, int cols, float* db,
     return cudaGetLastError();
 }
 
-__global__ void mlp_adam_kernel(float* __restrict__ w, const float* __restrict__ g, float* __restrict__ m,
-                                float* __restrict__ v, __nv_bfloat16* __restrict__ wb, long long n, float lr,
-                                float beta1, float beta2, float eps, float c1, float c2) {
+// Adam with the step's learning rate and bias corrections read from per-step tables at the step
+// counter *t (for replayed training graphs).
+__global__ void mlp_adam_sched_kernel(float* __restrict__ w, const float* __restrict__ g, float* __restrict__ m,
+                                      float* __restrict__ v, __nv_bfloat16* __restrict__ wb, long long n,
+                                      const float* __restrict__ sched, const int* __restrict__ t, float beta1,
+                                      float beta2, float eps) {
+    const int k = *t;
+    const float lr = sched[3 * k], c1 = sched[3 * k + 1], c2 = sched[3 * k + 2];
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
          i += (long long)gridDim.x * blockDim.x) {
         const float gi = g[i];
@@ -193,11 +198,16 @@ __global__ void mlp_adam_kernel(float* __restrict__ w, const float* __restrict__
     }
 }
 
-cudaError_t mlp_adam(float* w, const float* g, float* m, float* v, __nv_bfloat16* wb, long long n, float lr,
-                     float beta1, float beta2, float eps, int step, cudaStream_t s) {
-    const float c1 = 1.f / (1.f - powf(beta1, (float)step));
-    const float c2 = 1.f / (1.f - powf(beta2, (float)step));
-    mlp_adam_kernel<<<512, 256, 0, s>>>(w, g, m, v, wb, n, lr, beta1, beta2, eps, c1, c2);
+cudaError_t mlp_adam_sched(float* w, const float* g, float* m, float* v, __nv_bfloat16* wb, long long n,
+                           const float* sched, const int* t, float beta1, float beta2, float eps, cudaStream_t s) {
+    mlp_adam_sched_kernel<<<512, 256, 0, s>>>(w, g, m, v, wb, n, sched, t, beta1, beta2, eps);
+    return cudaGetLastError();
+}
+
+__global__ void mlp_step_advance_kernel(int* t) { *t += 1; }
+
+cudaError_t mlp_step_advance(int* t, cudaStream_t s) {
+    mlp_step_advance_kernel<<<1, 1, 0, s>>>(t);
     return cudaGetLastError();
 }
 
@@ -253,6 +263,27 @@ __global__ void mlp_gather_rows_kernel(const float* __restrict__ x, const int* _
         if (y) y[i] = v;
         if (yb) yb[i] = __float2bfloat16(v);
     }
+}
+
+// The rows of minibatch (*t mod steps) of a permutation: idx + (*t % steps) * rows.
+__global__ void mlp_gather_rows_step_kernel(const float* __restrict__ x, const int* __restrict__ perm,
+                                            const int* __restrict__ t, int steps, int rows, int cols,
+                                            float* __restrict__ y, __nv_bfloat16* __restrict__ yb) {
+    const int* idx = perm + (long long)(*t % steps) * rows;
+    const long long total = (long long)rows * cols;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
+         i += (long long)gridDim.x * blockDim.x) {
+        const long long r = i / cols, c = i % cols;
+        const float v = x[(long long)idx[r] * cols + c];
+        if (y) y[i] = v;
+        if (yb) yb[i] = __float2bfloat16(v);
+    }
+}
+
+cudaError_t mlp_gather_rows_step(const float* x, const int* perm, const int* t, int steps, int rows, int cols,
+                                 float* y, __nv_bfloat16* yb, cudaStream_t s) {
+    mlp_gather_rows_step_kernel<<<512, 256, 0, s>>>(x, perm, t, steps, rows, cols, y, yb);
+    return cudaGetLastError();
 }
 
 cudaError_t mlp_gather_rows(const float* x, const int* idx, int rows, int cols, float* y, __nv_bfloat16* yb,

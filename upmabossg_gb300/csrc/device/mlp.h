@@ -31,6 +31,8 @@ cudaError_t mlp_gemm(const GemmArgs& g, cudaStream_t s);
 // given transposed, K-contiguous), K, a_m and b_n multiples of 8 and 16-byte aligned A and B
 // (mlp_gemm_tc_supported); sets *error_flag if a completion wait gave up.
 bool mlp_gemm_tc_supported(const GemmArgs& g);
+// Sets the kernel's shared-memory limit (once per device, before any launch or graph capture).
+cudaError_t mlp_gemm_tc_configure();
 cudaError_t mlp_gemm_tc(const GemmArgs& g, unsigned* error_flag, cudaStream_t s);
 // y = x^T for a rows x cols BF16 matrix.
 cudaError_t mlp_transpose_bf16(const __nv_bfloat16* x, int rows, int cols, __nv_bfloat16* y, cudaStream_t s);
@@ -44,9 +46,11 @@ cudaError_t mlp_relu_backward(const float* da, const __nv_bfloat16* act, __nv_bf
                               cudaStream_t s);
 // db[c] = sum over rows of d[r, c] (d BF16, rows x cols row-major).
 cudaError_t mlp_bias_grad(const __nv_bfloat16* d, int rows, int cols, float* db, cudaStream_t s);
-// Adam on FP32 master weights; also writes the BF16 copy when wb is not null.
-cudaError_t mlp_adam(float* w, const float* g, float* m, float* v, __nv_bfloat16* wb, long long n, float lr,
-                     float beta1, float beta2, float eps, int step, cudaStream_t s);
+// Adam whose learning rate and bias corrections come from sched[3 * (*t) .. +2] = (lr, 1 / (1 - b1^k),
+// 1 / (1 - b2^k)), and the step counter increment: the step-dependent parts of a replayed graph.
+cudaError_t mlp_adam_sched(float* w, const float* g, float* m, float* v, __nv_bfloat16* wb, long long n,
+                           const float* sched, const int* t, float beta1, float beta2, float eps, cudaStream_t s);
+cudaError_t mlp_step_advance(int* t, cudaStream_t s);
 cudaError_t mlp_to_bf16(const float* x, __nv_bfloat16* y, long long n, cudaStream_t s);
 // probs: E members x rows x cols. mean = member average; spread[r] = max over members of the
 // total-variation distance between the member and the mean.
@@ -55,5 +59,8 @@ cudaError_t mlp_ensemble_stats(const float* probs, int members, int rows, int co
 // y[i, :] = x[idx[i], :] (rows of `cols` floats), converting to BF16 when yb is set.
 cudaError_t mlp_gather_rows(const float* x, const int* idx, int rows, int cols, float* y, __nv_bfloat16* yb,
                             cudaStream_t s);
+// Minibatch (*t mod steps) of the permutation perm (rows indices each).
+cudaError_t mlp_gather_rows_step(const float* x, const int* perm, const int* t, int steps, int rows, int cols,
+                                 float* y, __nv_bfloat16* yb, cudaStream_t s);
 
 }  // namespace mbg

@@ -257,15 +257,12 @@ bool mlp_gemm_tc_supported(const GemmArgs& g) {
            g.b_n % 8 == 0 && aligned16(g.A) && aligned16(g.B);
 }
 
+cudaError_t mlp_gemm_tc_configure() {
+    return cudaFuncSetAttribute(mlp_gemm_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes);
+}
+
 cudaError_t mlp_gemm_tc(const GemmArgs& g, unsigned* error_flag, cudaStream_t s) {
     if (!mlp_gemm_tc_supported(g)) return cudaErrorInvalidValue;
-    static bool configured = false;
-    if (!configured) {
-        cudaError_t e = cudaFuncSetAttribute(mlp_gemm_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             kSmemBytes);
-        if (e != cudaSuccess) return e;
-        configured = true;
-    }
     dim3 grid((g.N + TN - 1) / TN, (g.M + TM - 1) / TM);
     mlp_gemm_tc_kernel<<<grid, 128, kSmemBytes, s>>>(g, error_flag);
     return cudaGetLastError();

@@ -45,29 +45,37 @@ public:
     std::vector<Member> members;
 
 private:
+    // Activations, gradients and the stream of one forward/backward pass. Prediction uses `main`;
+    // training gives every member its own, so that the members train concurrently.
+    struct Work {
+        cudaStream_t stream = nullptr;
+        int cap_rows = 0;
+        __nv_bfloat16* xb = nullptr;
+        float* yt = nullptr;
+        std::vector<__nv_bfloat16*> acts;
+        float* logits = nullptr;
+        __nv_bfloat16* dlogits = nullptr;
+        float* da = nullptr;
+        __nv_bfloat16 *dh = nullptr, *dh2 = nullptr;
+        float* loss = nullptr;
+    };
     template <class T>
     T* alloc(size_t n);
+    void ensure_work(Work& w, int rows);
     void ensure_batch(int rows);
-    void forward(int member, int rows);
-    void backward(int member, int rows);
-    void adam_step(int member, float lr);
-    void refresh_transposed(int member);
+    void forward(int member, int rows, Work& w);
+    void backward(int member, int rows, Work& w);
+    void refresh_transposed(int member, cudaStream_t s);
     void check_tc_error();
 
     cudaStream_t stream = nullptr;
-    int cap_rows = 0;
-    __nv_bfloat16* xb = nullptr;
+    Work main;
+    std::vector<Work> train_work;
+    int cap_rows = 0;  // prediction buffers below
     float* xf = nullptr;
-    float* yt = nullptr;
-    std::vector<__nv_bfloat16*> acts;
-    float* logits = nullptr;
     float* probs = nullptr;
-    __nv_bfloat16* dlogits = nullptr;
-    float* da = nullptr;
-    __nv_bfloat16 *dh = nullptr, *dh2 = nullptr;
     float* mean = nullptr;
     float* spread = nullptr;
-    float* loss = nullptr;
     unsigned* tc_error = nullptr;   // set by a tcgen05 GEMM whose mbarrier wait gave up
     std::vector<bool> wt_stale;     // per member: wtb behind wb
     std::vector<void*> owned;
