@@ -21,7 +21,7 @@ extern "C" __global__ void __launch_bounds__(256, 4) mbg_sim_warp(const SimParam
 }
 
 // Gather variant, for models whose index cache would not fit beside enough warps.
-extern "C" __global__ void __launch_bounds__(256) mbg_sim_warp_gather(const SimParams p) {
+extern "C" __global__ void __launch_bounds__(256, 4) mbg_sim_warp_gather(const SimParams p) {
     extern __shared__ __align__(16) unsigned char smem[];
     sim_warp_body<false>(p, smem);
 }

@@ -69,6 +69,16 @@ __device__ __forceinline__ NodeHead load_head(const SimParams& p, int i) {
 
 __device__ __forceinline__ unsigned st_bit(const unsigned* st, int i) { return (st[i >> 5] >> (i & 31)) & 1u; }
 
+// Regulator index of a node with k <= 4 regulators packed as r01 = r0 | r1 << 16, r23 likewise.
+__device__ __forceinline__ unsigned warp_idx4(const unsigned* st, int k, unsigned r01, unsigned r23) {
+    unsigned idx = 0u;
+    if (k > 0) idx |= st_bit(st, (int)(r01 & 0xffffu));
+    if (k > 1) idx |= st_bit(st, (int)(r01 >> 16)) << 1;
+    if (k > 2) idx |= st_bit(st, (int)(r23 & 0xffffu)) << 2;
+    if (k > 3) idx |= st_bit(st, (int)(r23 >> 16)) << 3;
+    return idx;
+}
+
 // Regulator index of node i in state st (bit j = state of its j-th regulator).
 __device__ __forceinline__ unsigned gather_regs(const SimParams& p, int i, const NodeHead& h, const unsigned* st) {
     unsigned idx = 0u;
@@ -337,26 +347,30 @@ __device__ unsigned char warp_trajectory(const SimParams& p, const WarpSmem& m, 
                 const unsigned pos = e & 0xffu;
                 const unsigned self = st_bit(m.st, dn);
                 const unsigned self_old = pos == 0xffu ? self ^ 1u : self;
+                // the reader's 32-byte record: rates, and for up to 4 regulators their ids and table
+                const uint4* rec = reinterpret_cast<const uint4*>(p.lnodes + dn);
+                const uint4 ra = __ldg(rec), rb = __ldg(rec + 1);
+                const unsigned flags = rb.w >> 16;
                 unsigned idx, idx_old;
                 if (IDX) {
                     idx_old = m.idx[dn];
                     idx = pos == 0xffu ? idx_old : idx_old ^ (1u << pos);
                     if (pos != 0xffu) m.idx[dn] = idx;
                 } else {
-                    idx = gather_regs(p, dn, load_head(p, dn), m.st);
+                    idx = flags == 0u ? warp_idx4(m.st, kd, rb.y, rb.z) : gather_regs(p, dn, load_head(p, dn), m.st);
                     idx_old = pos == 0xffu ? idx : idx ^ (1u << pos);
                 }
                 unsigned long long r_new, r_old;
                 unsigned a_new, a_old;
-                const NodeHead hd = p.has_palette ? load_head(p, dn) : NodeHead{};
-                if (!p.has_palette || hd.kind == 0) {
-                    unsigned long long up, down;
-                    load_rates(p, dn, up, down);
-                    a_new = table_bit(p, dn, kd, self, idx);
+                if (!(flags & kLanePalette)) {
+                    const unsigned long long up = ((unsigned long long)ra.y << 32) | ra.x;
+                    const unsigned long long down = ((unsigned long long)ra.w << 32) | ra.z;
+                    a_new = flags == 0u ? (rb.x >> ((self << kd) | idx)) & 1u : table_bit(p, dn, kd, self, idx);
                     a_old = st_bit(m.act, dn);
                     r_new = a_new ? (self ? down : up) : 0ull;
                     r_old = a_old ? (self_old ? down : up) : 0ull;
                 } else {
+                    const NodeHead hd = load_head(p, dn);
                     r_new = palette_rate(p, hd, self, idx);
                     r_old = palette_rate(p, hd, self_old, idx_old);
                     a_new = r_new != 0ull;
