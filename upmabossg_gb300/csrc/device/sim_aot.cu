@@ -311,7 +311,11 @@ cudaError_t sim_lane_batch_configure(bool coop, size_t smem, int block, int* blo
                           block, blocks_per_sm);
 }
 
-size_t sim_lane_smem(int n, int block) { return (size_t)block * lane_smem_bytes(n) + lane_block_extra(block); }
+size_t sim_lane_smem(int n, int block, bool coop) {
+    return (size_t)block * lane_smem_bytes(n) + (coop ? lane_block_extra(block) : 0);
+}
+
+int sim_lane_rows(int n) { return lane_groups(n); }
 
 cudaError_t launch_fp_aggregate(const unsigned* fp_states, const unsigned* fp_count, unsigned capacity, int words,
                                 unsigned* slot_rep, unsigned* slot_cnt, unsigned n_slots, unsigned* out_states,

@@ -23,7 +23,8 @@ namespace mbg {
 __host__ __device__ __forceinline__ int lane_groups(int n) { return (n + 31) >> 5; }
 // Shared-memory bytes per thread (plus lane_block_extra per block).
 __host__ __device__ __forceinline__ unsigned lane_smem_bytes(int n) { return 16u * (unsigned)lane_groups(n); }
-// Per block: one word per warp (lanes whose output-node rates changed in a cooperative update).
+// Per block of the cooperative variant: one word per warp (lanes whose output-node rates changed in
+// a cooperative update); the per-lane variant needs none.
 __host__ __device__ __forceinline__ unsigned lane_block_extra(int block) { return 4u * (unsigned)((block + 31) / 32); }
 
 struct LaneSmem {

@@ -110,7 +110,7 @@ struct BatchDesc {
     int n_inst;
     unsigned long long* work;          // work-item counter
     unsigned slice_bytes;              // warp layout, per warp: SimParams copy (16-byte padded) + largest slice
-    int rows;                          // lane layout: shared-memory rows (groups of the largest instance)
+    int rows;                          // lane layout: 32-node groups of the largest instance
 };
 
 // Fixed-point hash table and compacted output of one batched instance.
