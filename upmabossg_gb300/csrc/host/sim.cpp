@@ -273,8 +273,12 @@ void Sim::autotune() {
     }
     // time every layout and block size on the pilot; all give identical results, so the kernel
     // times compare the same work
-    const uint64_t saved_n = prm.n_traj;
-    prm.n_traj = pilot;
+    struct PilotScope {  // the pilot's trajectory count, restored however the timing ends
+        SimParams& p;
+        uint64_t saved;
+        PilotScope(SimParams& q, uint64_t n) : p(q), saved(q.n_traj) { p.n_traj = n; }
+        ~PilotScope() { p.n_traj = saved; }
+    } scope(prm, pilot);
     const bool log = std::getenv("MBG_AUTOTUNE_LOG") != nullptr;
     double best = -1;
     Shape best_shape{MBG_LAYOUT_WARP, 256, false};
@@ -285,7 +289,11 @@ void Sim::autotune() {
                 if (lay != MBG_LAYOUT_LANE && (blk == 64 || coop)) continue;
                 if (lay == MBG_LAYOUT_THREAD && cm.words > 16) continue;
                 if (lay == MBG_LAYOUT_LANE && sim_lane_smem(cm.n, blk, coop != 0) > 227 * 1024) continue;
-                setup_layout(lay, blk, coop != 0);
+                try {
+                    setup_layout(lay, blk, coop != 0);
+                } catch (const JitError&) {
+                    continue;  // a thread-layout kernel NVRTC cannot build: the other layouts remain
+                }
                 run(nullptr);  // warm-up (and JIT load)
                 run(nullptr);
                 if (log)
@@ -298,7 +306,7 @@ void Sim::autotune() {
             }
         }
     }
-    prm.n_traj = saved_n;
+    scope.p.n_traj = scope.saved;
     ran = false;
     setup_layout(best_shape.layout, best_shape.block, best_shape.coop);
     std::lock_guard<std::mutex> lock(g_tune_mu);
