@@ -23,11 +23,21 @@ namespace mbg {
 
 namespace {
 
-constexpr int TM = 128, TN = 128, TK = 64, kStages = 3;
-constexpr int kTileBytes = TM * TK * 2;                      // 16 KiB per operand tile
-constexpr int kStageBytes = 2 * kTileBytes;                  // A tile, then B tile
-constexpr int kSmemBytes = kStages * kStageBytes + 1024;     // + alignment slack
-constexpr unsigned kSpinLimit = 1u << 26;                    // bounded mbarrier waits
+constexpr int TM = 128, TK = 64;
+constexpr int kTileBytesA = TM * TK * 2;  // 16 KiB A tile per stage
+constexpr unsigned kSpinLimit = 1u << 26;  // bounded mbarrier waits
+
+// Shapes: TN output columns per CTA (the MMA's N and the TMEM columns it holds), STAGES deep ring.
+template <int TN, int STAGES>
+struct TcShape {
+    static constexpr int kTileBytesB = TN * TK * 2;
+    static constexpr int kStageBytes = kTileBytesA + kTileBytesB;       // A tile, then B tile
+    static constexpr int kSmemBytes = STAGES * kStageBytes + 1024;      // + alignment slack
+    // Instruction descriptor of kind::f16: FP32 accumulator (bits 4-5 = 1), BF16 A and B (bits 7-9
+    // and 10-12 = 1), both K-major (bits 15, 16 = 0), N / 8 at bits 17-22, M / 16 at bits 24-28.
+    static constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(TN >> 3) << 17) |
+                                       ((uint32_t)(TM >> 4) << 24);
+};
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -38,11 +48,6 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint3
     return (uint64_t)((addr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
            ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
 }
-
-// Instruction descriptor of kind::f16: FP32 accumulator (bits 4-5 = 1), BF16 A and B (bits 7-9 and
-// 10-12 = 1), both K-major (bits 15, 16 = 0), N / 8 at bits 17-22, M / 16 at bits 24-28.
-constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(TN >> 3) << 17) |
-                            ((uint32_t)(TM >> 4) << 24);
 
 __device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
@@ -64,11 +69,12 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity) {
     return false;
 }
 
-__device__ __forceinline__ void mma_bf16_tc(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t accumulate) {
+__device__ __forceinline__ void mma_bf16_tc(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                            uint32_t accumulate) {
     asm volatile(
         "{\n .reg .pred p;\n setp.ne.u32 p, %4, 0;\n"
         " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
-        "l"(adesc), "l"(bdesc), "r"(kIdesc), "r"(accumulate)
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
         : "memory");
 }
 
@@ -97,10 +103,11 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
 // matrix (row stride ld elements) into the core-matrix layout at shared address dst: chunk c
 // (16 bytes) of the tile is row (c / 64) * 8 + c % 8, k group (c / 8) % 8, stored at byte 16 c, so
 // a warp's 32 chunks cover 8 rows x 64 contiguous bytes. Chunks outside the matrix are zero-filled.
+template <int ROWS>
 __device__ __forceinline__ void load_tile_async(uint32_t dst, const __nv_bfloat16* src, long long ld, int r0,
                                                 int rows, int k0, int K) {
 #pragma unroll
-    for (int i = 0; i < (TM * TK / 8) / 128; ++i) {
+    for (int i = 0; i < (ROWS * TK / 8) / 128; ++i) {
         const int c = (int)threadIdx.x + 128 * i;
         const int r = (c >> 6) * 8 + (c & 7);
         const int kq = (c >> 3) & 7;
@@ -120,7 +127,10 @@ __device__ __forceinline__ void cp_async_wait() {
 
 }  // namespace
 
+template <int TN, int STAGES>
 __global__ void __launch_bounds__(128) mlp_gemm_tc_kernel(const GemmArgs g, unsigned* error_flag) {
+    using S = TcShape<TN, STAGES>;
+    constexpr int kStages = STAGES, kStageBytes = S::kStageBytes;
     extern __shared__ unsigned char smem_raw[];
     __shared__ __align__(8) uint64_t bar[kStages];
     __shared__ uint32_t tmem_slot;
@@ -147,8 +157,8 @@ __global__ void __launch_bounds__(128) mlp_gemm_tc_kernel(const GemmArgs g, unsi
     for (int st = 0; st < kStages - 1; ++st) {
         if (st < nk) {
             const uint32_t d = sbase + st * kStageBytes;
-            load_tile_async(d, A, g.a_m, m0, g.M, st * TK, g.K);
-            load_tile_async(d + kTileBytes, g.B, g.b_n, n0, g.N, st * TK, g.K);
+            load_tile_async<TM>(d, A, g.a_m, m0, g.M, st * TK, g.K);
+            load_tile_async<TN>(d + kTileBytesA, g.B, g.b_n, n0, g.N, st * TK, g.K);
         }
         cp_async_commit();
     }
@@ -167,12 +177,12 @@ __global__ void __launch_bounds__(128) mlp_gemm_tc_kernel(const GemmArgs g, unsi
         if (threadIdx.x == 0) {
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
             const int steps = (min(TK, g.K - kb * TK) + 15) / 16;
-            const uint32_t a_addr = sbase + stage * kStageBytes, b_addr = a_addr + kTileBytes;
+            const uint32_t a_addr = sbase + stage * kStageBytes, b_addr = a_addr + kTileBytesA;
             for (int s = 0; s < steps; ++s) {
                 // K step s covers k groups 2s and 2s+1: 256 bytes further into each tile
                 const uint64_t ad = smem_desc(a_addr + 256u * s, 128u, 1024u);
                 const uint64_t bd = smem_desc(b_addr + 256u * s, 128u, 1024u);
-                mma_bf16_tc(tmem, ad, bd, (kb > 0 || s > 0) ? 1u : 0u);
+                mma_bf16_tc(tmem, ad, bd, S::kIdesc, (kb > 0 || s > 0) ? 1u : 0u);
             }
             mma_commit(&bar[stage]);
         }
@@ -182,8 +192,8 @@ __global__ void __launch_bounds__(128) mlp_gemm_tc_kernel(const GemmArgs g, unsi
             const int ns = next % kStages;
             if (kb >= 1 && !mbar_wait(&bar[ns], (unsigned)(((kb - 1) / kStages) & 1))) ok = false;
             const uint32_t d = sbase + ns * kStageBytes;
-            load_tile_async(d, A, g.a_m, m0, g.M, next * TK, g.K);
-            load_tile_async(d + kTileBytes, g.B, g.b_n, n0, g.N, next * TK, g.K);
+            load_tile_async<TM>(d, A, g.a_m, m0, g.M, next * TK, g.K);
+            load_tile_async<TN>(d + kTileBytesA, g.B, g.b_n, n0, g.N, next * TK, g.K);
         }
         cp_async_commit();
     }
@@ -258,13 +268,26 @@ bool mlp_gemm_tc_supported(const GemmArgs& g) {
 }
 
 cudaError_t mlp_gemm_tc_configure() {
-    return cudaFuncSetAttribute(mlp_gemm_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes);
+    cudaError_t e = cudaFuncSetAttribute(mlp_gemm_tc_kernel<128, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         TcShape<128, 3>::kSmemBytes);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(mlp_gemm_tc_kernel<256, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 TcShape<256, 2>::kSmemBytes);
+    return e;
 }
 
 cudaError_t mlp_gemm_tc(const GemmArgs& g, unsigned* error_flag, cudaStream_t s) {
     if (!mlp_gemm_tc_supported(g)) return cudaErrorInvalidValue;
-    dim3 grid((g.N + TN - 1) / TN, (g.M + TM - 1) / TM);
-    mlp_gemm_tc_kernel<<<grid, 128, kSmemBytes, s>>>(g, error_flag);
+    const dim3 rows(1, (g.M + TM - 1) / TM);
+    if (g.N > 128) {
+        // 128 x 256 tiles: half the A traffic of 128-wide tiles, two CTAs per SM (96 KB ring each,
+        // 256 TMEM columns each)
+        mlp_gemm_tc_kernel<256, 2><<<dim3((g.N + 255) / 256, rows.y), 128, TcShape<256, 2>::kSmemBytes, s>>>(
+            g, error_flag);
+    } else {
+        mlp_gemm_tc_kernel<128, 3><<<dim3((g.N + 127) / 128, rows.y), 128, TcShape<128, 3>::kSmemBytes, s>>>(
+            g, error_flag);
+    }
     return cudaGetLastError();
 }
 
