@@ -25,7 +25,7 @@ namespace {
 
 constexpr int TM = 128, TK = 64;
 constexpr int kTileBytesA = TM * TK * 2;  // 16 KiB A tile per stage
-constexpr unsigned kSpinLimit = 1u << 26;  // bounded mbarrier waits
+constexpr unsigned kSpinLimit = 1u << 22;  // bounded mbarrier waits
 
 // Shapes: TN output columns per CTA (the MMA's N and the TMEM columns it holds), STAGES deep ring.
 template <int TN, int STAGES>
@@ -201,6 +201,7 @@ __global__ void __launch_bounds__(128) mlp_gemm_tma_kernel(const __grid_constant
     const uint32_t lane_addr = tmem + ((uint32_t)(warp * 32) << 16);
     const bool vec_b = g.Cb && (g.ldcb % 8) == 0 && ((uintptr_t)g.Cb & 15u) == 0;
     const bool vec_f = g.C && !g.accumulate && (g.ldc % 4) == 0 && ((uintptr_t)g.C & 15u) == 0;
+    const bool vec_bias = ((uintptr_t)g.bias & 15u) == 0 && (n0 % 4) == 0;
 #pragma unroll 1
     for (int c0 = 0; c0 < TN; c0 += 32) {
         float v[32];
@@ -208,14 +209,28 @@ __global__ void __launch_bounds__(128) mlp_gemm_tma_kernel(const __grid_constant
         tmem_ld32(lane_addr + (uint32_t)c0, v);
         const int col0 = n0 + c0;
         if (!ok || row >= g.M || col0 >= g.N) continue;
+        const bool full_cols = col0 + 32 <= g.N;
+        float bias[32];
+        if (g.bias && full_cols && vec_bias) {
+            // the same 32 values for every lane: eight 16-byte broadcast loads
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+                const float4 b4 = __ldg(reinterpret_cast<const float4*>(g.bias + col0) + q);
+                bias[4 * q] = b4.x;
+                bias[4 * q + 1] = b4.y;
+                bias[4 * q + 2] = b4.z;
+                bias[4 * q + 3] = b4.w;
+            }
+        } else {
+#pragma unroll
+            for (int i = 0; i < 32; ++i) bias[i] = g.bias && col0 + i < g.N ? __ldg(g.bias + col0 + i) : 0.f;
+        }
 #pragma unroll
         for (int i = 0; i < 32; ++i) {
-            float x = g.alpha * (nk > 0 ? v[i] : 0.f);
-            if (g.bias && col0 + i < g.N) x += __ldg(g.bias + col0 + i);
+            float x = g.alpha * (nk > 0 ? v[i] : 0.f) + bias[i];
             if (g.relu) x = x > 0.f ? x : 0.f;
             v[i] = x;
         }
-        const bool full_cols = col0 + 32 <= g.N;
         if (g.Cb) {
             __nv_bfloat16* dst = g.Cb + (long long)row * g.ldcb + col0;
             if (full_cols && vec_b) {
