@@ -108,6 +108,12 @@ int mbg_device_count(void);
 
 mbg_status mbg_model_parse_files(const char* bnd_path, const char* cfg_path, mbg_model** out);
 mbg_status mbg_model_parse_strings(const char* bnd_text, const char* cfg_text, mbg_model** out);
+/* mbg_model_parse_files followed by the cfg statements in `cfg_overrides` (NULL or "": none),
+ * applied after the cfg file so that they replace its values: `$var = 2;`, `max_time = 50;`,
+ * `sample_count = 1000;`, `A.istate = 1;`, `[A].istate = 0.3 [1], 0.7 [0];`. Parameter overrides
+ * without editing the model files (the role of MaBoSS's `-e` configuration expressions). */
+mbg_status mbg_model_parse_files_overrides(const char* bnd_path, const char* cfg_path, const char* cfg_overrides,
+                                           mbg_model** out);
 void mbg_model_destroy(mbg_model* m);
 mbg_status mbg_model_info_get(const mbg_model* m, mbg_model_info* out);
 const char* mbg_model_node_name(const mbg_model* m, int32_t i);
@@ -127,6 +133,15 @@ mbg_status mbg_model_rate(const mbg_model* m, int32_t node, const uint8_t* state
  * them). */
 mbg_status mbg_model_with_rate_scales(const mbg_model* base, const double* up_scale, const double* down_scale,
                                       mbg_model** out);
+
+/* Mutant analysis: a copy of `base` with node nodes[j] clamped ON (values[j] = 1) or OFF (0). A
+ * clamped node starts at its value and its rate is zero wherever it holds it, so it never leaves
+ * it; every other node is unchanged. The copy simulates exactly as the model whose cfg sets the
+ * node's istate to the value and whose bnd sets its rate_down (ON) or rate_up (OFF) to 0. The
+ * reference lists mutant analysis as future work (README.md "Next steps"). No expression trees
+ * in the copy, as for mbg_model_with_rate_scales. */
+mbg_status mbg_model_with_mutations(const mbg_model* base, const int32_t* nodes, const int32_t* values,
+                                    int32_t count, mbg_model** out);
 
 /* Generates the model's thread-per-trajectory kernel and compiles it with NVRTC for sm_103a
  * without loading it (needs no GPU). */
@@ -155,6 +170,11 @@ mbg_status mbg_sim_trajectories(mbg_sim* s, uint32_t* states, double* times, uin
 
 mbg_status mbg_write_probtraj_csv(mbg_sim* s, const char* prefix);
 mbg_status mbg_write_fp_csv(mbg_sim* s, const char* prefix);
+/* <prefix>_final_states.csv: `Final States (K)`, a header `Proba\tState\t<output nodes>`, then one
+ * row per reached output state (increasing index) with its share of the trajectories, its name
+ * and one 0/1 column per output node. The reference prints this histogram to stdout only
+ * (final_states.cpp:53-68). */
+mbg_status mbg_write_final_states_csv(mbg_sim* s, const char* prefix);
 /* The reference's stdout report (final points, fixed points, windows) to a file path or "-". */
 mbg_status mbg_print_results(mbg_sim* s, const char* path);
 

@@ -23,12 +23,12 @@ STATUS = {0: "OK", 1: "ARG", 2: "IO", 3: "PARSE", 4: "MODEL", 5: "CUDA", 6: "JIT
 EXPORTS = (
     "mbg_last_error", "mbg_version", "mbg_device_count", "mbg_model_parse_files", "mbg_model_parse_strings",
     "mbg_model_destroy", "mbg_model_info_get", "mbg_model_node_name", "mbg_model_outputs", "mbg_model_rate",
-    "mbg_model_with_rate_scales",
+    "mbg_model_with_rate_scales", "mbg_model_parse_files_overrides", "mbg_model_with_mutations",
     "mbg_model_jit_check",
     "mbg_sim_opts_default", "mbg_sim_create", "mbg_sim_destroy", "mbg_sim_run", "mbg_sim_summary",
     "mbg_sim_probtraj", "mbg_sim_probtraj_raw", "mbg_sim_final_states", "mbg_sim_fixed_points",
     "mbg_sim_trajectories", "mbg_write_probtraj_csv", "mbg_write_fp_csv", "mbg_print_results",
-    "mbg_fixed_points_aggregate_noalloc",
+    "mbg_write_final_states_csv", "mbg_fixed_points_aggregate_noalloc",
     "mbg_batch_opts_default", "mbg_batch_create", "mbg_batch_destroy", "mbg_batch_run", "mbg_batch_summary",
     "mbg_batch_instance_summary", "mbg_batch_probtraj", "mbg_batch_probtraj_raw", "mbg_batch_final_states",
     "mbg_batch_fixed_points", "mbg_batch_class_count", "mbg_batch_class", "mbg_batch_class_timings",
@@ -109,6 +109,9 @@ def lib():
             "mbg_device_count": (ctypes.c_int, []),
             "mbg_model_parse_files": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_char_p, ctypes.POINTER(vp)]),
             "mbg_model_parse_strings": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_char_p, ctypes.POINTER(vp)]),
+            "mbg_model_parse_files_overrides": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p,
+                                                               ctypes.POINTER(vp)]),
+            "mbg_model_with_mutations": (ctypes.c_int, [vp, dp, dp, i32, ctypes.POINTER(vp)]),
             "mbg_model_destroy": (None, [vp]),
             "mbg_model_info_get": (ctypes.c_int, [vp, ctypes.POINTER(ModelInfo)]),
             "mbg_model_node_name": (ctypes.c_char_p, [vp, i32]),
@@ -128,6 +131,7 @@ def lib():
             "mbg_sim_trajectories": (ctypes.c_int, [vp, dp, dp, dp, dp]),
             "mbg_write_probtraj_csv": (ctypes.c_int, [vp, ctypes.c_char_p]),
             "mbg_write_fp_csv": (ctypes.c_int, [vp, ctypes.c_char_p]),
+            "mbg_write_final_states_csv": (ctypes.c_int, [vp, ctypes.c_char_p]),
             "mbg_print_results": (ctypes.c_int, [vp, ctypes.c_char_p]),
             "mbg_fixed_points_aggregate_noalloc": (ctypes.c_int, [vp, ctypes.c_uint32, i32, vp, vp, vp, vp]),
             "mbg_batch_opts_default": (None, [ctypes.POINTER(BatchOpts)]),
@@ -193,9 +197,15 @@ class Model:
         self.outputs = [int(x) for x in out[:info.outputs]]
 
     @classmethod
-    def from_files(cls, bnd_path, cfg_path):
+    def from_files(cls, bnd_path, cfg_path, overrides=None):
+        """Parse the model files; `overrides` (cfg statements, e.g. "$k = 2; max_time = 50;") are
+        applied after the cfg file and replace its values."""
         h = ctypes.c_void_p()
-        _check(lib().mbg_model_parse_files(os.fsencode(bnd_path), os.fsencode(cfg_path), ctypes.byref(h)))
+        if overrides:
+            _check(lib().mbg_model_parse_files_overrides(os.fsencode(bnd_path), os.fsencode(cfg_path),
+                                                         overrides.encode(), ctypes.byref(h)))
+        else:
+            _check(lib().mbg_model_parse_files(os.fsencode(bnd_path), os.fsencode(cfg_path), ctypes.byref(h)))
         return cls(h)
 
     @classmethod
@@ -223,6 +233,24 @@ class Model:
                 raise ValueError("one scale per node")
         h = ctypes.c_void_p()
         _check(lib().mbg_model_with_rate_scales(self._h, _p(u), _p(d), ctypes.byref(h)))
+        return Model(h)
+
+    def with_mutations(self, mutants) -> "Model":
+        """Mutant copy: `mutants` maps node names (or indices) to "ON"/"OFF" (or 1/0); each such
+        node starts at that value and never leaves it."""
+        idx, val = [], []
+        for k, v in dict(mutants).items():
+            i = self.names.index(k) if isinstance(k, str) else int(k)
+            if isinstance(v, str):
+                if v.upper() not in ("ON", "OFF"):
+                    raise ValueError(f"mutant value {v!r}: expected ON or OFF")
+                v = 1 if v.upper() == "ON" else 0
+            idx.append(i)
+            val.append(int(v))
+        n = np.ascontiguousarray(np.asarray(idx, dtype=np.int32))
+        w = np.ascontiguousarray(np.asarray(val, dtype=np.int32))
+        h = ctypes.c_void_p()
+        _check(lib().mbg_model_with_mutations(self._h, _p(n), _p(w), len(idx), ctypes.byref(h)))
         return Model(h)
 
     def jit_check(self) -> float:
@@ -316,9 +344,11 @@ class Simulation:
         _check(lib().mbg_sim_trajectories(self._h, _p(st), _p(t), _p(tr), _p(s)))
         return st, t, tr, s
 
-    def write_csv(self, prefix):
+    def write_csv(self, prefix, final_states=False):
         _check(lib().mbg_write_probtraj_csv(self._h, os.fsencode(prefix)))
         _check(lib().mbg_write_fp_csv(self._h, os.fsencode(prefix)))
+        if final_states:
+            _check(lib().mbg_write_final_states_csv(self._h, os.fsencode(prefix)))
 
     def print_results(self, path="-"):
         _check(lib().mbg_print_results(self._h, os.fsencode(path)))

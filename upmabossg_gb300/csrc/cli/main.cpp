@@ -7,7 +7,10 @@
 // (main.cpp:148-152) is lifted to the library's own limits.
 //
 // Environment (the argument list stays the reference's): MBG_DEVICE (CUDA ordinal),
-// MBG_LAYOUT (auto | thread | warp | lane), MBG_TIMINGS=1 (JSON run summary on stderr).
+// MBG_LAYOUT (auto | thread | warp | lane), MBG_TIMINGS=1 (JSON run summary on stderr),
+// MBG_CONFIG_EXPR (cfg statements applied after the cfg file, e.g. "$k = 2; max_time = 50;"),
+// MBG_MUTANTS (comma-separated NODE:ON / NODE:OFF clamps), MBG_FINAL_STATES_CSV=1 (with -o,
+// also <prefix>_final_states.csv).
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -30,9 +33,45 @@ int main(int argc, char** argv) {
         cfg = args[3];
     }
     mbg_model* model = nullptr;
-    if (mbg_model_parse_files(bnd.c_str(), cfg.c_str(), &model) != MBG_OK) {
+    if (mbg_model_parse_files_overrides(bnd.c_str(), cfg.c_str(), std::getenv("MBG_CONFIG_EXPR"), &model) != MBG_OK) {
         std::cerr << mbg_last_error() << std::endl;
         return 1;
+    }
+    if (const char* mu = std::getenv("MBG_MUTANTS"); mu && *mu) {
+        mbg_model_info mi;
+        mbg_model_info_get(model, &mi);
+        std::vector<int32_t> nodes, values;
+        std::string spec(mu), bad;
+        size_t pos = 0;
+        while (pos <= spec.size() && bad.empty()) {
+            size_t end = spec.find(',', pos);
+            if (end == std::string::npos) end = spec.size();
+            std::string item = spec.substr(pos, end - pos);
+            pos = end + 1;
+            if (item.empty()) continue;
+            size_t colon = item.rfind(':');
+            std::string name = colon == std::string::npos ? item : item.substr(0, colon);
+            std::string val = colon == std::string::npos ? "" : item.substr(colon + 1);
+            int32_t idx = -1;
+            for (int32_t i = 0; i < mi.nodes; ++i)
+                if (name == mbg_model_node_name(model, i)) idx = i;
+            if (idx < 0 || (val != "ON" && val != "OFF")) {
+                bad = item;
+                break;
+            }
+            nodes.push_back(idx);
+            values.push_back(val == "ON" ? 1 : 0);
+        }
+        mbg_model* mutant = nullptr;
+        if (!bad.empty()) {
+            std::cerr << "MBG_MUTANTS: cannot read '" << bad << "' (expected NODE:ON or NODE:OFF)" << std::endl;
+        } else if (mbg_model_with_mutations(model, nodes.data(), values.data(), (int32_t)nodes.size(), &mutant) !=
+                   MBG_OK) {
+            std::cerr << mbg_last_error() << std::endl;
+        }
+        mbg_model_destroy(model);
+        if (!mutant) return 1;
+        model = mutant;
     }
     mbg_model_info info;
     mbg_model_info_get(model, &info);
@@ -60,6 +99,8 @@ int main(int argc, char** argv) {
                             : (mbg_write_probtraj_csv(sim, prefix.c_str()) == MBG_OK
                                    ? mbg_write_fp_csv(sim, prefix.c_str())
                                    : MBG_ERR_IO);
+        const char* fs = std::getenv("MBG_FINAL_STATES_CSV");
+        if (st == MBG_OK && !prefix.empty() && fs && *fs == '1') st = mbg_write_final_states_csv(sim, prefix.c_str());
         if (st != MBG_OK) {
             std::cerr << mbg_last_error() << std::endl;
             rc = 1;

@@ -73,13 +73,14 @@ mbg_status guard(F&& f) {
 }
 
 mbg_status build_model(const std::string& bnd, const std::string& cfg, const std::string& bnd_name,
-                       const std::string& cfg_name, mbg_model** out) {
+                       const std::string& cfg_name, mbg_model** out, const char* overrides = nullptr) {
     if (!out) return fail(MBG_ERR_ARG, "null output pointer");
     *out = nullptr;
     std::unique_ptr<mbg_model> m(new mbg_model());
     mbg_status st = guard([&] {
         mbg::parse_bnd(m->model, bnd, bnd_name);
         mbg::parse_cfg(m->model, cfg, cfg_name);
+        if (overrides && *overrides) mbg::parse_cfg(m->model, overrides, "<overrides>");
     });
     if (st != MBG_OK) return st;
     st = guard([&] {
@@ -117,6 +118,11 @@ int mbg_device_count(void) {
 }
 
 mbg_status mbg_model_parse_files(const char* bnd_path, const char* cfg_path, mbg_model** out) {
+    return mbg_model_parse_files_overrides(bnd_path, cfg_path, nullptr, out);
+}
+
+mbg_status mbg_model_parse_files_overrides(const char* bnd_path, const char* cfg_path, const char* cfg_overrides,
+                                           mbg_model** out) {
     if (!bnd_path || !cfg_path) return fail(MBG_ERR_ARG, "null path");
     std::string bnd, cfg;
     try {
@@ -125,7 +131,7 @@ mbg_status mbg_model_parse_files(const char* bnd_path, const char* cfg_path, mbg
     } catch (const std::exception& e) {
         return fail(MBG_ERR_IO, e.what());
     }
-    return build_model(bnd, cfg, bnd_path, cfg_path, out);
+    return build_model(bnd, cfg, bnd_path, cfg_path, out, cfg_overrides);
 }
 
 mbg_status mbg_model_parse_strings(const char* bnd_text, const char* cfg_text, mbg_model** out) {
@@ -198,6 +204,25 @@ mbg_status mbg_model_with_rate_scales(const mbg_model* base, const double* up_sc
     std::unique_ptr<mbg_model> m(new mbg_model());
     mbg_status st = guard([&] {
         m->cm = mbg::rescale_model(base->cm, up_scale, down_scale);
+        m->names = base->names;
+    });
+    if (st != MBG_OK) return st;
+    *out = m.release();
+    return MBG_OK;
+}
+
+mbg_status mbg_model_with_mutations(const mbg_model* base, const int32_t* nodes, const int32_t* values,
+                                    int32_t count, mbg_model** out) {
+    if (!base || !out || (count > 0 && (!nodes || !values)) || count < 0) return fail(MBG_ERR_ARG, "null argument");
+    *out = nullptr;
+    std::unique_ptr<mbg_model> m(new mbg_model());
+    mbg_status st = guard([&] {
+        std::vector<int> nd(nodes, nodes + count), val(values, values + count);
+        try {
+            m->cm = mbg::mutate_model(base->cm, nd.data(), val.data(), count);
+        } catch (const mbg::Error& e) {
+            throw mbg::ModelError(e.what());
+        }
         m->names = base->names;
     });
     if (st != MBG_OK) return st;
@@ -323,6 +348,14 @@ mbg_status mbg_write_fp_csv(mbg_sim* s, const char* prefix) {
     return guard([&] {
         s->sim.fetch();
         mbg::write_fp_csv(s->sim, std::string(prefix) + "_fp.csv");
+    });
+}
+
+mbg_status mbg_write_final_states_csv(mbg_sim* s, const char* prefix) {
+    if (!s || !prefix) return fail(MBG_ERR_ARG, "null argument");
+    return guard([&] {
+        s->sim.fetch();
+        mbg::write_final_states_csv(s->sim, std::string(prefix) + "_final_states.csv");
     });
 }
 

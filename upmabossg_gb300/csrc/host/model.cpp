@@ -262,6 +262,113 @@ static int frac_bits_for(double sum_max) {
     return fb;
 }
 
+// Binary form (one up rate, one down rate, a bit per assignment saying whether the rate is
+// non-zero) when every non-zero up value is equal and every non-zero down value is equal,
+// palette form otherwise. `tab` holds the node's rate per assignment (self bit k).
+static void classify_node(CompiledNode& cn, const std::vector<double>& tab, int fb, const std::string& name) {
+    const int k = (int)cn.regs.size();
+    const uint64_t half = 1ull << k, total = half << 1;
+    std::set<double> upv, dnv;
+    for (uint64_t a = 0; a < total; ++a)
+        if (tab[a] != 0) (a < half ? upv : dnv).insert(tab[a]);
+    cn.bits.clear();
+    cn.pidx.clear();
+    cn.palette.clear();
+    cn.palette_real.clear();
+    if (upv.size() <= 1 && dnv.size() <= 1) {
+        cn.kind = NODE_BINARY;
+        cn.up_real = upv.empty() ? 0 : *upv.begin();
+        cn.down_real = dnv.empty() ? 0 : *dnv.begin();
+        cn.up = quantize_rate(cn.up_real, fb);
+        cn.down = quantize_rate(cn.down_real, fb);
+        cn.bits.assign((total + 31) / 32, 0u);
+        for (uint64_t a = 0; a < total; ++a)
+            if (tab[a] != 0) cn.bits[a >> 5] |= 1u << (a & 31);
+    } else {
+        if (k > kMaxPaletteRegs)
+            throw Error("node " + name + " has a multi-valued rate over " + std::to_string(k) + " nodes (limit " +
+                        std::to_string(kMaxPaletteRegs) + ")");
+        std::set<double> all(tab.begin(), tab.end());
+        if (all.size() > 256) throw Error("node " + name + " has more than 256 distinct rates");
+        cn.kind = NODE_PALETTE;
+        cn.up = cn.down = 0;
+        cn.up_real = cn.down_real = 0;
+        cn.palette_real.assign(all.begin(), all.end());
+        for (double r : cn.palette_real) cn.palette.push_back(quantize_rate(r, fb));
+        cn.pidx.resize(total);
+        for (uint64_t a = 0; a < total; ++a)
+            cn.pidx[a] = (uint8_t)(std::lower_bound(cn.palette_real.begin(), cn.palette_real.end(), tab[a]) -
+                                   cn.palette_real.begin());
+    }
+}
+
+// The node's rate per assignment, in double, rebuilt from its compiled form.
+static std::vector<double> node_table(const CompiledNode& cn) {
+    const int k = (int)cn.regs.size();
+    const uint64_t half = 1ull << k, total = half << 1;
+    std::vector<double> tab(total, 0.0);
+    for (uint64_t a = 0; a < total; ++a) {
+        if (cn.kind == NODE_BINARY) {
+            if ((cn.bits[a >> 5] >> (a & 31)) & 1u) tab[a] = a < half ? cn.up_real : cn.down_real;
+        } else {
+            tab[a] = cn.palette_real[cn.pidx[a]];
+        }
+    }
+    return tab;
+}
+
+static double node_max_rate(const CompiledNode& cn) {
+    if (cn.kind == NODE_PALETTE) return cn.palette_real.empty() ? 0.0 : cn.palette_real.back();
+    const int k = (int)cn.regs.size();
+    const uint64_t half = 1ull << k, total = half << 1;
+    bool any_up = false, any_down = false;
+    for (uint64_t a = 0; a < total; ++a)
+        if ((cn.bits[a >> 5] >> (a & 31)) & 1u) (a < half ? any_up : any_down) = true;
+    return std::max(any_up ? cn.up_real : 0.0, any_down ? cn.down_real : 0.0);
+}
+
+CompiledModel mutate_model(const CompiledModel& src, const int* nodes, const int* values, int count) {
+    CompiledModel cm = src;
+    std::vector<int> value(cm.n, -1);
+    for (int j = 0; j < count; ++j) {
+        if (nodes[j] < 0 || nodes[j] >= cm.n) throw Error("mutant node index out of range");
+        if (values[j] != 0 && values[j] != 1) throw Error("mutant value must be 0 (OFF) or 1 (ON)");
+        value[nodes[j]] = values[j];
+    }
+    std::vector<std::vector<double>> tabs(cm.n);
+    double sum_max = 0;
+    for (int i = 0; i < cm.n; ++i) {
+        CompiledNode& cn = cm.nodes[i];
+        if (value[i] < 0) {
+            sum_max += node_max_rate(cn);
+            continue;
+        }
+        // the node leaves `value` at rate 0: assignments whose self bit equals the value
+        tabs[i] = node_table(cn);
+        const int k = (int)cn.regs.size();
+        const uint64_t half = 1ull << k, total = half << 1;
+        for (uint64_t a = value[i] ? half : 0; a < (value[i] ? total : half); ++a) tabs[i][a] = 0.0;
+        double mx = 0;
+        for (double r : tabs[i]) mx = std::max(mx, r);
+        sum_max += mx;
+        cm.istate[i] = value[i];
+        cm.istate_thr[i] = value[i] ? 16777216u : 0u;
+    }
+    cm.frac_bits = frac_bits_for(sum_max);
+    for (int i = 0; i < cm.n; ++i) {
+        CompiledNode& cn = cm.nodes[i];
+        if (value[i] >= 0) {
+            classify_node(cn, tabs[i], cm.frac_bits, "#" + std::to_string(i));
+        } else if (cn.kind == NODE_BINARY) {
+            cn.up = quantize_rate(cn.up_real, cm.frac_bits);
+            cn.down = quantize_rate(cn.down_real, cm.frac_bits);
+        } else {
+            for (size_t q = 0; q < cn.palette.size(); ++q) cn.palette[q] = quantize_rate(cn.palette_real[q], cm.frac_bits);
+        }
+    }
+    return cm;
+}
+
 CompiledModel rescale_model(const CompiledModel& src, const double* up_scale, const double* down_scale) {
     CompiledModel cm = src;
     double sum_max = 0;
@@ -352,38 +459,7 @@ CompiledModel compile_model(const Model& m) {
     const int fb = frac_bits_for(sum_max);
     cm.frac_bits = fb;
 
-    for (int i = 0; i < cm.n; ++i) {
-        CompiledNode& cn = cm.nodes[i];
-        const int k = (int)cn.regs.size();
-        const uint64_t half = 1ull << k, total = half << 1;
-        const std::vector<double>& tab = tabs[i];
-        std::set<double> upv, dnv;
-        for (uint64_t a = 0; a < total; ++a)
-            if (tab[a] != 0) (a < half ? upv : dnv).insert(tab[a]);
-        if (upv.size() <= 1 && dnv.size() <= 1) {
-            cn.kind = NODE_BINARY;
-            cn.up_real = upv.empty() ? 0 : *upv.begin();
-            cn.down_real = dnv.empty() ? 0 : *dnv.begin();
-            cn.up = quantize_rate(cn.up_real, fb);
-            cn.down = quantize_rate(cn.down_real, fb);
-            cn.bits.assign((total + 31) / 32, 0u);
-            for (uint64_t a = 0; a < total; ++a)
-                if (tab[a] != 0) cn.bits[a >> 5] |= 1u << (a & 31);
-        } else {
-            if (k > kMaxPaletteRegs)
-                throw Error("node " + m.nodes[i].name + " has a multi-valued rate over " + std::to_string(k) +
-                            " nodes (limit " + std::to_string(kMaxPaletteRegs) + ")");
-            std::set<double> all(tab.begin(), tab.end());
-            if (all.size() > 256) throw Error("node " + m.nodes[i].name + " has more than 256 distinct rates");
-            cn.kind = NODE_PALETTE;
-            cn.palette_real.assign(all.begin(), all.end());
-            for (double r : cn.palette_real) cn.palette.push_back(quantize_rate(r, fb));
-            cn.pidx.resize(total);
-            for (uint64_t a = 0; a < total; ++a)
-                cn.pidx[a] = (uint8_t)(std::lower_bound(cn.palette_real.begin(), cn.palette_real.end(), tab[a]) -
-                                       cn.palette_real.begin());
-        }
-    }
+    for (int i = 0; i < cm.n; ++i) classify_node(cm.nodes[i], tabs[i], fb, m.nodes[i].name);
 
     cm.deps.assign(cm.n, {});
     for (int i = 0; i < cm.n; ++i) {

@@ -116,6 +116,11 @@ CompiledModel compile_model(const Model& m);
 // Copy of cm with node i's up rates times up_scale[i] and down rates times down_scale[i] (null:
 // 1), fixed-point scale and quantisation redone by compile_model's rule. Throws for palette nodes.
 CompiledModel rescale_model(const CompiledModel& cm, const double* up_scale, const double* down_scale);
+// Copy of cm with node nodes[j] clamped to values[j] (1 ON, 0 OFF): its initial state is the value
+// and its rate is zero wherever it holds the value. The fixed-point scale and the compiled form of
+// every node are what compile_model gives for the model whose clamped nodes have `istate` the value
+// and the opposite rate (rate_down for ON, rate_up for OFF) equal to 0.
+CompiledModel mutate_model(const CompiledModel& cm, const int* nodes, const int* values, int count);
 uint64_t quantize_rate(double r, int frac_bits);  // round-to-nearest, throws on overflow
 
 }  // namespace mbg

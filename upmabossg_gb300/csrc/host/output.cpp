@@ -1,6 +1,9 @@
 // Result formats of the reference, byte for byte in layout:
 //   <prefix>_probtraj.csv   src/statistics/window_average_small.cpp:181-250
 //   <prefix>_fp.csv         src/statistics/fixed_states.cu:154-187
+//   <prefix>_final_states.csv  (no reference file: the reference prints its final-state
+//                           histogram, final_states.cpp:53-66, only to stdout and leaves
+//                           final_states::write_csv empty, final_states.cpp:68)
 //   stdout report           final_states.cpp:53-66, fixed_states.cu:139-152,
 //                           window_average_small.cpp:142-179, in the order of main.cpp:65-74
 // Probabilities are computed in double from the exact fixed-point sums and printed through
@@ -110,6 +113,28 @@ void write_fp_csv(const Sim& s, const std::string& path) {
         for (int i = 0; i < s.cm.n; ++i) ofs << "\t" << ((f.words[i >> 5] >> (i & 31)) & 1u);
         ofs << "\n";
         ++i_fp;
+    }
+    if (!ofs) throw IoError("error writing " + path);
+}
+
+// Final-state histogram in the layout of the fixed-point file: a count line, a header naming the
+// output nodes, then one row per reached output state in increasing index order with its share of
+// the trajectories and one 0/1 column per output node.
+void write_final_states_csv(const Sim& s, const std::string& path) {
+    std::ofstream ofs(path);
+    if (!ofs) throw IoError("cannot write " + path);
+    const size_t S = (size_t)1 << s.cm.n_out;
+    size_t reached = 0;
+    for (size_t x = 0; x < S; ++x) reached += s.fin[x] != 0;
+    ofs << "Final States (" << reached << ")\n";
+    ofs << "Proba\tState";
+    for (int q = 0; q < s.cm.n_out; ++q) ofs << "\t" << s.names[s.cm.out_nodes[q]];
+    ofs << "\n";
+    for (size_t x = 0; x < S; ++x) {
+        if (s.fin[x] == 0) continue;
+        ofs << (float)((double)s.fin[x] / (double)s.n_traj) << "\t" << out_state_string(s, (uint32_t)x);
+        for (int q = 0; q < s.cm.n_out; ++q) ofs << "\t" << ((x >> q) & 1u);
+        ofs << "\n";
     }
     if (!ofs) throw IoError("error writing " + path);
 }

@@ -61,6 +61,7 @@ public:
 // Output formats (output.cpp).
 void write_probtraj_csv(const Sim& s, const std::string& path);
 void write_fp_csv(const Sim& s, const std::string& path);
+void write_final_states_csv(const Sim& s, const std::string& path);
 void print_results(const Sim& s, std::ostream& os);
 double window_prob(const Sim& s, size_t idx);
 double window_th(const Sim& s, int w);
