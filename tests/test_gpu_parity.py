@@ -76,6 +76,42 @@ def test_mid_network_parity(layout):
     compare_histograms(model, sim, orc, 400)
 
 
+def wide_network(n=72, seed=5):
+    """Two-valued nodes over every regulator count from 0 to 14: table and regulators in the lane
+    record (k <= 4), in its 32-byte side entry with the table inline (k = 5, 6) or in the shared
+    table array (k = 7..12), and in the general node records (k > 12)."""
+    rng = np.random.default_rng(seed)
+    names = [f"W{i}" for i in range(n)]
+    lines = []
+    for i, nm in enumerate(names):
+        k = i % 15
+        regs = list(rng.choice([x for x in names if x != nm], size=k, replace=False))
+        if k == 0:
+            logic = "1" if i % 2 else "0"
+        else:
+            logic = regs[0]
+            for j, r in enumerate(regs[1:]):
+                op = (" & ", " | ", " ^ ")[int(rng.integers(0, 3))]
+                logic = f"({logic}{op}{'!' if j % 3 == 1 else ''}{r})"
+        u = float(np.round(rng.lognormal(0.0, 0.5), 4))
+        d = float(np.round(rng.lognormal(0.0, 0.5), 4))
+        lines.append(f"Node {nm} {{ logic = {logic}; rate_up = @logic ? {u} : 0; rate_down = @logic ? 0 : {d}; }}\n")
+    out = set(rng.choice(names, size=8, replace=False))
+    cfg = "".join(f"{nm}.is_internal = {0 if nm in out else 1};\n" for nm in names)
+    cfg += "max_time = 10;\ntime_tick = 0.5;\nsample_count = 3000;\nseed_pseudorandom = 17;\n"
+    return "".join(lines), cfg
+
+
+@pytest.mark.parametrize("layout", ALL_LAYOUTS)
+def test_wide_node_parity(layout):
+    bnd, cfg = wide_network()
+    model, sim = run_device(bnd, cfg, 3000, **layout_kw(layout))
+    assert model.info.max_regulators == 14
+    orc = run_oracle(bnd, cfg, model, 3000)
+    compare_trajectories(sim, orc)
+    compare_histograms(model, sim, orc, 3000)
+
+
 @pytest.mark.parametrize("layout", [mbg.LAYOUT_WARP, mbg.LAYOUT_LANE])
 def test_large_network_parity(layout):
     net = synth.large()

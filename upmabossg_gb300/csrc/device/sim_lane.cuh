@@ -104,14 +104,37 @@ __device__ __forceinline__ unsigned lane_idx4(const unsigned* st, int T, int k, 
     return idx;
 }
 
+// Table bit of a two-valued node over 5..12 regulators (kLaneWideTable): regulators 0..3 from its
+// LaneNode's second half rb, the rest and the table (inline up to 6 regulators) from its LaneWide
+// entry.
+__device__ __forceinline__ unsigned lane_wide_bit(const SimParams& p, uint4 rb, int k, unsigned self,
+                                                  const unsigned* st, int T) {
+    const uint4* w = reinterpret_cast<const uint4*>(p.lwide + rb.x);
+    const uint4 w0 = __ldg(w), w1 = __ldg(w + 1);
+    unsigned idx = lane_idx4(st, T, 4, rb.y, rb.z) | (lane_idx4(st, T, min(k - 4, 4), w0.x, w0.y) << 4);
+    if (k > 8) idx |= lane_idx4(st, T, k - 8, w0.z, w0.w) << 8;
+    const unsigned a = (self << k) | idx;
+    unsigned word;
+    if (k <= 6) {
+        const unsigned q = a >> 5;
+        word = q == 0u ? w1.x : q == 1u ? w1.y : q == 2u ? w1.z : w1.w;
+    } else {
+        word = __ldg(p.tabs + w1.x + (a >> 5));
+    }
+    return (word >> (a & 31u)) & 1u;
+}
+
 // Rate of node i in the state column st, evaluated from its tables.
 __device__ __forceinline__ unsigned long long lane_eval(const SimParams& p, int i, const unsigned* st, int T) {
     const uint4* rec = reinterpret_cast<const uint4*>(p.lnodes + i);
     const uint4 ra = __ldg(rec), rb = __ldg(rec + 1);
     const unsigned self = col_bit(st, T, i);
-    if ((rb.w >> 16) == 0u) {
+    const unsigned flags = rb.w >> 16;
+    if (flags == 0u || flags == kLaneWideTable) {
         const int k = (int)(rb.w & 0xffffu);
-        if (!((rb.x >> ((self << k) | lane_idx4(st, T, k, rb.y, rb.z))) & 1u)) return 0ull;
+        const unsigned on = flags == 0u ? (rb.x >> ((self << k) | lane_idx4(st, T, k, rb.y, rb.z))) & 1u
+                                        : lane_wide_bit(p, rb, k, self, st, T);
+        if (!on) return 0ull;
         return self ? (((unsigned long long)ra.w << 32) | ra.z) : (((unsigned long long)ra.y << 32) | ra.x);
     }
     const NodeHead h = load_head(p, i);
@@ -214,6 +237,27 @@ __device__ __forceinline__ int lane_pick(const SimParams& p, const unsigned* st,
     if (g >= G) return -1;
     unsigned aw = act[g * T];
     const unsigned sw = st[g * T];
+    if (!p.has_palette) {
+        // the next four active nodes' rates are loaded together, then compared in node order
+        const unsigned long long* rates = &p.lnodes[g * 32].up;  // 4 words per LaneNode
+        while (aw) {
+            int b[4];
+            unsigned long long v[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                b[u] = aw ? __ffs(aw) - 1 : -1;
+                aw &= aw - 1u;
+                v[u] = b[u] >= 0 ? __ldg(rates + 4 * b[u] + ((sw >> (b[u] & 31)) & 1u)) : 0ull;
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                if (b[u] < 0) return -1;
+                if (r < v[u]) return g * 32 + b[u];
+                r -= v[u];
+            }
+        }
+        return -1;
+    }
     while (aw) {
         const int b = __ffs(aw) - 1;
         aw &= aw - 1u;
@@ -247,6 +291,8 @@ __device__ __forceinline__ unsigned long long lane_reader_rec(const SimParams& p
         if (flags == 0u) {
             // up to 4 regulators and their table in the record itself
             a_new = (rb.x >> ((self << kd) | lane_idx4(st, T, kd, rb.y, rb.z))) & 1u;
+        } else if (flags == kLaneWideTable) {
+            a_new = lane_wide_bit(p, rb, kd, self, st, T);
         } else {
             a_new = table_bit(p, dn, kd, self, lane_gather(p, dn, kd, st, T));
         }

@@ -48,22 +48,29 @@ struct DevNode {
 };
 
 // The lane layout's per-node record, 32 bytes (one sector): everything a step reads about a
-// node whose rate is a two-valued table over at most 4 regulators. Other nodes carry a flag and
-// are read from their DevNode.
-constexpr unsigned kLaneWideTable = 1u;  // more than 4 regulators: table and regulators in DevNode
+// node whose rate is a two-valued table over at most 4 regulators. A two-valued node over 5..12
+// regulators adds one 32-byte LaneWide entry; other nodes carry a flag and are read from their
+// DevNode.
+constexpr unsigned kLaneWideTable = 1u;  // 5..12 regulators: `table` indexes the LaneWide entries
 constexpr unsigned kLanePalette = 2u;    // multi-valued rate: DevNode palette path
+constexpr unsigned kLaneFar = 4u;        // more than 12 regulators: table and regulators in DevNode
 struct LaneNode {
     unsigned long long up, down;  // fixed-point rates (BINARY)
-    unsigned int table;           // k <= 4: the 2^(k+1) table bits
+    unsigned int table;           // k <= 4: the 2^(k+1) table bits; kLaneWideTable: LaneWide index
     unsigned short r[4];          // the first min(k, 4) regulators
     unsigned short k;             // number of regulators
-    unsigned short flags;         // kLaneWideTable | kLanePalette
+    unsigned short flags;         // kLaneWideTable | kLanePalette | kLaneFar
+};
+struct LaneWide {
+    unsigned short r[8];  // regulators 4 .. k-1
+    unsigned int table[4];  // k <= 6: the 2^(k+1) table bits; k > 6: table[0] = word offset into tabs
 };
 
 struct SimParams {
     // model
     const DevNode* nodes;
     const LaneNode* lnodes;
+    const LaneWide* lwide;
     const unsigned short* regs;
     const unsigned int* tabs;
     const unsigned char* pidx;

@@ -121,7 +121,7 @@ void Batch::create(const std::vector<const CompiledModel*>& models, const std::v
     std::vector<DeviceLayout> dls(n);
     Layout ml, rl, pl, fl;
     struct Off {
-        size_t nodes, lnodes, regs, tabs, pidx, palette, dep_off, deps, out_nodes, out_pos, istate;
+        size_t nodes, lnodes, lwide, regs, tabs, pidx, palette, dep_off, deps, out_nodes, out_pos, istate;
         size_t hist, th, fin, fp_count, slot_cnt, rep, fp_states, out_states, out_cnt;
     };
     std::vector<Off> off(n);
@@ -134,6 +134,7 @@ void Batch::create(const std::vector<const CompiledModel*>& models, const std::v
         Off& f = off[i];
         f.nodes = ml.add(d.nodes.size() * sizeof(DevNode));
         f.lnodes = ml.add(d.lnodes.size() * sizeof(LaneNode));
+        f.lwide = ml.add(d.lwide.size() * sizeof(LaneWide));
         f.regs = ml.add(d.regs.size() * 2);
         f.tabs = ml.add(d.tabs.size() * 4);
         f.pidx = ml.add(d.pidx.size());
@@ -170,6 +171,7 @@ void Batch::create(const std::vector<const CompiledModel*>& models, const std::v
         const Off& f = off[i];
         put(f.nodes, d.nodes.data(), d.nodes.size() * sizeof(DevNode));
         put(f.lnodes, d.lnodes.data(), d.lnodes.size() * sizeof(LaneNode));
+        put(f.lwide, d.lwide.data(), d.lwide.size() * sizeof(LaneWide));
         put(f.regs, d.regs.data(), d.regs.size() * 2);
         put(f.tabs, d.tabs.data(), d.tabs.size() * 4);
         put(f.pidx, d.pidx.data(), d.pidx.size());
@@ -202,6 +204,7 @@ void Batch::create(const std::vector<const CompiledModel*>& models, const std::v
         std::memset(&p, 0, sizeof p);
         p.nodes = reinterpret_cast<const DevNode*>(model_arena + f.nodes);
         p.lnodes = reinterpret_cast<const LaneNode*>(model_arena + f.lnodes);
+        p.lwide = reinterpret_cast<const LaneWide*>(model_arena + f.lwide);
         p.regs = reinterpret_cast<const unsigned short*>(model_arena + f.regs);
         p.tabs = reinterpret_cast<const unsigned*>(model_arena + f.tabs);
         p.pidx = reinterpret_cast<const unsigned char*>(model_arena + f.pidx);

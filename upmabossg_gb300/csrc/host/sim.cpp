@@ -91,9 +91,24 @@ DeviceLayout layout_model(const CompiledModel& cm) {
         ln.down = dn.down;
         ln.k = dn.k;
         for (size_t j = 0; j < cn.regs.size() && j < 4; ++j) ln.r[j] = (uint16_t)cn.regs[j];
-        if (cn.kind != NODE_BINARY) ln.flags = kLanePalette;
-        else if (cn.regs.size() > 4) ln.flags = kLaneWideTable;
-        else ln.table = cn.bits[0];
+        if (cn.kind != NODE_BINARY) {
+            ln.flags = kLanePalette;
+        } else if (cn.regs.size() > 12) {
+            ln.flags = kLaneFar;
+        } else if (cn.regs.size() > 4) {
+            LaneWide w;
+            std::memset(&w, 0, sizeof w);
+            for (size_t j = 4; j < cn.regs.size(); ++j) w.r[j - 4] = (uint16_t)cn.regs[j];
+            if (cn.regs.size() <= 6)
+                for (size_t q = 0; q < cn.bits.size() && q < 4; ++q) w.table[q] = cn.bits[q];
+            else
+                w.table[0] = dn.tab_off;
+            ln.flags = kLaneWideTable;
+            ln.table = (uint32_t)d.lwide.size();
+            d.lwide.push_back(w);
+        } else {
+            ln.table = cn.bits[0];
+        }
         d.lnodes.push_back(ln);
     }
     d.dep_off.push_back(0);
@@ -176,6 +191,7 @@ void Sim::create(const CompiledModel& model, const std::vector<std::string>& nod
     std::memset(&prm, 0, sizeof prm);
     prm.nodes = upload(dl.nodes, owned);
     prm.lnodes = upload(dl.lnodes, owned);
+    prm.lwide = upload(dl.lwide, owned);
     prm.regs = upload(dl.regs, owned);
     prm.tabs = upload(dl.tabs, owned);
     prm.pidx = upload(dl.pidx, owned);

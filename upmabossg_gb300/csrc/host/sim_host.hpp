@@ -24,6 +24,7 @@ struct IoError : Error { using Error::Error; };
 struct DeviceLayout {
     std::vector<DevNode> nodes;
     std::vector<LaneNode> lnodes;
+    std::vector<LaneWide> lwide;
     std::vector<uint16_t> regs;
     std::vector<uint32_t> tabs;
     std::vector<uint8_t> pidx;
