@@ -271,7 +271,8 @@ __device__ __forceinline__ int lane_pick(const SimParams& p, const unsigned* st,
 }
 
 // Re-evaluates reader dn of a node that just flipped, in the trajectory whose entries start at
-// `col`: dependency entry e = (dn << 16) | (k_dn << 8) | pos (pos 0xFF: dn itself flipped).
+// `col`: dependency entry e = (dn << 16) | (out << 15) | (k_dn << 8) | pos (pos 0xFF: dn itself
+// flipped).
 // Patches the active bits and the Fenwick tree (with shared-memory atomics when several lanes may
 // patch the same trajectory), returns the rate change and sets `out` when dn is an output node
 // whose rate changed.
@@ -279,7 +280,7 @@ template <bool ATOMIC>
 __device__ __forceinline__ unsigned long long lane_reader_rec(const SimParams& p, unsigned e, uint4 ra, uint4 rb,
                                                               const LaneSmem& m, int T, int col, bool& out) {
     const int dn = (int)(e >> 16);
-    const int kd = (int)((e >> 8) & 0xffu);
+    const int kd = (int)((e >> 8) & 0x7fu);
     const unsigned pos = e & 0xffu;
     const unsigned* st = m.st + col;
     const unsigned self = col_bit(st, T, dn);
@@ -322,7 +323,7 @@ __device__ __forceinline__ unsigned long long lane_reader_rec(const SimParams& p
         const int G = lane_groups(p.n);
         if (ATOMIC) fen_add_atomic(m.fen + col, T, G, g, delta);
         else fen_add(m.fen + col, T, G, g, delta);
-        out |= __ldg(p.out_pos + dn) >= 0;
+        out |= ((e >> 15) & 1u) != 0u;
     }
     return delta;
 }
@@ -480,7 +481,9 @@ __device__ __forceinline__ int lane_step_front(const SimParams& p, const LaneSme
     }
     const int G = lane_groups(p.n);
     unsigned* st = m.st + col;
-    const int k = lane_pick(p, st, m.act + col, m.fen + col, T, G, 1 << (31 - __clz(G)),
+    // the tree's root (G a power of two) holds the total, which r never reaches: start below it
+    const int top = 1 << (31 - __clz(G));
+    const int k = lane_pick(p, st, m.act + col, m.fen + col, T, G, top == G ? top >> 1 : top,
                             pick_target(d.y, d.z, tr.total));
     if (k < 0 || k >= p.n) {
         tr.status = TRAJ_ERROR;

@@ -76,8 +76,9 @@ struct SimParams {
     const unsigned char* pidx;
     const unsigned long long* palette;
     const unsigned int* dep_off;  // n + 1
-    // For node k: every node d whose rate reads k, plus k itself, as (d << 16) | (k_d << 8) | pos,
-    // k_d = number of regulators of d, pos = position of k among them (0xFF for d == k).
+    // For node k: every node d whose rate reads k, plus k itself, as
+    // (d << 16) | (out_d << 15) | (k_d << 8) | pos: out_d = d is an output node, k_d = number of
+    // regulators of d (< 128), pos = position of k among them (0xFF for d == k).
     const unsigned int* deps;
     const unsigned short* out_nodes;  // n_out
     const short* out_pos;             // n: position among outputs or -1

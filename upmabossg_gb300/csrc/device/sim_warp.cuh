@@ -343,7 +343,7 @@ __device__ unsigned char warp_trajectory(const SimParams& p, const WarpSmem& m, 
             if (q < d1) {
                 const unsigned e = __ldg(p.deps + q);
                 dn = (int)(e >> 16);
-                const int kd = (int)((e >> 8) & 0xffu);
+                const int kd = (int)((e >> 8) & 0x7fu);
                 const unsigned pos = e & 0xffu;
                 const unsigned self = st_bit(m.st, dn);
                 const unsigned self_old = pos == 0xffu ? self ^ 1u : self;
@@ -380,7 +380,7 @@ __device__ unsigned char warp_trajectory(const SimParams& p, const WarpSmem& m, 
                 delta = r_new - r_old;
                 if (delta != 0ull) {
                     if (two_level) atomicAdd(m.l1 + (dn >> 5), delta);
-                    out_touched |= __ldg(p.out_pos + dn) >= 0;
+                    out_touched |= ((e >> 15) & 1u) != 0u;
                 }
             }
             // broadcast each change into the register prefix

@@ -118,7 +118,8 @@ DeviceLayout layout_model(const CompiledModel& cm) {
             uint32_t pos = 0xFF;
             for (size_t j = 0; j < regs.size(); ++j)
                 if (regs[j] == i) pos = (uint32_t)j;
-            d.deps.push_back(((uint32_t)x << 16) | ((uint32_t)regs.size() << 8) | pos);
+            const uint32_t out = cm.out_pos[x] >= 0 ? 1u : 0u;
+            d.deps.push_back(((uint32_t)x << 16) | (out << 15) | ((uint32_t)regs.size() << 8) | pos);
         }
         d.dep_off.push_back((uint32_t)d.deps.size());
     }
