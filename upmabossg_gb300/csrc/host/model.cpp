@@ -29,9 +29,13 @@ Model::Model() {
 }
 
 int Model::node_index(const std::string& name) const {
-    for (size_t i = 0; i < nodes.size(); ++i)
-        if (nodes[i].name == name) return (int)i;
-    return -1;
+    auto it = index.find(name);
+    return it == index.end() ? -1 : it->second;
+}
+
+void Model::add_node(Node&& n) {
+    index.emplace(n.name, (int)nodes.size());
+    nodes.push_back(std::move(n));
 }
 
 double Model::constant(const std::string& n) const {
@@ -210,13 +214,34 @@ void run_block(const std::vector<Instr>& prog, uint64_t a0, std::vector<double>&
             }
             case Instr::Un: {
                 double* d = &stack[(sp - 1) * kBlock];
-                for (int t = 0; t < kBlock; ++t) d[t] = apply_unary(in.op, d[t]);
+                switch (in.op) {
+                    case Op::Plus: break;
+                    case Op::Minus: for (int t = 0; t < kBlock; ++t) d[t] = -d[t]; break;
+                    case Op::Not: for (int t = 0; t < kBlock; ++t) d[t] = d[t] == 0 ? 1.0 : 0.0; break;
+                    default: for (int t = 0; t < kBlock; ++t) d[t] = apply_unary(in.op, d[t]); break;
+                }
                 break;
             }
             case Instr::Bin: {
+                // one loop per operator (apply_binary's rules), so that each loop vectorises
                 double* l = &stack[(sp - 2) * kBlock];
-                double* r = &stack[(sp - 1) * kBlock];
-                for (int t = 0; t < kBlock; ++t) l[t] = apply_binary(in.op, l[t], r[t]);
+                const double* r = &stack[(sp - 1) * kBlock];
+                switch (in.op) {
+                    case Op::Plus: for (int t = 0; t < kBlock; ++t) l[t] = l[t] + r[t]; break;
+                    case Op::Minus: for (int t = 0; t < kBlock; ++t) l[t] = l[t] - r[t]; break;
+                    case Op::Star: for (int t = 0; t < kBlock; ++t) l[t] = l[t] * r[t]; break;
+                    case Op::Slash: for (int t = 0; t < kBlock; ++t) l[t] = l[t] / r[t]; break;
+                    case Op::And: for (int t = 0; t < kBlock; ++t) l[t] = (l[t] != 0 && r[t] != 0) ? 1.0 : 0.0; break;
+                    case Op::Or: for (int t = 0; t < kBlock; ++t) l[t] = (l[t] != 0 || r[t] != 0) ? 1.0 : 0.0; break;
+                    case Op::Xor: for (int t = 0; t < kBlock; ++t) l[t] = ((l[t] != 0) != (r[t] != 0)) ? 1.0 : 0.0; break;
+                    case Op::Eq: for (int t = 0; t < kBlock; ++t) l[t] = l[t] == r[t] ? 1.0 : 0.0; break;
+                    case Op::Ne: for (int t = 0; t < kBlock; ++t) l[t] = l[t] != r[t] ? 1.0 : 0.0; break;
+                    case Op::Le: for (int t = 0; t < kBlock; ++t) l[t] = l[t] <= r[t] ? 1.0 : 0.0; break;
+                    case Op::Lt: for (int t = 0; t < kBlock; ++t) l[t] = l[t] < r[t] ? 1.0 : 0.0; break;
+                    case Op::Ge: for (int t = 0; t < kBlock; ++t) l[t] = l[t] >= r[t] ? 1.0 : 0.0; break;
+                    case Op::Gt: for (int t = 0; t < kBlock; ++t) l[t] = l[t] > r[t] ? 1.0 : 0.0; break;
+                    default: for (int t = 0; t < kBlock; ++t) l[t] = apply_binary(in.op, l[t], r[t]); break;
+                }
                 --sp;
                 break;
             }
@@ -231,6 +256,139 @@ void run_block(const std::vector<Instr>& prog, uint64_t a0, std::vector<double>&
         }
     }
     std::memcpy(out, stack.data(), sizeof(double) * kBlock);
+}
+
+// The same evaluation, bit-sliced where it can be: a stack entry is a scalar constant, a 64-bit
+// mask (a 0/1 value per assignment: node bits, logical operators and comparisons of 0/1 values)
+// or a vector of 64 doubles (arithmetic). Logical operators and comparisons always give 0.0 or
+// 1.0, so masks stand for exactly the doubles run_block would hold; arithmetic and comparisons
+// that need real values expand their operands to vectors and use run_block's rules. Results are
+// identical to run_block's; the usual `@logic ? rate : 0` forms never leave masks and scalars.
+struct Slot {
+    enum Kind { Scalar, Mask, Vec } kind;
+    double c;
+    uint64_t m;
+    double* v;
+};
+
+uint64_t bit_pattern(uint64_t a0, int bit) {
+    static const uint64_t low[6] = {0xAAAAAAAAAAAAAAAAull, 0xCCCCCCCCCCCCCCCCull, 0xF0F0F0F0F0F0F0F0ull,
+                                    0xFF00FF00FF00FF00ull, 0xFFFF0000FFFF0000ull, 0xFFFFFFFF00000000ull};
+    if (bit < 6) return low[bit];
+    return ((a0 >> bit) & 1u) ? ~0ull : 0ull;
+}
+
+uint64_t as_mask(const Slot& s) {  // truthiness per assignment
+    if (s.kind == Slot::Mask) return s.m;
+    if (s.kind == Slot::Scalar) return s.c != 0 ? ~0ull : 0ull;
+    uint64_t m = 0;
+    for (int t = 0; t < kBlock; ++t) m |= (uint64_t)(s.v[t] != 0) << t;
+    return m;
+}
+
+void as_vec(const Slot& s, double* out) {
+    if (s.kind == Slot::Vec) {
+        if (s.v != out) std::memcpy(out, s.v, sizeof(double) * kBlock);
+    } else if (s.kind == Slot::Scalar) {
+        for (int t = 0; t < kBlock; ++t) out[t] = s.c;
+    } else {
+        for (int t = 0; t < kBlock; ++t) out[t] = (double)((s.m >> t) & 1u);
+    }
+}
+
+uint64_t compare_masks(Op op, uint64_t a, uint64_t b) {
+    switch (op) {
+        case Op::Eq: return ~(a ^ b);
+        case Op::Ne: return a ^ b;
+        case Op::Lt: return ~a & b;
+        case Op::Le: return ~a | b;
+        case Op::Gt: return a & ~b;
+        default: return a | ~b;  // Ge
+    }
+}
+
+bool is_compare(Op op) {
+    return op == Op::Eq || op == Op::Ne || op == Op::Lt || op == Op::Le || op == Op::Gt || op == Op::Ge;
+}
+
+void run_block_bits(const std::vector<Instr>& prog, uint64_t a0, std::vector<double>& store, std::vector<Slot>& st,
+                    double* out) {
+    size_t sp = 0;
+    auto vec_at = [&](size_t i) { return &store[i * kBlock]; };
+    for (const Instr& in : prog) {
+        switch (in.code) {
+            case Instr::Const: st[sp++] = Slot{Slot::Scalar, in.c, 0, nullptr}; break;
+            case Instr::Bit: st[sp++] = Slot{Slot::Mask, 0, bit_pattern(a0, in.bit), nullptr}; break;
+            case Instr::Un: {
+                Slot& x = st[sp - 1];
+                if (in.op == Op::Plus) break;
+                if (x.kind == Slot::Scalar) {
+                    x.c = apply_unary(in.op, x.c);
+                } else if (in.op == Op::Not) {
+                    x = Slot{Slot::Mask, 0, ~as_mask(x), nullptr};
+                } else {
+                    double* d = vec_at(sp - 1);
+                    as_vec(x, d);
+                    for (int t = 0; t < kBlock; ++t) d[t] = apply_unary(in.op, d[t]);
+                    x = Slot{Slot::Vec, 0, 0, d};
+                }
+                break;
+            }
+            case Instr::Bin: {
+                Slot& l = st[sp - 2];
+                const Slot r = st[sp - 1];
+                --sp;
+                if (l.kind == Slot::Scalar && r.kind == Slot::Scalar) {
+                    l.c = apply_binary(in.op, l.c, r.c);
+                } else if (in.op == Op::And || in.op == Op::Or || in.op == Op::Xor) {
+                    const uint64_t a = as_mask(l), b = as_mask(r);
+                    l = Slot{Slot::Mask, 0, in.op == Op::And ? (a & b) : in.op == Op::Or ? (a | b) : (a ^ b), nullptr};
+                } else if (is_compare(in.op) && l.kind == Slot::Mask && r.kind == Slot::Mask) {
+                    l = Slot{Slot::Mask, 0, compare_masks(in.op, l.m, r.m), nullptr};
+                } else {
+                    double* dl = vec_at(sp - 1);
+                    double rv[kBlock];
+                    as_vec(l, dl);
+                    as_vec(r, rv);
+                    if (is_compare(in.op)) {
+                        uint64_t m = 0;
+                        for (int t = 0; t < kBlock; ++t) m |= (uint64_t)(apply_binary(in.op, dl[t], rv[t]) != 0) << t;
+                        l = Slot{Slot::Mask, 0, m, nullptr};
+                    } else {
+                        for (int t = 0; t < kBlock; ++t) dl[t] = apply_binary(in.op, dl[t], rv[t]);
+                        l = Slot{Slot::Vec, 0, 0, dl};
+                    }
+                }
+                break;
+            }
+            case Instr::Tern: {
+                const uint64_t c = as_mask(st[sp - 3]);
+                const Slot x = st[sp - 2], y = st[sp - 1];
+                sp -= 2;
+                if (c == ~0ull) {
+                    st[sp - 1] = x;
+                } else if (c == 0) {
+                    st[sp - 1] = y;
+                } else if (x.kind == Slot::Scalar && y.kind == Slot::Scalar && x.c == 1.0 && y.c == 0.0) {
+                    st[sp - 1] = Slot{Slot::Mask, 0, c, nullptr};
+                } else {
+                    double xv[kBlock], yv[kBlock];
+                    as_vec(x, xv);
+                    as_vec(y, yv);
+                    double* d = vec_at(sp - 1);
+                    for (int t = 0; t < kBlock; ++t) d[t] = ((c >> t) & 1u) ? xv[t] : yv[t];
+                    st[sp - 1] = Slot{Slot::Vec, 0, 0, d};
+                }
+                if (st[sp - 1].kind == Slot::Vec && st[sp - 1].v != vec_at(sp - 1)) {
+                    // a branch's vector moved down the stack: keep it in its own slot's storage
+                    std::memcpy(vec_at(sp - 1), st[sp - 1].v, sizeof(double) * kBlock);
+                    st[sp - 1].v = vec_at(sp - 1);
+                }
+                break;
+            }
+        }
+    }
+    as_vec(st[0], out);
 }
 
 size_t stack_depth(const std::vector<Instr>& prog) {
@@ -431,20 +589,29 @@ CompiledModel compile_model(const Model& m) {
         std::vector<Instr> pu, pd;
         flatten(*up, m, i, inputs, pu, 0);
         flatten(*down, m, i, inputs, pd, 0);
-        std::vector<double> stack(kBlock * (std::max(stack_depth(pu), stack_depth(pd)) + 1));
+        const size_t depth = std::max(stack_depth(pu), stack_depth(pd)) + 1;
+        std::vector<double> stack(kBlock * depth);
+        std::vector<Slot> slots(depth);
         const uint64_t half = 1ull << k, total = half << 1;
         std::vector<double>& tab = tabs[i];
         tab.assign(std::max<uint64_t>(total, kBlock), 0.0);
         double buf[kBlock];
+        // assignments with the self bit (bit k) clear read rate_up, set read rate_down: rate_up
+        // runs over the lower half only, rate_down over the upper half only (a block never
+        // straddles the halves when half >= kBlock)
         for (uint64_t a0 = 0; a0 < total; a0 += kBlock) {
-            // assignments with the self bit (bit k) clear read rate_up, set read rate_down
-            uint64_t n_here = std::min<uint64_t>(kBlock, total - a0);
-            run_block(pu, a0, stack, buf);
-            for (uint64_t t = 0; t < n_here; ++t)
-                if (!(((a0 + t) >> k) & 1u)) tab[a0 + t] = buf[t];
-            run_block(pd, a0, stack, buf);
-            for (uint64_t t = 0; t < n_here; ++t)
-                if (((a0 + t) >> k) & 1u) tab[a0 + t] = buf[t];
+            const uint64_t n_here = std::min<uint64_t>(kBlock, total - a0);
+            const bool any_up = a0 < half, any_down = a0 + n_here > half;
+            if (any_up) {
+                run_block_bits(pu, a0, stack, slots, buf);
+                for (uint64_t t = 0; t < n_here; ++t)
+                    if (!(((a0 + t) >> k) & 1u)) tab[a0 + t] = buf[t];
+            }
+            if (any_down) {
+                run_block_bits(pd, a0, stack, slots, buf);
+                for (uint64_t t = 0; t < n_here; ++t)
+                    if (((a0 + t) >> k) & 1u) tab[a0 + t] = buf[t];
+            }
         }
         tab.resize(total);
         double mx = 0;

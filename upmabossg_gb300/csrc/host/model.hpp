@@ -15,6 +15,7 @@
 #include <memory>
 #include <stdexcept>
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 namespace mbg {
@@ -51,8 +52,11 @@ struct Model {
     std::map<std::string, double> variables;  // "$name" -> value
     std::map<std::string, double> constants;  // defaults from driver.cpp:9-13
 
+    std::unordered_map<std::string, int> index;  // node name -> position in `nodes`
+
     Model();
     int node_index(const std::string& name) const;  // -1 if unknown
+    void add_node(Node&& n);                          // appends and indexes
     bool is_internal(int i) const;                   // parse_types.cpp:20-23
     double constant(const std::string& n) const;
 };

@@ -312,7 +312,7 @@ private:
         if (!n.attr("rate_down"))
             lx_.fail(name.line, name.col, "Node " + name.text + " does not have rate_down attribute");
         if ((int)m_.nodes.size() >= kMaxNodes) lx_.fail(name.line, name.col, "too many nodes");
-        m_.nodes.push_back(std::move(n));
+        m_.add_node(std::move(n));
     }
 
     double guarded_eval(const Expr& e, const Token& at) {
