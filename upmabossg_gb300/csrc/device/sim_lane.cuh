@@ -4,16 +4,17 @@
 // The reference re-evaluates all N rates and scans them on every step
 // (src/jit_kernels/simulation.cu:9-21 and 77-164 with the generated compute_transition_rates of
 // src/generator.cpp:124-144). Here a lane keeps, for its trajectory:
-//   fen[G]  a Fenwick tree over the exact 64-bit fixed-point rate sums of the 32-node groups
-//           (G = W): entry i (1-based) holds the sum of groups (i - lowbit(i), i],
+//   fen[L]  a Fenwick tree over the exact 64-bit fixed-point rate sums of leaves of
+//           2^kLeafShift 32-node groups (L = ceil(W / 2^kLeafShift)): entry i (1-based) holds the
+//           sum of leaves (i - lowbit(i), i],
 //   st[W]   state words,
 //   act[W]  active words (bit i: node i's rate is non-zero),
 // in shared memory, in rows of blockDim.x entries (entry [row][thread]), so that the 32 lanes of a
 // warp always touch 32 distinct banks whatever rows they read. A step descends the tree to the
-// group holding the target (log2 G loads, the same count on every lane), then walks the active
-// nodes of that group in node order: the reference's first-prefix pick, exactly. A flip of node k
-// re-evaluates only the nodes whose rate reads k (the dependency CSR) and adds each rate change
-// along its group's tree path. A new trajectory is set up by the whole warp at once (one node per
+// leaf holding the target (log2 L loads, the same count on every lane), then walks the active
+// nodes of that leaf's groups in node order: the reference's first-prefix pick, exactly. A
+// flip of node k re-evaluates only the nodes whose rate reads k (the dependency CSR) and adds each
+// rate change along its leaf's tree path. A new trajectory is set up by the whole warp at once (one node per
 // lane), because that pass is O(N).
 // Includes nothing: sim_types.h, philox.h, sim_core.cuh and sim_warp.cuh come first.
 #pragma once
@@ -21,8 +22,16 @@
 namespace mbg {
 
 __host__ __device__ __forceinline__ int lane_groups(int n) { return (n + 31) >> 5; }
+// Fenwick leaves: 2^kLeafShift consecutive 32-node groups each. Wider leaves shrink the tree (and
+// a trajectory's shared memory: more resident trajectories per SM) but lengthen the walk.
+constexpr int kLeafShift = 1;
+__host__ __device__ __forceinline__ int lane_leaves(int groups) {
+    return (groups + (1 << kLeafShift) - 1) >> kLeafShift;
+}
 // Shared-memory bytes per thread (plus lane_block_extra per block).
-__host__ __device__ __forceinline__ unsigned lane_smem_bytes(int n) { return 16u * (unsigned)lane_groups(n); }
+__host__ __device__ __forceinline__ unsigned lane_smem_bytes(int n) {
+    return 8u * (unsigned)lane_groups(n) + 8u * (unsigned)lane_leaves(lane_groups(n));
+}
 // Per block of the cooperative variant: one word per warp (lanes whose output-node rates changed in
 // a cooperative update); the per-lane variant needs none.
 __host__ __device__ __forceinline__ unsigned lane_block_extra(int block) { return 4u * (unsigned)((block + 31) / 32); }
@@ -38,7 +47,7 @@ struct LaneSmem {
 __device__ __forceinline__ LaneSmem lane_smem_at(unsigned char* base, int G, int T) {
     LaneSmem m;
     m.fen = reinterpret_cast<unsigned long long*>(base);
-    m.st = reinterpret_cast<unsigned*>(m.fen + (size_t)G * T);
+    m.st = reinterpret_cast<unsigned*>(m.fen + (size_t)lane_leaves(G) * T);
     m.act = m.st + (size_t)G * T;
     m.wtouch = m.act + (size_t)G * T;
     return m;
@@ -50,7 +59,8 @@ __device__ __forceinline__ unsigned col_bit(const unsigned* col, int T, int i) {
     return (col[(i >> 5) * T] >> (i & 31)) & 1u;
 }
 
-// Fenwick tree of one trajectory (`col` points at its entry of row 0; tree index i is row i-1).
+// Fenwick tree of one trajectory over G leaves (`col` points at its entry of row 0; tree index i is
+// row i-1).
 __device__ __forceinline__ void fen_add(unsigned long long* col, int T, int G, int g, unsigned long long delta) {
     for (int i = g + 1; i <= G; i += i & -i) col[(size_t)(i - 1) * T] += delta;
 }
@@ -58,8 +68,9 @@ __device__ __forceinline__ void fen_add_atomic(unsigned long long* col, int T, i
                                                unsigned long long delta) {
     for (int i = g + 1; i <= G; i += i & -i) atomicAdd(col + (size_t)(i - 1) * T, delta);
 }
-// Group holding target r (r < total): the largest g with sum(groups < g) <= r; r becomes relative
-// to that group. `top` is the largest power of two <= G.
+// Leaf holding target r (r < total): the largest l with sum(leaves < l) <= r; r becomes relative
+// to that leaf. `top` is the largest power of two <= G (the tree's size), or half of it when that
+// entry is the root.
 __device__ __forceinline__ int fen_find(const unsigned long long* col, int T, int G, int top,
                                         unsigned long long& r) {
     int pos = 0;
@@ -177,9 +188,9 @@ __device__ __forceinline__ float lane_entropy(const SimParams& p, const unsigned
 }
 
 // The whole warp sets up the trajectory `traj` in column `c` (state, active bits, Fenwick tree);
-// returns the total rate on every lane. Groups are processed 32 at a time (chunk): lane l holds
-// the sum of group 32 * chunk + l, a scan gives the prefixes, and tree entry
-// i = P(i) - P(i - lowbit(i)) (P(x) = sum of groups < x) takes P(i - lowbit(i)) from this chunk
+// returns the total rate on every lane. Leaves are processed 32 at a time (chunk): lane l holds
+// the sum of leaf 32 * chunk + l, a scan gives the prefixes, and tree entry
+// i = P(i) - P(i - lowbit(i)) (P(x) = sum of leaves < x) takes P(i - lowbit(i)) from this chunk
 // or, at a multiple of 32, from the chunk boundaries kept one per lane.
 __device__ __forceinline__ unsigned long long lane_coop_init(const SimParams& p, const LaneSmem& m, int T, int c,
                                                              unsigned long long traj, unsigned lane) {
@@ -202,19 +213,26 @@ __device__ __forceinline__ unsigned long long lane_coop_init(const SimParams& p,
         st[w * T] = word;
     }
     __syncwarp();
+    const int L = lane_leaves(G);
     unsigned long long carry = 0ull, bnd = 0ull;
-    for (int ch = 0; ch * 32 < G; ++ch) {
+    for (int ch = 0; ch * 32 < L; ++ch) {
         if ((int)lane == ch) bnd = carry;  // P(32 * ch)
         unsigned long long mine = 0ull;
-        const int gend = min(G - ch * 32, 32);
-        for (int gg = 0; gg < gend; ++gg) {
-            const int g = ch * 32 + gg;
-            const int i = g * 32 + (int)lane;
-            const unsigned long long v = i < n ? lane_eval(p, i, st, T) : 0ull;
-            const unsigned a = __ballot_sync(MBG_FULL, v != 0ull);
+        const int lend = min(L - ch * 32, 32);
+        for (int ll = 0; ll < lend; ++ll) {
+            // leaf ch * 32 + ll: its groups in turn, one node per lane
+            unsigned long long v = 0ull;
+            for (int h = 0; h < (1 << kLeafShift); ++h) {
+                const int g = ((ch * 32 + ll) << kLeafShift) + h;
+                if (g >= G) break;
+                const int i = g * 32 + (int)lane;
+                const unsigned long long vi = i < n ? lane_eval(p, i, st, T) : 0ull;
+                const unsigned a = __ballot_sync(MBG_FULL, vi != 0ull);
+                if (lane == 0u) m.act[(size_t)g * T + c] = a;
+                v += vi;
+            }
             const unsigned long long s = warp_sum_u64(v);
-            if (lane == 0u) m.act[(size_t)g * T + c] = a;
-            if ((int)lane == gg) mine = s;
+            if ((int)lane == ll) mine = s;
         }
         const unsigned long long P = carry + warp_scan_u64(mine, lane);  // P(32 * ch + lane + 1)
         const int idx = ch * 32 + (int)lane + 1;                        // tree index
@@ -222,19 +240,17 @@ __device__ __forceinline__ unsigned long long lane_coop_init(const SimParams& p,
         const unsigned long long v_in = __shfl_sync(MBG_FULL, P, (j - 1 - ch * 32) & 31);
         const unsigned long long v_bnd = __shfl_sync(MBG_FULL, bnd, (j >> 5) & 31);
         const unsigned long long Pj = j > ch * 32 ? v_in : v_bnd;
-        if (idx <= G) m.fen[(size_t)(idx - 1) * T + c] = P - Pj;
+        if (idx <= L) m.fen[(size_t)(idx - 1) * T + c] = P - Pj;
         carry = __shfl_sync(MBG_FULL, P, 31);
     }
     __syncwarp();
     return carry;
 }
 
-// First node whose inclusive rate prefix exceeds r (r < total), or -1.
-__device__ __forceinline__ int lane_pick(const SimParams& p, const unsigned* st, const unsigned* act,
-                                         const unsigned long long* fen, int T, int G, int top,
-                                         unsigned long long r) {
-    const int g = fen_find(fen, T, G, top, r);
-    if (g >= G) return -1;
+// Walks the active nodes of group g in node order: the first whose inclusive rate prefix exceeds
+// r, or -1 with r reduced by the group's total.
+__device__ __forceinline__ int lane_walk(const SimParams& p, const unsigned* st, const unsigned* act, int T, int g,
+                                         unsigned long long& r) {
     unsigned aw = act[g * T];
     const unsigned sw = st[g * T];
     if (!p.has_palette) {
@@ -266,6 +282,21 @@ __device__ __forceinline__ int lane_pick(const SimParams& p, const unsigned* st,
             p.has_palette ? lane_rate(p, i, st, act, T) : __ldg(&p.lnodes[i].up + ((sw >> b) & 1u));
         if (r < v) return i;
         r -= v;
+    }
+    return -1;
+}
+
+// First node whose inclusive rate prefix exceeds r (r < total), or -1: the leaf from the tree,
+// then its groups in turn.
+__device__ __forceinline__ int lane_pick(const SimParams& p, const unsigned* st, const unsigned* act,
+                                         const unsigned long long* fen, int T, int G, int top,
+                                         unsigned long long r) {
+    const int l = fen_find(fen, T, lane_leaves(G), top, r);
+    for (int h = 0; h < (1 << kLeafShift); ++h) {
+        const int g = (l << kLeafShift) + h;
+        if (g >= G) return -1;
+        const int k = lane_walk(p, st, act, T, g, r);
+        if (k >= 0) return k;
     }
     return -1;
 }
@@ -320,9 +351,9 @@ __device__ __forceinline__ unsigned long long lane_reader_rec(const SimParams& p
     }
     const unsigned long long delta = r_new - r_old;
     if (delta != 0ull) {
-        const int G = lane_groups(p.n);
-        if (ATOMIC) fen_add_atomic(m.fen + col, T, G, g, delta);
-        else fen_add(m.fen + col, T, G, g, delta);
+        const int L = lane_leaves(lane_groups(p.n));
+        if (ATOMIC) fen_add_atomic(m.fen + col, T, L, g >> kLeafShift, delta);
+        else fen_add(m.fen + col, T, L, g >> kLeafShift, delta);
         out |= ((e >> 15) & 1u) != 0u;
     }
     return delta;
@@ -479,11 +510,11 @@ __device__ __forceinline__ int lane_step_front(const SimParams& p, const LaneSme
         tr.status = TRAJ_FINISHED;
         return -1;
     }
-    const int G = lane_groups(p.n);
+    const int G = lane_groups(p.n), L = lane_leaves(G);
     unsigned* st = m.st + col;
-    // the tree's root (G a power of two) holds the total, which r never reaches: start below it
-    const int top = 1 << (31 - __clz(G));
-    const int k = lane_pick(p, st, m.act + col, m.fen + col, T, G, top == G ? top >> 1 : top,
+    // the tree's root (L a power of two) holds the total, which r never reaches: start below it
+    const int top = 1 << (31 - __clz(L));
+    const int k = lane_pick(p, st, m.act + col, m.fen + col, T, G, top == L ? top >> 1 : top,
                             pick_target(d.y, d.z, tr.total));
     if (k < 0 || k >= p.n) {
         tr.status = TRAJ_ERROR;
@@ -499,7 +530,7 @@ __device__ __forceinline__ int lane_step_front(const SimParams& p, const LaneSme
 // when an output node's rate changed.
 __device__ __forceinline__ void lane_after_coop(const SimParams& p, const LaneSmem& m, int T, int col, int wbase,
                                                 unsigned lane, LaneTraj& tr) {
-    tr.total = fen_total(m.fen + col, T, lane_groups(p.n));
+    tr.total = fen_total(m.fen + col, T, lane_leaves(lane_groups(p.n)));
     if ((m.wtouch[wbase >> 5] >> lane) & 1u) tr.h = lane_entropy(p, m.st + col, m.act + col, T);
 }
 
