@@ -414,7 +414,8 @@ def run_ours(args):
         "vs_baseline": None, "dtype": "u64", "data": "synthetic",
         "config": {"workload": WORKLOADS[args.workload], "trajectories_per_gpu": n_rank,
                    "transitions_per_step": trans_all, "layout": ["", "thread", "warp", "lane"][summary["layout"]],
-                   "block_size": summary.get("block_size"),
+                   "block_size": summary.get("block_size"), "grid_size": summary.get("grid_size"),
+                   "lane_update": summary.get("lane_update"),
                    "l2": "flushed between steps (256 MiB write)", "wall_s": wall},
         "e2e": {"value": e2e_value, "unit": "transitions/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "ms_per_step": e2e_step_ms,

@@ -312,7 +312,8 @@ cudaError_t sim_lane_batch_configure(bool coop, size_t smem, int block, int* blo
 }
 
 size_t sim_lane_smem(int n, int block, bool coop) {
-    return (size_t)block * lane_smem_bytes(n) + (coop ? lane_block_extra(block) : 0);
+    (void)coop;  // both reader-update variants use the same per-thread rows
+    return (size_t)block * lane_smem_bytes(n);
 }
 
 int sim_lane_rows(int n) { return lane_groups(n); }

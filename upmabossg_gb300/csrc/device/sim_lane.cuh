@@ -28,19 +28,17 @@ constexpr int kLeafShift = 1;
 __host__ __device__ __forceinline__ int lane_leaves(int groups) {
     return (groups + (1 << kLeafShift) - 1) >> kLeafShift;
 }
-// Shared-memory bytes per thread (plus lane_block_extra per block).
+// Shared-memory bytes per thread.
 __host__ __device__ __forceinline__ unsigned lane_smem_bytes(int n) {
     return 8u * (unsigned)lane_groups(n) + 8u * (unsigned)lane_leaves(lane_groups(n));
 }
 // Per block of the cooperative variant: one word per warp (lanes whose output-node rates changed in
 // a cooperative update); the per-lane variant needs none.
-__host__ __device__ __forceinline__ unsigned lane_block_extra(int block) { return 4u * (unsigned)((block + 31) / 32); }
 
 struct LaneSmem {
     unsigned long long* fen;  // [G][T]
     unsigned* st;             // [G][T]
     unsigned* act;            // [G][T]
-    unsigned* wtouch;         // [T / 32]
 };
 
 // `G` rows of T entries per array: the largest model's group count in a batched launch.
@@ -49,7 +47,6 @@ __device__ __forceinline__ LaneSmem lane_smem_at(unsigned char* base, int G, int
     m.fen = reinterpret_cast<unsigned long long*>(base);
     m.st = reinterpret_cast<unsigned*>(m.fen + (size_t)lane_leaves(G) * T);
     m.act = m.st + (size_t)G * T;
-    m.wtouch = m.act + (size_t)G * T;
     return m;
 }
 
@@ -395,10 +392,11 @@ __device__ __forceinline__ bool lane_update(const SimParams& p, int k, const Lan
 // Warp-cooperative form of lane_update for every lane at once (k < 0: nothing flipped): the
 // reader lists of the 32 flipped nodes are concatenated and dealt out one entry per lane, so a
 // step costs ceil(total length / 32) rounds instead of the longest list. Entries of one trajectory
-// patch its shared-memory rows with atomics; lanes whose output-node rates changed are marked in
-// the warp's wtouch word. `owner(o)` gives the model of lane o's trajectory (called by all lanes).
+// patch its shared-memory rows with atomics. Returns (on every lane) the mask of lanes whose
+// output-node rates changed. `owner(o)` gives the model of lane o's trajectory (called by all
+// lanes).
 template <class Owner>
-__device__ __forceinline__ void lane_coop_update(const SimParams& mine, Owner owner, const LaneSmem& m, int T,
+__device__ __forceinline__ unsigned lane_coop_update(const SimParams& mine, Owner owner, const LaneSmem& m, int T,
                                                  int wbase, unsigned lane, int k) {
     int d0 = 0, c = 0;
     if (k >= 0) {
@@ -431,8 +429,8 @@ __device__ __forceinline__ void lane_coop_update(const SimParams& mine, Owner ow
         if (q < C) lane_reader<true>(po, __ldg(po.deps + o_d0 + (q - o_ex)), m, T, wbase + o, out);
         touched |= __reduce_or_sync(MBG_FULL, out ? 1u << o : 0u);
     }
-    if (lane == 0u) m.wtouch[wbase >> 5] = touched;
-    __syncwarp();
+    __syncwarp();  // every patch is visible to its trajectory's lane
+    return touched;
 }
 
 // Registers of the trajectory a lane is running.
@@ -528,10 +526,10 @@ __device__ __forceinline__ int lane_step_front(const SimParams& p, const LaneSme
 
 // After the readers of k were updated cooperatively: the new total from the tree, the entropy
 // when an output node's rate changed.
-__device__ __forceinline__ void lane_after_coop(const SimParams& p, const LaneSmem& m, int T, int col, int wbase,
-                                                unsigned lane, LaneTraj& tr) {
+__device__ __forceinline__ void lane_after_coop(const SimParams& p, const LaneSmem& m, int T, int col,
+                                                unsigned touched, unsigned lane, LaneTraj& tr) {
     tr.total = fen_total(m.fen + col, T, lane_leaves(lane_groups(p.n)));
-    if ((m.wtouch[wbase >> 5] >> lane) & 1u) tr.h = lane_entropy(p, m.st + col, m.act + col, T);
+    if ((touched >> lane) & 1u) tr.h = lane_entropy(p, m.st + col, m.act + col, T);
 }
 
 // Completes the step: output state, clock, transition count; at the end of the trajectory its
@@ -605,8 +603,9 @@ __device__ void sim_lane_body(const SimParams& p, unsigned char* smem) {
         if (!COOP && !tr.have) continue;
         const int k = tr.have ? lane_step_front(p, m, T, col, tr, COOP) : -1;
         if (COOP) {
-            lane_coop_update(p, [&](int) -> const SimParams& { return p; }, m, T, wbase, lane, k);
-            if (k >= 0) lane_after_coop(p, m, T, col, wbase, lane, tr);
+            const unsigned touched =
+                lane_coop_update(p, [&](int) -> const SimParams& { return p; }, m, T, wbase, lane, k);
+            if (k >= 0) lane_after_coop(p, m, T, col, touched, lane, tr);
         }
         if (tr.have) lane_step_back(p, m, T, col, tr, k, c);
     }
@@ -674,14 +673,14 @@ __device__ void sim_lane_batch_body(const BatchDesc& b, unsigned char* smem) {
         const SimParams& p = *pp;
         const int k = tr.have ? lane_step_front(p, m, T, col, tr, COOP) : -1;
         if (COOP) {
-            lane_coop_update(
+            const unsigned touched = lane_coop_update(
                 p,
                 [&](int o) -> const SimParams& {
                     return *reinterpret_cast<const SimParams*>(
                         __shfl_sync(MBG_FULL, reinterpret_cast<unsigned long long>(pp), o));
                 },
                 m, T, wbase, lane, k);
-            if (k >= 0) lane_after_coop(p, m, T, col, wbase, lane, tr);
+            if (k >= 0) lane_after_coop(p, m, T, col, touched, lane, tr);
         }
         if (tr.have) lane_step_back(p, m, T, col, tr, k, c);
     }

@@ -299,6 +299,7 @@ void Sim::autotune() {
     const bool log = std::getenv("MBG_AUTOTUNE_LOG") != nullptr;
     double best = -1;
     Shape best_shape{MBG_LAYOUT_WARP, 256, false};
+    std::vector<std::pair<double, Shape>> timed;
     for (int lay : {MBG_LAYOUT_THREAD, MBG_LAYOUT_WARP, MBG_LAYOUT_LANE}) {
         for (int blk : {64, 128, 256}) {
             for (int coop = 0; coop < 2; ++coop) {
@@ -316,10 +317,34 @@ void Sim::autotune() {
                 if (log)
                     std::fprintf(stderr, "mbg autotune: n=%d pilot=%llu layout=%d block=%d coop=%d kernel_ms=%.3f\n",
                                  cm.n, (unsigned long long)pilot, lay, blk, coop, summary.kernel_ms);
+                timed.push_back({summary.kernel_ms, Shape{lay, blk, coop != 0}});
                 if (best < 0 || summary.kernel_ms < best) {
                     best = summary.kernel_ms;
                     best_shape = Shape{lay, blk, coop != 0};
                 }
+            }
+        }
+    }
+    // A short pilot starts every lane's first trajectory together; a long run reaches a steady
+    // state in which the lanes of a warp are at unrelated points of their trajectories, and the
+    // layouts rank differently there. The closest candidates are timed again on a pilot four
+    // times longer.
+    const uint64_t pilot2 = std::min<uint64_t>(n_traj, 4 * pilot);
+    if (pilot2 > pilot && timed.size() > 1) {
+        std::sort(timed.begin(), timed.end(), [](const auto& a, const auto& b) { return a.first < b.first; });
+        scope.p.n_traj = pilot2;
+        best = -1;
+        for (size_t i = 0; i < timed.size() && i < 3 && timed[i].first <= 1.15 * timed[0].first; ++i) {
+            const Shape& sh = timed[i].second;
+            setup_layout(sh.layout, sh.block, sh.coop);
+            run(nullptr);
+            if (log)
+                std::fprintf(stderr, "mbg autotune: n=%d pilot=%llu layout=%d block=%d coop=%d kernel_ms=%.3f\n",
+                             cm.n, (unsigned long long)pilot2, sh.layout, sh.block, sh.coop ? 1 : 0,
+                             summary.kernel_ms);
+            if (best < 0 || summary.kernel_ms < best) {
+                best = summary.kernel_ms;
+                best_shape = sh;
             }
         }
     }
