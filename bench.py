@@ -402,7 +402,7 @@ def run_ours(args):
     kms = sum(kernel_ms) / len(kernel_ms)
     achieved = trans_step * w_tr / (kms * 1e-3)
     kernel = {MBG_LAYOUTS["thread"]: "mbg_sim_thread", MBG_LAYOUTS["warp"]: "mbg_sim_warp",
-              MBG_LAYOUTS["lane"]: "mbg_sim_lane"}[summary["layout"]]
+              MBG_LAYOUTS["lane"]: "mbg_sim_lane" if summary.get("lane_update") else "mbg_sim_lane_coop"}[summary["layout"]]
     prof = profile_figures(kernel, args.workload)
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu:
