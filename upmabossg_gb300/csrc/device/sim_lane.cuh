@@ -5,7 +5,7 @@
 // (src/jit_kernels/simulation.cu:9-21 and 77-164 with the generated compute_transition_rates of
 // src/generator.cpp:124-144). Here a lane keeps, for its trajectory:
 //   fen[L]  a Fenwick tree over the exact 64-bit fixed-point rate sums of leaves of
-//           2^kLeafShift 32-node groups (L = ceil(W / 2^kLeafShift)): entry i (1-based) holds the
+//           2^shift 32-node groups (L = ceil(W / 2^shift)): entry i (1-based) holds the
 //           sum of leaves (i - lowbit(i), i],
 //   st[W]   state words,
 //   act[W]  active words (bit i: node i's rate is non-zero),
@@ -22,30 +22,33 @@
 namespace mbg {
 
 __host__ __device__ __forceinline__ int lane_groups(int n) { return (n + 31) >> 5; }
-// Fenwick leaves: 2^kLeafShift consecutive 32-node groups each. Wider leaves shrink the tree (and
-// a trajectory's shared memory: more resident trajectories per SM) but lengthen the walk.
-constexpr int kLeafShift = 1;
-__host__ __device__ __forceinline__ int lane_leaves(int groups) {
-    return (groups + (1 << kLeafShift) - 1) >> kLeafShift;
+// Fenwick leaves: 2^shift consecutive 32-node groups each. Wider leaves shrink the tree (and a
+// trajectory's shared memory) but lengthen the walk, so they pay only where shared memory rather
+// than registers limits the resident trajectories: beyond 16 groups (512 nodes) of the largest
+// model a launch holds.
+__host__ __device__ __forceinline__ int lane_leaf_shift(int groups) { return groups > 16 ? 1 : 0; }
+__host__ __device__ __forceinline__ int lane_leaves(int groups, int shift) {
+    return (groups + (1 << shift) - 1) >> shift;
 }
 // Shared-memory bytes per thread.
 __host__ __device__ __forceinline__ unsigned lane_smem_bytes(int n) {
-    return 8u * (unsigned)lane_groups(n) + 8u * (unsigned)lane_leaves(lane_groups(n));
+    const int G = lane_groups(n);
+    return 8u * (unsigned)G + 8u * (unsigned)lane_leaves(G, lane_leaf_shift(G));
 }
-// Per block of the cooperative variant: one word per warp (lanes whose output-node rates changed in
-// a cooperative update); the per-lane variant needs none.
-
 struct LaneSmem {
-    unsigned long long* fen;  // [G][T]
+    unsigned long long* fen;  // [L][T]
     unsigned* st;             // [G][T]
     unsigned* act;            // [G][T]
+    int shift;                // leaves of 2^shift groups
 };
 
-// `G` rows of T entries per array: the largest model's group count in a batched launch.
+// `G` rows of T entries per array: the largest model's group count in a batched launch, which
+// also sets the leaf width of every trajectory of the launch.
 __device__ __forceinline__ LaneSmem lane_smem_at(unsigned char* base, int G, int T) {
     LaneSmem m;
+    m.shift = lane_leaf_shift(G);
     m.fen = reinterpret_cast<unsigned long long*>(base);
-    m.st = reinterpret_cast<unsigned*>(m.fen + (size_t)lane_leaves(G) * T);
+    m.st = reinterpret_cast<unsigned*>(m.fen + (size_t)lane_leaves(G, m.shift) * T);
     m.act = m.st + (size_t)G * T;
     return m;
 }
@@ -210,7 +213,7 @@ __device__ __forceinline__ unsigned long long lane_coop_init(const SimParams& p,
         st[w * T] = word;
     }
     __syncwarp();
-    const int L = lane_leaves(G);
+    const int L = lane_leaves(G, m.shift);
     unsigned long long carry = 0ull, bnd = 0ull;
     for (int ch = 0; ch * 32 < L; ++ch) {
         if ((int)lane == ch) bnd = carry;  // P(32 * ch)
@@ -219,8 +222,8 @@ __device__ __forceinline__ unsigned long long lane_coop_init(const SimParams& p,
         for (int ll = 0; ll < lend; ++ll) {
             // leaf ch * 32 + ll: its groups in turn, one node per lane
             unsigned long long v = 0ull;
-            for (int h = 0; h < (1 << kLeafShift); ++h) {
-                const int g = ((ch * 32 + ll) << kLeafShift) + h;
+            for (int h = 0; h < (1 << m.shift); ++h) {
+                const int g = ((ch * 32 + ll) << m.shift) + h;
                 if (g >= G) break;
                 const int i = g * 32 + (int)lane;
                 const unsigned long long vi = i < n ? lane_eval(p, i, st, T) : 0ull;
@@ -286,11 +289,11 @@ __device__ __forceinline__ int lane_walk(const SimParams& p, const unsigned* st,
 // First node whose inclusive rate prefix exceeds r (r < total), or -1: the leaf from the tree,
 // then its groups in turn.
 __device__ __forceinline__ int lane_pick(const SimParams& p, const unsigned* st, const unsigned* act,
-                                         const unsigned long long* fen, int T, int G, int top,
+                                         const unsigned long long* fen, int T, int G, int shift, int top,
                                          unsigned long long r) {
-    const int l = fen_find(fen, T, lane_leaves(G), top, r);
-    for (int h = 0; h < (1 << kLeafShift); ++h) {
-        const int g = (l << kLeafShift) + h;
+    const int l = fen_find(fen, T, lane_leaves(G, shift), top, r);
+    for (int h = 0; h < (1 << shift); ++h) {
+        const int g = (l << shift) + h;
         if (g >= G) return -1;
         const int k = lane_walk(p, st, act, T, g, r);
         if (k >= 0) return k;
@@ -348,9 +351,9 @@ __device__ __forceinline__ unsigned long long lane_reader_rec(const SimParams& p
     }
     const unsigned long long delta = r_new - r_old;
     if (delta != 0ull) {
-        const int L = lane_leaves(lane_groups(p.n));
-        if (ATOMIC) fen_add_atomic(m.fen + col, T, L, g >> kLeafShift, delta);
-        else fen_add(m.fen + col, T, L, g >> kLeafShift, delta);
+        const int L = lane_leaves(lane_groups(p.n), m.shift);
+        if (ATOMIC) fen_add_atomic(m.fen + col, T, L, g >> m.shift, delta);
+        else fen_add(m.fen + col, T, L, g >> m.shift, delta);
         out |= ((e >> 15) & 1u) != 0u;
     }
     return delta;
@@ -508,11 +511,11 @@ __device__ __forceinline__ int lane_step_front(const SimParams& p, const LaneSme
         tr.status = TRAJ_FINISHED;
         return -1;
     }
-    const int G = lane_groups(p.n), L = lane_leaves(G);
+    const int G = lane_groups(p.n), L = lane_leaves(G, m.shift);
     unsigned* st = m.st + col;
     // the tree's root (L a power of two) holds the total, which r never reaches: start below it
     const int top = 1 << (31 - __clz(L));
-    const int k = lane_pick(p, st, m.act + col, m.fen + col, T, G, top == L ? top >> 1 : top,
+    const int k = lane_pick(p, st, m.act + col, m.fen + col, T, G, m.shift, top == L ? top >> 1 : top,
                             pick_target(d.y, d.z, tr.total));
     if (k < 0 || k >= p.n) {
         tr.status = TRAJ_ERROR;
@@ -528,7 +531,7 @@ __device__ __forceinline__ int lane_step_front(const SimParams& p, const LaneSme
 // when an output node's rate changed.
 __device__ __forceinline__ void lane_after_coop(const SimParams& p, const LaneSmem& m, int T, int col,
                                                 unsigned touched, unsigned lane, LaneTraj& tr) {
-    tr.total = fen_total(m.fen + col, T, lane_leaves(lane_groups(p.n)));
+    tr.total = fen_total(m.fen + col, T, lane_leaves(lane_groups(p.n), m.shift));
     if ((touched >> lane) & 1u) tr.h = lane_entropy(p, m.st + col, m.act + col, T);
 }
 

@@ -37,6 +37,8 @@ public:
         size_t first = 0;                   // position of the first member in the class-ordered arrays
         BatchDesc desc{};                   // work over all members' trajectories
         BatchDesc pilot{};                  // a subset of every member's trajectories, for timing shapes
+        BatchDesc pilot_long{};             // four times the pilot, for re-timing the closest shapes
+        bool has_long = false;              // pilot_long covers more than the pilot
         int layout = MBG_LAYOUT_LANE;       // MBG_LAYOUT_LANE or MBG_LAYOUT_WARP
         int block = 128;
         bool variant = false;               // lane: cooperative reader update; warp: regulator index cache
