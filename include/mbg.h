@@ -265,6 +265,11 @@ mbg_status mbg_surrogate_train(mbg_surrogate* s, const float* x, const float* y,
                                int32_t batch, float lr, uint64_t seed, float* last_loss);
 /* probs: n x out_dim ensemble-mean distributions; spread: n values (either may be NULL). */
 mbg_status mbg_surrogate_predict(mbg_surrogate* s, const float* x, int64_t n, float* probs, float* spread);
+/* score: n ensemble-mean probabilities of output state `column` alone; spread as above (may be
+ * NULL). For screening many candidates on one target state without reading every distribution
+ * back. */
+mbg_status mbg_surrogate_predict_column(mbg_surrogate* s, const float* x, int64_t n, int32_t column, float* score,
+                                        float* spread);
 int64_t mbg_surrogate_param_count(const mbg_surrogate* s);
 mbg_status mbg_surrogate_get_params(mbg_surrogate* s, int32_t member, float* params);
 mbg_status mbg_surrogate_set_params(mbg_surrogate* s, int32_t member, const float* params);

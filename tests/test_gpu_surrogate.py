@@ -54,6 +54,25 @@ def test_tcgen05_forward_matches_mma_sync(dims, rows):
     assert np.abs(a - mlp.softmax(z)).max() < 2e-3
 
 
+def test_predict_column_matches_full_prediction():
+    """The screening read-back (one output column and the spread, per row) equals the full
+    ensemble prediction's column bit for bit, across chunk boundaries and for any subset of rows
+    (rows are independent in every product)."""
+    rng = np.random.default_rng(5)
+    s = mbg.Surrogate(32, 256, hidden=128, hidden_layers=2, ensemble=3, seed=4)
+    x = rng.uniform(-1, 1, size=(70000, 32)).astype(np.float32)
+    probs, spread = s.predict(x)
+    for col in (0, 77, 255):
+        score, sp = s.predict_column(x, col)
+        assert np.array_equal(score, probs[:, col])
+        assert np.array_equal(sp, spread)
+    sub = np.array([3, 65535, 65536, 69999])
+    p_sub, s_sub = s.predict(x[sub])
+    assert np.array_equal(p_sub, probs[sub]) and np.array_equal(s_sub, spread[sub])
+    with pytest.raises(mbg.MbgError):
+        s.predict_column(x[:10], 256)
+
+
 def test_gradients_match_reference():
     rng = np.random.default_rng(1)
     s = make()

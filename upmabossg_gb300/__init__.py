@@ -34,7 +34,7 @@ EXPORTS = (
     "mbg_batch_fixed_points", "mbg_batch_class_count", "mbg_batch_class", "mbg_batch_class_timings",
     "mbg_surrogate_create", "mbg_surrogate_destroy", "mbg_surrogate_train", "mbg_surrogate_predict",
     "mbg_surrogate_param_count", "mbg_surrogate_get_params", "mbg_surrogate_set_params", "mbg_surrogate_gradients",
-    "mbg_surrogate_set_tensor_path", "mbg_surrogate_time_forward",
+    "mbg_surrogate_set_tensor_path", "mbg_surrogate_time_forward", "mbg_surrogate_predict_column",
 )
 
 
@@ -154,6 +154,7 @@ def lib():
             "mbg_surrogate_train": (ctypes.c_int, [vp, dp, dp, ctypes.c_int64, i32, i32, ctypes.c_float, u64,
                                                    ctypes.POINTER(ctypes.c_float)]),
             "mbg_surrogate_predict": (ctypes.c_int, [vp, dp, ctypes.c_int64, dp, dp]),
+            "mbg_surrogate_predict_column": (ctypes.c_int, [vp, dp, ctypes.c_int64, i32, dp, dp]),
             "mbg_surrogate_param_count": (ctypes.c_int64, [vp]),
             "mbg_surrogate_get_params": (ctypes.c_int, [vp, i32, dp]),
             "mbg_surrogate_set_params": (ctypes.c_int, [vp, i32, dp]),
@@ -497,6 +498,14 @@ class Surrogate:
         spread = np.zeros(len(x), np.float32)
         _check(lib().mbg_surrogate_predict(self._h, _p(x), len(x), _p(probs), _p(spread)))
         return probs, spread
+
+    def predict_column(self, x, column):
+        """Ensemble-mean probability of output state `column` and the spread, per row."""
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        score = np.zeros(len(x), np.float32)
+        spread = np.zeros(len(x), np.float32)
+        _check(lib().mbg_surrogate_predict_column(self._h, _p(x), len(x), int(column), _p(score), _p(spread)))
+        return score, spread
 
     def params(self, member=0):
         out = np.zeros(self.param_count(), np.float32)

@@ -247,6 +247,18 @@ __global__ void mlp_ensemble_stats_kernel(const float* __restrict__ probs, int m
     if (lane == 0) spread[row] = worst;
 }
 
+__global__ void mlp_gather_column_kernel(const float* __restrict__ x, int rows, int cols, int column,
+                                         float* __restrict__ y) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r < rows) y[r] = x[(size_t)r * cols + column];
+}
+
+cudaError_t mlp_gather_column(const float* x, int rows, int cols, int column, float* y, cudaStream_t s) {
+    if (rows <= 0) return cudaSuccess;
+    mlp_gather_column_kernel<<<(rows + 255) / 256, 256, 0, s>>>(x, rows, cols, column, y);
+    return cudaGetLastError();
+}
+
 cudaError_t mlp_ensemble_stats(const float* probs, int members, int rows, int cols, float* mean, float* spread,
                                cudaStream_t s) {
     mlp_ensemble_stats_kernel<<<(rows + 7) / 8, 256, 0, s>>>(probs, members, rows, cols, mean, spread);

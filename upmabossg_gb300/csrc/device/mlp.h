@@ -56,6 +56,8 @@ cudaError_t mlp_to_bf16(const float* x, __nv_bfloat16* y, long long n, cudaStrea
 // total-variation distance between the member and the mean.
 cudaError_t mlp_ensemble_stats(const float* probs, int members, int rows, int cols, float* mean, float* spread,
                                cudaStream_t s);
+// y[r] = x[r, column] for a rows x cols matrix.
+cudaError_t mlp_gather_column(const float* x, int rows, int cols, int column, float* y, cudaStream_t s);
 // y[i, :] = x[idx[i], :] (rows of `cols` floats), converting to BF16 when yb is set.
 cudaError_t mlp_gather_rows(const float* x, const int* idx, int rows, int cols, float* y, __nv_bfloat16* yb,
                             cudaStream_t s);

@@ -527,6 +527,12 @@ mbg_status mbg_surrogate_predict(mbg_surrogate* s, const float* x, int64_t n, fl
     return guard([&] { s->s.predict(x, n, probs, spread); });
 }
 
+mbg_status mbg_surrogate_predict_column(mbg_surrogate* s, const float* x, int64_t n, int32_t column, float* score,
+                                        float* spread) {
+    if (!s || !x || !score) return fail(MBG_ERR_ARG, "null argument");
+    return guard([&] { s->s.predict(x, n, nullptr, spread, column, score); });
+}
+
 int64_t mbg_surrogate_param_count(const mbg_surrogate* s) { return s ? s->s.param_count() : -1; }
 
 mbg_status mbg_surrogate_get_params(mbg_surrogate* s, int32_t member, float* params) {

@@ -349,8 +349,10 @@ float Surrogate::train(const float* x, const float* y, int64_t n, int epochs, in
     }
 }
 
-void Surrogate::predict(const float* x, int64_t n, float* out_probs, float* out_spread, int chunk) {
+void Surrogate::predict(const float* x, int64_t n, float* out_probs, float* out_spread, int column,
+                        float* out_score, int chunk) {
     ck(cudaSetDevice(device), "cudaSetDevice");
+    if (out_score && (column < 0 || column >= out_dim)) throw ArgError("output column out of range");
     chunk = (int)std::max<int64_t>(1, std::min<int64_t>(chunk, n));
     ensure_batch(chunk);
     for (int64_t r0 = 0; r0 < n; r0 += chunk) {
@@ -372,6 +374,12 @@ void Surrogate::predict(const float* x, int64_t n, float* out_probs, float* out_
         if (out_spread)
             ck(cudaMemcpyAsync(out_spread + r0, spread, (size_t)rows * 4, cudaMemcpyDeviceToHost, stream),
                "cudaMemcpyAsync");
+        if (out_score) {
+            // the column is gathered into the first rows of the (already copied) per-member buffer
+            ck(mlp_gather_column(mean, rows, out_dim, column, probs, stream), "mlp_gather_column");
+            ck(cudaMemcpyAsync(out_score + r0, probs, (size_t)rows * 4, cudaMemcpyDeviceToHost, stream),
+               "cudaMemcpyAsync");
+        }
         ck(cudaStreamSynchronize(stream), "prediction");
     }
     check_tc_error();

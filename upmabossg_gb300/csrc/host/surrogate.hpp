@@ -31,7 +31,10 @@ public:
     ~Surrogate();
     void create(int in_dim, int hidden, int hidden_layers, int out_dim, int ensemble, uint64_t seed, int device);
     float train(const float* x, const float* y, int64_t n, int epochs, int batch, float lr, uint64_t seed);
-    void predict(const float* x, int64_t n, float* probs, float* spread, int chunk = 8192);
+    // Ensemble mean distribution (probs, n x out; may be null), spread (may be null) and, when
+    // score is set, the mean probability of output `column` alone.
+    void predict(const float* x, int64_t n, float* probs, float* spread, int column = -1, float* score = nullptr,
+                 int chunk = 65536);
     float gradients(int member, const float* x, const float* y, int rows);
     int64_t param_count() const;
     // Device time (ms) of one forward pass of every member over `rows` rows, mean of `reps`.

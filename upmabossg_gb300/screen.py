@@ -101,18 +101,21 @@ def screen(surrogate: mbg.Surrogate, sim: PointSimulator, candidates: np.ndarray
     likely first) and re-simulates them together with every candidate whose ensemble spread
     exceeds spread_cut."""
     t0 = time.perf_counter()
-    probs, spread = surrogate.predict(encode(candidates))
-    predict_s = time.perf_counter() - t0
-    score = probs[:, target_state]
+    # the target state's probability and the spread for every candidate; full distributions only
+    # for the reported ones
+    score, spread = surrogate.predict_column(encode(candidates), target_state)
     hits = np.nonzero(score >= threshold)[0]
     hits = hits[np.argsort(-score[hits])][:max_report]
+    hit_probs = surrogate.predict(encode(candidates[hits]))[0] if len(hits) else np.zeros((0, surrogate.out_dim))
+    predict_s = time.perf_counter() - t0
     uncertain = np.nonzero(spread > spread_cut)[0]
     todo = np.union1d(hits, uncertain)
     t1 = time.perf_counter()
-    truth = sim.final_window(candidates[todo], ids=todo) if len(todo) else np.zeros((0, probs.shape[1]))
+    truth = sim.final_window(candidates[todo], ids=todo) if len(todo) else np.zeros((0, hit_probs.shape[1]))
     resim_s = time.perf_counter() - t1
     pos = {int(i): k for k, i in enumerate(todo)}
-    tv = np.array([total_variation(probs[i], truth[pos[int(i)]]) for i in hits]) if len(hits) else np.zeros(0)
+    tv = np.array([total_variation(hit_probs[k], truth[pos[int(i)]]) for k, i in enumerate(hits)]) \
+        if len(hits) else np.zeros(0)
     total_s = predict_s + resim_s
     screened = len(candidates) / total_s if total_s > 0 else math.inf
     return ScreenReport(
@@ -121,5 +124,5 @@ def screen(surrogate: mbg.Surrogate, sim: PointSimulator, candidates: np.ndarray
         tv_max=float(tv.max()) if len(tv) else 0.0, tv_frac_ok=float((tv <= 0.01).mean()) if len(tv) else 1.0,
         plain_points_per_s=plain_points_per_s, screened_points_per_s=screened,
         speedup=screened / plain_points_per_s if plain_points_per_s > 0 else math.inf,
-        hits=hits, hit_probs=probs[hits],
-        hit_truth=np.array([truth[pos[int(i)]] for i in hits]) if len(hits) else np.zeros((0, probs.shape[1])))
+        hits=hits, hit_probs=hit_probs,
+        hit_truth=np.array([truth[pos[int(i)]] for i in hits]) if len(hits) else np.zeros((0, hit_probs.shape[1])))
