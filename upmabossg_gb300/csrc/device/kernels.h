@@ -16,8 +16,8 @@ unsigned sim_warp_smem_per_warp(int n, bool cached_index);
 cudaError_t sim_warp_occupancy(bool cached_index, int block, size_t smem, int* blocks_per_sm);
 cudaError_t launch_sim_lane(const SimParams& p, bool coop, int grid, int block, size_t smem, cudaStream_t stream);
 cudaError_t sim_lane_configure(bool coop, size_t smem, int block, int* blocks_per_sm);
-// Dynamic shared memory of a lane-layout block (the cooperative variant adds one word per warp).
-size_t sim_lane_smem(int n, int block, bool coop);
+// Dynamic shared memory of a lane-layout block (the same for both reader-update variants).
+size_t sim_lane_smem(int n, int block);
 int sim_lane_rows(int n);                 // BatchDesc::rows for models of up to n nodes
 // Re-applies the attributes of a simulation kernel for the launch shapes that are about to use it
 // (kernel 0: mbg_sim_lane[_coop], 1: mbg_sim_lane_batch[_coop], 2: mbg_sim_warp_batch[_gather],

@@ -311,10 +311,7 @@ cudaError_t sim_lane_batch_configure(bool coop, size_t smem, int block, int* blo
                           block, blocks_per_sm);
 }
 
-size_t sim_lane_smem(int n, int block, bool coop) {
-    (void)coop;  // both reader-update variants use the same per-thread rows
-    return (size_t)block * lane_smem_bytes(n);
-}
+size_t sim_lane_smem(int n, int block) { return (size_t)block * lane_smem_bytes(n); }
 
 int sim_lane_rows(int n) { return lane_groups(n); }
 

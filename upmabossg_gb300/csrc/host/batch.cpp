@@ -282,7 +282,7 @@ void Batch::create(const std::vector<const CompiledModel*>& models, const std::v
     for (size_t c = 0; c < classes.size(); ++c) {
         Class& k = classes[c];
         const int blk = o.block_size > 0 ? o.block_size : 128;
-        const bool lane_fits = sim_lane_smem(k.max_n, blk, false) <= kSmemLimit;
+        const bool lane_fits = sim_lane_smem(k.max_n, blk) <= kSmemLimit;
         const int lay = o.layout ? o.layout : (lane_fits ? MBG_LAYOUT_LANE : MBG_LAYOUT_WARP);
         const bool variant =
             lay == MBG_LAYOUT_WARP && (size_t)(blk / 32) * sim_warp_batch_slice_bytes(k.max_n, true) <= 100 * 1024;
@@ -296,7 +296,7 @@ void Batch::configure(int c, int lay, int blk, bool variant) {
     int bps = 0;
     size_t sm = 0;
     if (lay == MBG_LAYOUT_LANE) {
-        sm = sim_lane_smem(k.max_n, blk, variant);
+        sm = sim_lane_smem(k.max_n, blk);
         if (sm > kSmemLimit) throw ModelError("largest instance of a size class too large for the batched lane layout");
         ck(sim_lane_batch_configure(variant, sm, blk, &bps), "batched lane kernel occupancy");
     } else {
@@ -369,7 +369,7 @@ void Batch::autotune() {
             for (int blk : {64, 128, 256}) {
                 if (opts.block_size > 0 && blk != opts.block_size) continue;
                 for (int var = 0; var < 2; ++var) {
-                    if (lay == MBG_LAYOUT_LANE && sim_lane_smem(k.max_n, blk, var != 0) > kSmemLimit) continue;
+                    if (lay == MBG_LAYOUT_LANE && sim_lane_smem(k.max_n, blk) > kSmemLimit) continue;
                     if (lay == MBG_LAYOUT_WARP &&
                         (size_t)(blk / 32) * sim_warp_batch_slice_bytes(k.max_n, var != 0) > 100 * 1024)
                         continue;

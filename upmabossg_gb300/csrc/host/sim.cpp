@@ -246,7 +246,7 @@ void Sim::create(const CompiledModel& model, const std::vector<std::string>& nod
             // the lane layout's shared memory grows with N: the largest block that fits
             blk = 256;
             if (o.layout == MBG_LAYOUT_LANE)
-                while (blk > 32 && sim_lane_smem(cm.n, blk, o.lane_update != 1) > 227 * 1024) blk >>= 1;
+                while (blk > 32 && sim_lane_smem(cm.n, blk) > 227 * 1024) blk >>= 1;
         }
         setup_layout(o.layout, blk, o.lane_update != 1);
     } else if (o.thread_cutoff > 0) {
@@ -306,7 +306,7 @@ void Sim::autotune() {
                 if (opts.block_size > 0 && blk != opts.block_size) continue;
                 if (lay != MBG_LAYOUT_LANE && (blk == 64 || coop)) continue;
                 if (lay == MBG_LAYOUT_THREAD && cm.words > 16) continue;
-                if (lay == MBG_LAYOUT_LANE && sim_lane_smem(cm.n, blk, coop != 0) > 227 * 1024) continue;
+                if (lay == MBG_LAYOUT_LANE && sim_lane_smem(cm.n, blk) > 227 * 1024) continue;
                 try {
                     setup_layout(lay, blk, coop != 0);
                 } catch (const JitError&) {
@@ -368,7 +368,7 @@ void Sim::setup_layout(int lay, int blk, bool coop) {
         ck(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, (const void*)thread_kernel, block, 0),
            "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
     } else if (layout == MBG_LAYOUT_LANE) {
-        smem = sim_lane_smem(cm.n, block, lane_coop);
+        smem = sim_lane_smem(cm.n, block);
         if (smem > 227 * 1024) throw ModelError("model too large for the lane layout's shared memory at this block size");
         ck(sim_lane_configure(lane_coop, smem, block, &bps), "configuring mbg_sim_lane");
     } else {
