@@ -287,11 +287,21 @@ __device__ __forceinline__ int lane_walk(const SimParams& p, const unsigned* st,
 }
 
 // First node whose inclusive rate prefix exceeds r (r < total), or -1: the leaf from the tree,
-// then its groups in turn.
+// then its groups in turn. SPLIT writes the two walks of a two-group leaf out separately instead
+// of as a loop: the same result, different code; which one runs faster depends on the kernel it
+// is compiled into (measured per kernel).
+template <bool SPLIT>
 __device__ __forceinline__ int lane_pick(const SimParams& p, const unsigned* st, const unsigned* act,
                                          const unsigned long long* fen, int T, int G, int shift, int top,
                                          unsigned long long r) {
     const int l = fen_find(fen, T, lane_leaves(G, shift), top, r);
+    if (SPLIT) {
+        const int g = l << shift;
+        if (g >= G) return -1;
+        const int k = lane_walk(p, st, act, T, g, r);
+        if (k >= 0 || shift == 0 || g + 1 >= G) return k;
+        return lane_walk(p, st, act, T, g + 1, r);
+    }
     for (int h = 0; h < (1 << shift); ++h) {
         const int g = (l << shift) + h;
         if (g >= G) return -1;
@@ -487,6 +497,7 @@ __device__ __forceinline__ void lane_begin(const SimParams& p, const LaneSmem& m
 // One Gillespie step up to the flip (src/jit_kernels/simulation.cu:104-147): fixed point, step
 // cap, dt and window accumulation, end of time, pick and flip. Returns the flipped node or -1;
 // tr.status says whether the trajectory ended. Without `coop` the readers are updated here.
+template <bool SPLIT>
 __device__ __forceinline__ int lane_step_front(const SimParams& p, const LaneSmem& m, int T, int col, LaneTraj& tr,
                                                bool coop) {
     tr.status = TRAJ_CONTINUE;
@@ -515,7 +526,7 @@ __device__ __forceinline__ int lane_step_front(const SimParams& p, const LaneSme
     unsigned* st = m.st + col;
     // the tree's root (L a power of two) holds the total, which r never reaches: start below it
     const int top = 1 << (31 - __clz(L));
-    const int k = lane_pick(p, st, m.act + col, m.fen + col, T, G, m.shift, top == L ? top >> 1 : top,
+    const int k = lane_pick<SPLIT>(p, st, m.act + col, m.fen + col, T, G, m.shift, top == L ? top >> 1 : top,
                             pick_target(d.y, d.z, tr.total));
     if (k < 0 || k >= p.n) {
         tr.status = TRAJ_ERROR;
@@ -604,7 +615,7 @@ __device__ void sim_lane_body(const SimParams& p, unsigned char* smem) {
         }
         if (__all_sync(MBG_FULL, tr.done)) break;
         if (!COOP && !tr.have) continue;
-        const int k = tr.have ? lane_step_front(p, m, T, col, tr, COOP) : -1;
+        const int k = tr.have ? lane_step_front<false>(p, m, T, col, tr, COOP) : -1;
         if (COOP) {
             const unsigned touched =
                 lane_coop_update(p, [&](int) -> const SimParams& { return p; }, m, T, wbase, lane, k);
@@ -674,7 +685,7 @@ __device__ void sim_lane_batch_body(const BatchDesc& b, unsigned char* smem) {
         if (__all_sync(MBG_FULL, tr.done)) break;
         if (!COOP && !tr.have) continue;
         const SimParams& p = *pp;
-        const int k = tr.have ? lane_step_front(p, m, T, col, tr, COOP) : -1;
+        const int k = tr.have ? lane_step_front<true>(p, m, T, col, tr, COOP) : -1;
         if (COOP) {
             const unsigned touched = lane_coop_update(
                 p,

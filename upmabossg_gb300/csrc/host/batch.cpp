@@ -357,6 +357,7 @@ void Batch::autotune() {
     // and the second run's kernel time decides. Pilot runs write into the result buffers, which
     // the graph clears before every real run; a fixed-point buffer that fills up during the pilots
     // only sets an error bit in those buffers.
+    const bool log = std::getenv("MBG_AUTOTUNE_LOG") != nullptr;
     cudaStream_t s = capture_stream;
     for (size_t c = 0; c < classes.size(); ++c) {
         Class& k = classes[c];
@@ -384,6 +385,9 @@ void Batch::autotune() {
                         ck(cudaEventElapsedTime(&ms, ev0, ev1), "cudaEventElapsedTime");
                     }
                     k.timings.push_back(mbg_batch_class_timing{lay, blk, var, 0, (double)ms});
+                    if (log)
+                        std::fprintf(stderr, "mbg batch autotune: class max_n=%d layout=%d block=%d variant=%d kernel_ms=%.3f\n",
+                                     k.max_n, lay, blk, var, ms);
                     if (best < 0 || ms < best) {
                         best = ms;
                         best_lay = lay;
@@ -399,8 +403,19 @@ void Batch::autotune() {
             std::vector<mbg_batch_class_timing> order = k.timings;
             std::sort(order.begin(), order.end(),
                       [](const mbg_batch_class_timing& a, const mbg_batch_class_timing& b) { return a.kernel_ms < b.kernel_ms; });
+            // the three fastest within 15%, and the fastest of every (layout, variant) within 30%:
+            // a short pilot can misrank the reader-update variants
+            std::vector<size_t> pick;
+            for (size_t i = 0; i < order.size(); ++i) {
+                bool first_of_kind = true;
+                for (size_t j = 0; j < i; ++j)
+                    if (order[j].layout == order[i].layout && order[j].variant == order[i].variant) first_of_kind = false;
+                if ((i < 3 && order[i].kernel_ms <= 1.15 * order[0].kernel_ms) ||
+                    (first_of_kind && order[i].kernel_ms <= 1.3 * order[0].kernel_ms))
+                    pick.push_back(i);
+            }
             best = -1;
-            for (size_t i = 0; i < order.size() && i < 3 && order[i].kernel_ms <= 1.15 * order[0].kernel_ms; ++i) {
+            for (size_t i : pick) {
                 const mbg_batch_class_timing& t = order[i];
                 configure((int)c, t.layout, t.block_size, t.variant != 0);
                 float ms = 0.f;
@@ -410,6 +425,9 @@ void Batch::autotune() {
                 ck(cudaEventRecord(ev1, s), "cudaEventRecord");
                 ck(cudaStreamSynchronize(s), "autotune run");
                 ck(cudaEventElapsedTime(&ms, ev0, ev1), "cudaEventElapsedTime");
+                if (log)
+                    std::fprintf(stderr, "mbg batch autotune: class max_n=%d long pilot layout=%d block=%d variant=%d kernel_ms=%.3f\n",
+                                 k.max_n, t.layout, t.block_size, t.variant, ms);
                 if (best < 0 || ms < best) {
                     best = ms;
                     best_lay = t.layout;

@@ -333,8 +333,20 @@ void Sim::autotune() {
     if (pilot2 > pilot && timed.size() > 1) {
         std::sort(timed.begin(), timed.end(), [](const auto& a, const auto& b) { return a.first < b.first; });
         scope.p.n_traj = pilot2;
+        // the three fastest within 15%, and the fastest of every (layout, variant) within 30%: a
+        // short pilot can misrank the reader-update variants
+        std::vector<size_t> pick;
+        for (size_t i = 0; i < timed.size(); ++i) {
+            bool first_of_kind = true;
+            for (size_t j = 0; j < i; ++j)
+                if (timed[j].second.layout == timed[i].second.layout && timed[j].second.coop == timed[i].second.coop)
+                    first_of_kind = false;
+            if ((i < 3 && timed[i].first <= 1.15 * timed[0].first) ||
+                (first_of_kind && timed[i].first <= 1.3 * timed[0].first))
+                pick.push_back(i);
+        }
         best = -1;
-        for (size_t i = 0; i < timed.size() && i < 3 && timed[i].first <= 1.15 * timed[0].first; ++i) {
+        for (size_t i : pick) {
             const Shape& sh = timed[i].second;
             setup_layout(sh.layout, sh.block, sh.coop);
             run(nullptr);
