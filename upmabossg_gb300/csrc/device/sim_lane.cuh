@@ -254,19 +254,19 @@ __device__ __forceinline__ int lane_walk(const SimParams& p, const unsigned* st,
     unsigned aw = act[g * T];
     const unsigned sw = st[g * T];
     if (!p.has_palette) {
-        // the next four active nodes' rates are loaded together, then compared in node order
+        // the next eight active nodes' rates are loaded together, then compared in node order
         const unsigned long long* rates = &p.lnodes[g * 32].up;  // 4 words per LaneNode
         while (aw) {
-            int b[4];
-            unsigned long long v[4];
+            int b[8];
+            unsigned long long v[8];
 #pragma unroll
-            for (int u = 0; u < 4; ++u) {
+            for (int u = 0; u < 8; ++u) {
                 b[u] = aw ? __ffs(aw) - 1 : -1;
                 aw &= aw - 1u;
                 v[u] = b[u] >= 0 ? __ldg(rates + 4 * b[u] + ((sw >> (b[u] & 31)) & 1u)) : 0ull;
             }
 #pragma unroll
-            for (int u = 0; u < 4; ++u) {
+            for (int u = 0; u < 8; ++u) {
                 if (b[u] < 0) return -1;
                 if (r < v[u]) return g * 32 + b[u];
                 r -= v[u];
