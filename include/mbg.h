@@ -143,6 +143,12 @@ mbg_status mbg_model_with_rate_scales(const mbg_model* base, const double* up_sc
 mbg_status mbg_model_with_mutations(const mbg_model* base, const int32_t* nodes, const int32_t* values,
                                     int32_t count, mbg_model** out);
 
+/* Builds the model's device tables on the host and checks every index the kernels read from them
+ * (node, regulator and dependency ids, table, palette and side-record offsets) against the array
+ * it indexes; MBG_ERR_MODEL names the first one out of range. Needs no GPU; mbg_sim_create and
+ * mbg_batch_create run the same check before uploading. */
+mbg_status mbg_model_layout_check(const mbg_model* m);
+
 /* Generates the model's thread-per-trajectory kernel and compiles it with NVRTC for sm_103a
  * without loading it (needs no GPU). */
 mbg_status mbg_model_jit_check(const mbg_model* m, double* compile_ms);

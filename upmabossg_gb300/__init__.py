@@ -24,7 +24,7 @@ EXPORTS = (
     "mbg_last_error", "mbg_version", "mbg_device_count", "mbg_model_parse_files", "mbg_model_parse_strings",
     "mbg_model_destroy", "mbg_model_info_get", "mbg_model_node_name", "mbg_model_outputs", "mbg_model_rate",
     "mbg_model_with_rate_scales", "mbg_model_parse_files_overrides", "mbg_model_with_mutations",
-    "mbg_model_jit_check",
+    "mbg_model_jit_check", "mbg_model_layout_check",
     "mbg_sim_opts_default", "mbg_sim_create", "mbg_sim_destroy", "mbg_sim_run", "mbg_sim_summary",
     "mbg_sim_probtraj", "mbg_sim_probtraj_raw", "mbg_sim_final_states", "mbg_sim_fixed_points",
     "mbg_sim_trajectories", "mbg_write_probtraj_csv", "mbg_write_fp_csv", "mbg_print_results",
@@ -118,6 +118,7 @@ def lib():
             "mbg_model_outputs": (i32, [vp, dp, i32]),
             "mbg_model_rate": (ctypes.c_int, [vp, i32, dp, ctypes.POINTER(u64), ctypes.POINTER(ctypes.c_double)]),
             "mbg_model_jit_check": (ctypes.c_int, [vp, ctypes.POINTER(ctypes.c_double)]),
+            "mbg_model_layout_check": (ctypes.c_int, [vp]),
             "mbg_model_with_rate_scales": (ctypes.c_int, [vp, dp, dp, ctypes.POINTER(vp)]),
             "mbg_sim_opts_default": (None, [ctypes.POINTER(SimOpts)]),
             "mbg_sim_create": (ctypes.c_int, [vp, ctypes.POINTER(SimOpts), ctypes.POINTER(vp)]),
@@ -253,6 +254,10 @@ class Model:
         h = ctypes.c_void_p()
         _check(lib().mbg_model_with_mutations(self._h, _p(n), _p(w), len(idx), ctypes.byref(h)))
         return Model(h)
+
+    def layout_check(self):
+        """Checks the model's device tables on the host (raises MbgError on an index out of range)."""
+        _check(lib().mbg_model_layout_check(self._h))
 
     def jit_check(self) -> float:
         ms = ctypes.c_double()

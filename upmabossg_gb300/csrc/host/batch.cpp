@@ -130,6 +130,7 @@ void Batch::create(const std::vector<const CompiledModel*>& models, const std::v
         const CompiledModel& cm = x.cm;
         total_traj += x.n_traj;
         dls[i] = layout_model(cm);
+        check_layout(cm, dls[i]);
         const DeviceLayout& d = dls[i];
         Off& f = off[i];
         f.nodes = ml.add(d.nodes.size() * sizeof(DevNode));

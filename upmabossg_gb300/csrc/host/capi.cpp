@@ -230,6 +230,11 @@ mbg_status mbg_model_with_mutations(const mbg_model* base, const int32_t* nodes,
     return MBG_OK;
 }
 
+mbg_status mbg_model_layout_check(const mbg_model* m) {
+    if (!m) return fail(MBG_ERR_ARG, "null model");
+    return guard([&] { mbg::check_layout(m->cm, mbg::layout_model(m->cm)); });
+}
+
 mbg_status mbg_model_jit_check(const mbg_model* m, double* compile_ms) {
     if (!m) return fail(MBG_ERR_ARG, "null model");
     return guard([&] {

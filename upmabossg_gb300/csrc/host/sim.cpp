@@ -129,6 +129,57 @@ DeviceLayout layout_model(const CompiledModel& cm) {
     return d;
 }
 
+void check_layout(const CompiledModel& cm, const DeviceLayout& d) {
+    const uint32_t n = (uint32_t)cm.n;
+    auto need = [](bool ok, const char* what, uint32_t i) {
+        if (!ok) throw ModelError(std::string("device layout check: ") + what + " (node " + std::to_string(i) + ")");
+    };
+    need(d.nodes.size() == n && d.lnodes.size() == n && d.out_pos.size() == n && d.istate_thr.size() == n,
+         "per-node arrays sized to the model", 0);
+    need(d.dep_off.size() == n + 1 && d.dep_off[n] == d.deps.size(), "dependency offsets", n);
+    for (uint32_t i = 0; i < n; ++i) {
+        const DevNode& dn = d.nodes[i];
+        const LaneNode& ln = d.lnodes[i];
+        const uint32_t k = dn.k;
+        need(k == cm.nodes[i].regs.size() && ln.k == k, "regulator count", i);
+        need((uint64_t)dn.reg_off + k <= d.regs.size(), "regulator list inside regs", i);
+        for (uint32_t j = 0; j < k; ++j) need(d.regs[dn.reg_off + j] < n, "regulator id", i);
+        for (uint32_t j = 0; j < k && j < (uint32_t)kInlineRegs; ++j) need(dn.r[j] < n, "inline regulator id", i);
+        for (uint32_t j = 0; j < k && j < 4; ++j) need(ln.r[j] < n, "lane-record regulator id", i);
+        const uint64_t entries = 2ull << k;  // table assignments (self bit + k regulators)
+        if (dn.kind == NODE_BINARY) {
+            need((uint64_t)dn.tab_off + (entries + 31) / 32 <= d.tabs.size(), "truth table inside tabs", i);
+            need(ln.flags == 0u || ln.flags == kLaneWideTable || ln.flags == kLaneFar, "lane-record kind", i);
+            need((ln.flags == 0u) == (k <= 4), "lane-record inline table", i);
+            if (ln.flags == kLaneWideTable) {
+                need(k > 4 && k <= 12 && ln.table < d.lwide.size(), "side record index", i);
+                const LaneWide& w = d.lwide[ln.table];
+                for (uint32_t j = 4; j < k; ++j) need(w.r[j - 4] < n, "side-record regulator id", i);
+                if (k > 6) need((uint64_t)w.table[0] + (entries + 31) / 32 <= d.tabs.size(), "side-record table", i);
+            }
+        } else {
+            need(ln.flags == kLanePalette, "lane-record kind", i);
+            need((uint64_t)dn.tab_off + entries <= d.pidx.size(), "palette indices inside pidx", i);
+            const size_t np = cm.nodes[i].palette.size();
+            need((uint64_t)dn.pal_off + np <= d.palette.size(), "palette inside palette array", i);
+            for (uint64_t a = 0; a < entries; ++a) need(d.pidx[dn.tab_off + a] < np, "palette index", i);
+        }
+        need(d.dep_off[i] <= d.dep_off[i + 1], "dependency list order", i);
+        for (uint32_t q = d.dep_off[i]; q < d.dep_off[i + 1]; ++q) {
+            const uint32_t e = d.deps[q], dn_id = e >> 16, kd = (e >> 8) & 0x7fu, pos = e & 0xffu;
+            need(dn_id < n, "dependency entry node", i);
+            need(kd == d.nodes[dn_id].k, "dependency entry regulator count", i);
+            need(pos == 0xffu ? dn_id == i : (pos < kd && d.regs[d.nodes[dn_id].reg_off + pos] == i),
+                 "dependency entry position", i);
+            need(((e >> 15) & 1u) == (cm.out_pos[dn_id] >= 0 ? 1u : 0u), "dependency entry output flag", i);
+        }
+    }
+    need(d.out_nodes.size() == (size_t)cm.n_out, "output list", 0);
+    for (size_t q = 0; q < d.out_nodes.size(); ++q) {
+        need(d.out_nodes[q] < n && d.out_pos[d.out_nodes[q]] == (int16_t)q, "output node", (uint32_t)q);
+    }
+}
+
 void set_model_constants(SimParams& prm, const CompiledModel& cm) {
     prm.n = cm.n;
     prm.words = cm.words;
@@ -188,6 +239,7 @@ void Sim::create(const CompiledModel& model, const std::vector<std::string>& nod
     ck(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device), "cudaDeviceGetAttribute");
 
     dl = layout_model(cm);
+    check_layout(cm, dl);
     // model arrays
     std::memset(&prm, 0, sizeof prm);
     prm.nodes = upload(dl.nodes, owned);

@@ -38,6 +38,10 @@ struct DeviceLayout {
 };
 
 DeviceLayout layout_model(const CompiledModel& cm);
+// Checks every index the kernels read out of a layout against the array it indexes (node ids,
+// regulator ids, dependency entries, table, palette and side-record offsets); throws an Error
+// (ModelError) naming the first one out of range. Runs on the host before any upload.
+void check_layout(const CompiledModel& cm, const DeviceLayout& d);
 // Model-dependent SimParams fields (sizes, clock, rate scale).
 void set_model_constants(SimParams& prm, const CompiledModel& cm);
 // Throws if a run of n_traj trajectories of cm exceeds the result representation.
