@@ -14,21 +14,25 @@ cudaError_t launch_sim_warp(const SimParams& p, bool cached_index, int grid, int
 cudaError_t sim_warp_configure(bool cached_index, size_t smem);
 unsigned sim_warp_smem_per_warp(int n, bool cached_index);
 cudaError_t sim_warp_occupancy(bool cached_index, int block, size_t smem, int* blocks_per_sm);
-cudaError_t launch_sim_lane(const SimParams& p, bool coop, int grid, int block, size_t smem, cudaStream_t stream);
-cudaError_t sim_lane_configure(bool coop, size_t smem, int block, int* blocks_per_sm);
+// `full`: the model has multi-valued rates or nodes over more than 12 regulators (the `_full`
+// kernels); otherwise the kernels without those paths run.
+cudaError_t launch_sim_lane(const SimParams& p, bool coop, bool full, int grid, int block, size_t smem,
+                            cudaStream_t stream);
+cudaError_t sim_lane_configure(bool coop, bool full, size_t smem, int block, int* blocks_per_sm);
 // Dynamic shared memory of a lane-layout block (the same for both reader-update variants).
 size_t sim_lane_smem(int n, int block);
 int sim_lane_rows(int n);                 // BatchDesc::rows for models of up to n nodes
 // Re-applies the attributes of a simulation kernel for the launch shapes that are about to use it
 // (kernel 0: mbg_sim_lane[_coop], 1: mbg_sim_lane_batch[_coop], 2: mbg_sim_warp_batch[_gather],
-// 3: mbg_sim_warp[_gather]; variant selects the second name): kernel attributes are process-wide,
+// 3: mbg_sim_warp[_gather], 4: mbg_sim_lane[_coop]_full, 5: mbg_sim_lane_batch[_coop]_full;
+// variant selects the second name): kernel attributes are process-wide,
 // so another handle may have changed them since this one was configured.
 cudaError_t sim_kernel_limits(int kernel, bool variant, const int* blocks, const size_t* smems, const int* want,
                               int count);
 std::mutex& kernel_attr_mutex();
-cudaError_t launch_sim_lane_batch(const BatchDesc& b, bool coop, int grid, int block, size_t smem,
+cudaError_t launch_sim_lane_batch(const BatchDesc& b, bool coop, bool full, int grid, int block, size_t smem,
                                   cudaStream_t stream);
-cudaError_t sim_lane_batch_configure(bool coop, size_t smem, int block, int* blocks_per_sm);
+cudaError_t sim_lane_batch_configure(bool coop, bool full, size_t smem, int block, int* blocks_per_sm);
 cudaError_t launch_sim_warp_batch(const BatchDesc& b, bool cached_index, int grid, int block, size_t smem,
                                   cudaStream_t stream);
 cudaError_t sim_warp_batch_configure(bool cached_index, size_t smem, int block, int* blocks_per_sm);

@@ -135,7 +135,10 @@ __device__ __forceinline__ unsigned lane_wide_bit(const SimParams& p, uint4 rb, 
     return (word >> (a & 31u)) & 1u;
 }
 
-// Rate of node i in the state column st, evaluated from its tables.
+// Rate of node i in the state column st, evaluated from its tables. FULL: the model may have
+// multi-valued (palette) rates or nodes over more than 12 regulators; without them those paths
+// are left out of the kernel (a smaller loop body).
+template <bool FULL>
 __device__ __forceinline__ unsigned long long lane_eval(const SimParams& p, int i, const unsigned* st, int T) {
     const uint4* rec = reinterpret_cast<const uint4*>(p.lnodes + i);
     const uint4 ra = __ldg(rec), rb = __ldg(rec + 1);
@@ -148,15 +151,17 @@ __device__ __forceinline__ unsigned long long lane_eval(const SimParams& p, int 
         if (!on) return 0ull;
         return self ? (((unsigned long long)ra.w << 32) | ra.z) : (((unsigned long long)ra.y << 32) | ra.x);
     }
+    if (!FULL) return 0ull;
     const NodeHead h = load_head(p, i);
     return rate_at(p, i, h, self, lane_gather(p, i, h.k, st, T));
 }
 
 // Current rate of node i from its active bit (BINARY) or its table (PALETTE).
+template <bool FULL>
 __device__ __forceinline__ unsigned long long lane_rate(const SimParams& p, int i, const unsigned* st,
                                                         const unsigned* act, int T) {
     const unsigned self = col_bit(st, T, i);
-    if (p.has_palette && (__ldg(&p.lnodes[i].flags) & kLanePalette)) {
+    if (FULL && p.has_palette && (__ldg(&p.lnodes[i].flags) & kLanePalette)) {
         const NodeHead h = load_head(p, i);
         return palette_rate(p, h, self, lane_gather(p, i, h.k, st, T));
     }
@@ -173,11 +178,12 @@ __device__ __forceinline__ unsigned lane_out_index(const SimParams& p, const uns
 
 // Transition entropy over the output nodes (generator.cpp:146-175) from one pass:
 // -sum p log2 p = log2 R - (sum r log2 r) / R.
+template <bool FULL>
 __device__ __forceinline__ float lane_entropy(const SimParams& p, const unsigned* st, const unsigned* act, int T) {
     unsigned long long R = 0ull;
     float c = 0.f;
     for (int q = 0; q < p.n_out; ++q) {
-        const unsigned long long r = lane_rate(p, __ldg(p.out_nodes + q), st, act, T);
+        const unsigned long long r = lane_rate<FULL>(p, __ldg(p.out_nodes + q), st, act, T);
         if (r) {
             R += r;
             const float rr = u64_to_f32(r) * p.to_real;
@@ -192,6 +198,7 @@ __device__ __forceinline__ float lane_entropy(const SimParams& p, const unsigned
 // the sum of leaf 32 * chunk + l, a scan gives the prefixes, and tree entry
 // i = P(i) - P(i - lowbit(i)) (P(x) = sum of leaves < x) takes P(i - lowbit(i)) from this chunk
 // or, at a multiple of 32, from the chunk boundaries kept one per lane.
+template <bool FULL>
 __device__ __forceinline__ unsigned long long lane_coop_init(const SimParams& p, const LaneSmem& m, int T, int c,
                                                              unsigned long long traj, unsigned lane) {
     const int n = p.n, G = lane_groups(n);
@@ -226,7 +233,7 @@ __device__ __forceinline__ unsigned long long lane_coop_init(const SimParams& p,
                 const int g = ((ch * 32 + ll) << m.shift) + h;
                 if (g >= G) break;
                 const int i = g * 32 + (int)lane;
-                const unsigned long long vi = i < n ? lane_eval(p, i, st, T) : 0ull;
+                const unsigned long long vi = i < n ? lane_eval<FULL>(p, i, st, T) : 0ull;
                 const unsigned a = __ballot_sync(MBG_FULL, vi != 0ull);
                 if (lane == 0u) m.act[(size_t)g * T + c] = a;
                 v += vi;
@@ -249,11 +256,12 @@ __device__ __forceinline__ unsigned long long lane_coop_init(const SimParams& p,
 
 // Walks the active nodes of group g in node order: the first whose inclusive rate prefix exceeds
 // r, or -1 with r reduced by the group's total.
+template <bool FULL>
 __device__ __forceinline__ int lane_walk(const SimParams& p, const unsigned* st, const unsigned* act, int T, int g,
                                          unsigned long long& r) {
     unsigned aw = act[g * T];
     const unsigned sw = st[g * T];
-    if (!p.has_palette) {
+    if (!FULL || !p.has_palette) {
         // the next eight active nodes' rates are loaded together, then compared in node order
         const unsigned long long* rates = &p.lnodes[g * 32].up;  // 4 words per LaneNode
         while (aw) {
@@ -279,7 +287,7 @@ __device__ __forceinline__ int lane_walk(const SimParams& p, const unsigned* st,
         aw &= aw - 1u;
         const int i = g * 32 + b;
         const unsigned long long v =
-            p.has_palette ? lane_rate(p, i, st, act, T) : __ldg(&p.lnodes[i].up + ((sw >> b) & 1u));
+            p.has_palette ? lane_rate<FULL>(p, i, st, act, T) : __ldg(&p.lnodes[i].up + ((sw >> b) & 1u));
         if (r < v) return i;
         r -= v;
     }
@@ -290,7 +298,7 @@ __device__ __forceinline__ int lane_walk(const SimParams& p, const unsigned* st,
 // then its groups in turn. SPLIT writes the two walks of a two-group leaf out separately instead
 // of as a loop: the same result, different code; which one runs faster depends on the kernel it
 // is compiled into (measured per kernel).
-template <bool SPLIT>
+template <bool SPLIT, bool FULL>
 __device__ __forceinline__ int lane_pick(const SimParams& p, const unsigned* st, const unsigned* act,
                                          const unsigned long long* fen, int T, int G, int shift, int top,
                                          unsigned long long r) {
@@ -298,14 +306,14 @@ __device__ __forceinline__ int lane_pick(const SimParams& p, const unsigned* st,
     if (SPLIT) {
         const int g = l << shift;
         if (g >= G) return -1;
-        const int k = lane_walk(p, st, act, T, g, r);
+        const int k = lane_walk<FULL>(p, st, act, T, g, r);
         if (k >= 0 || shift == 0 || g + 1 >= G) return k;
-        return lane_walk(p, st, act, T, g + 1, r);
+        return lane_walk<FULL>(p, st, act, T, g + 1, r);
     }
     for (int h = 0; h < (1 << shift); ++h) {
         const int g = (l << shift) + h;
         if (g >= G) return -1;
-        const int k = lane_walk(p, st, act, T, g, r);
+        const int k = lane_walk<FULL>(p, st, act, T, g, r);
         if (k >= 0) return k;
     }
     return -1;
@@ -317,7 +325,7 @@ __device__ __forceinline__ int lane_pick(const SimParams& p, const unsigned* st,
 // Patches the active bits and the Fenwick tree (with shared-memory atomics when several lanes may
 // patch the same trajectory), returns the rate change and sets `out` when dn is an output node
 // whose rate changed.
-template <bool ATOMIC>
+template <bool ATOMIC, bool FULL>
 __device__ __forceinline__ unsigned long long lane_reader_rec(const SimParams& p, unsigned e, uint4 ra, uint4 rb,
                                                               const LaneSmem& m, int T, int col, bool& out) {
     const int dn = (int)(e >> 16);
@@ -329,11 +337,11 @@ __device__ __forceinline__ unsigned long long lane_reader_rec(const SimParams& p
     const unsigned flags = rb.w >> 16;
     unsigned long long r_new, r_old;
     unsigned a_new, a_old;
-    if (!(flags & kLanePalette)) {
+    if (!FULL || !(flags & kLanePalette)) {
         if (flags == 0u) {
             // up to 4 regulators and their table in the record itself
             a_new = (rb.x >> ((self << kd) | lane_idx4(st, T, kd, rb.y, rb.z))) & 1u;
-        } else if (flags == kLaneWideTable) {
+        } else if (!FULL || flags == kLaneWideTable) {
             a_new = lane_wide_bit(p, rb, kd, self, st, T);
         } else {
             a_new = table_bit(p, dn, kd, self, lane_gather(p, dn, kd, st, T));
@@ -369,15 +377,16 @@ __device__ __forceinline__ unsigned long long lane_reader_rec(const SimParams& p
     return delta;
 }
 
-template <bool ATOMIC>
+template <bool ATOMIC, bool FULL>
 __device__ __forceinline__ unsigned long long lane_reader(const SimParams& p, unsigned e, const LaneSmem& m, int T,
                                                           int col, bool& out) {
     const uint4* rec = reinterpret_cast<const uint4*>(p.lnodes + (e >> 16));
-    return lane_reader_rec<ATOMIC>(p, e, __ldg(rec), __ldg(rec + 1), m, T, col, out);
+    return lane_reader_rec<ATOMIC, FULL>(p, e, __ldg(rec), __ldg(rec + 1), m, T, col, out);
 }
 
 // After node k flipped in this lane's trajectory: re-evaluates every node whose rate reads k (and
 // k itself) in turn. Returns whether an output node's rate changed.
+template <bool FULL>
 __device__ __forceinline__ bool lane_update(const SimParams& p, int k, const LaneSmem& m, int T, int col,
                                             unsigned long long& total) {
     const int d0 = (int)__ldg(p.dep_off + k), d1 = (int)__ldg(p.dep_off + k + 1);
@@ -394,7 +403,7 @@ __device__ __forceinline__ bool lane_update(const SimParams& p, int k, const Lan
             ra2 = __ldg(reinterpret_cast<const uint4*>(p.lnodes + (e2 >> 16)));
             rb2 = __ldg(reinterpret_cast<const uint4*>(p.lnodes + (e2 >> 16)) + 1);
         }
-        total += lane_reader_rec<false>(p, e, ra, rb, m, T, col, out);
+        total += lane_reader_rec<false, FULL>(p, e, ra, rb, m, T, col, out);
         e = e2;
         ra = ra2;
         rb = rb2;
@@ -408,7 +417,7 @@ __device__ __forceinline__ bool lane_update(const SimParams& p, int k, const Lan
 // patch its shared-memory rows with atomics. Returns (on every lane) the mask of lanes whose
 // output-node rates changed. `owner(o)` gives the model of lane o's trajectory (called by all
 // lanes).
-template <class Owner>
+template <bool FULL, class Owner>
 __device__ __forceinline__ unsigned lane_coop_update(const SimParams& mine, Owner owner, const LaneSmem& m, int T,
                                                  int wbase, unsigned lane, int k) {
     int d0 = 0, c = 0;
@@ -439,7 +448,7 @@ __device__ __forceinline__ unsigned lane_coop_update(const SimParams& mine, Owne
         const int o_d0 = __shfl_sync(MBG_FULL, d0, o);
         const SimParams& po = owner(o);
         bool out = false;
-        if (q < C) lane_reader<true>(po, __ldg(po.deps + o_d0 + (q - o_ex)), m, T, wbase + o, out);
+        if (q < C) lane_reader<true, FULL>(po, __ldg(po.deps + o_d0 + (q - o_ex)), m, T, wbase + o, out);
         touched |= __reduce_or_sync(MBG_FULL, out ? 1u << o : 0u);
     }
     __syncwarp();  // every patch is visible to its trajectory's lane
@@ -484,20 +493,21 @@ struct LaneCounts {
 };
 
 // A new trajectory's registers once its state is set up.
+template <bool FULL>
 __device__ __forceinline__ void lane_begin(const SimParams& p, const LaneSmem& m, int T, int col, LaneTraj& tr) {
     tr.have = true;
     tr.t = 0;
     tr.step = 0;
     tr.trans = 0;
     tr.so = lane_out_index(p, m.st + col, T);
-    tr.h = lane_entropy(p, m.st + col, m.act + col, T);
+    tr.h = lane_entropy<FULL>(p, m.st + col, m.act + col, T);
     win_begin(tr.acc, p, tr.so);
 }
 
 // One Gillespie step up to the flip (src/jit_kernels/simulation.cu:104-147): fixed point, step
 // cap, dt and window accumulation, end of time, pick and flip. Returns the flipped node or -1;
 // tr.status says whether the trajectory ended. Without `coop` the readers are updated here.
-template <bool SPLIT>
+template <bool SPLIT, bool FULL>
 __device__ __forceinline__ int lane_step_front(const SimParams& p, const LaneSmem& m, int T, int col, LaneTraj& tr,
                                                bool coop) {
     tr.status = TRAJ_CONTINUE;
@@ -526,7 +536,7 @@ __device__ __forceinline__ int lane_step_front(const SimParams& p, const LaneSme
     unsigned* st = m.st + col;
     // the tree's root (L a power of two) holds the total, which r never reaches: start below it
     const int top = 1 << (31 - __clz(L));
-    const int k = lane_pick<SPLIT>(p, st, m.act + col, m.fen + col, T, G, m.shift, top == L ? top >> 1 : top,
+    const int k = lane_pick<SPLIT, FULL>(p, st, m.act + col, m.fen + col, T, G, m.shift, top == L ? top >> 1 : top,
                             pick_target(d.y, d.z, tr.total));
     if (k < 0 || k >= p.n) {
         tr.status = TRAJ_ERROR;
@@ -534,16 +544,17 @@ __device__ __forceinline__ int lane_step_front(const SimParams& p, const LaneSme
         return -1;
     }
     st[(k >> 5) * T] ^= 1u << (k & 31);
-    if (!coop && lane_update(p, k, m, T, col, tr.total)) tr.h = lane_entropy(p, st, m.act + col, T);
+    if (!coop && lane_update<FULL>(p, k, m, T, col, tr.total)) tr.h = lane_entropy<FULL>(p, st, m.act + col, T);
     return k;
 }
 
 // After the readers of k were updated cooperatively: the new total from the tree, the entropy
 // when an output node's rate changed.
+template <bool FULL>
 __device__ __forceinline__ void lane_after_coop(const SimParams& p, const LaneSmem& m, int T, int col,
                                                 unsigned touched, unsigned lane, LaneTraj& tr) {
     tr.total = fen_total(m.fen + col, T, lane_leaves(lane_groups(p.n), m.shift));
-    if ((touched >> lane) & 1u) tr.h = lane_entropy(p, m.st + col, m.act + col, T);
+    if ((touched >> lane) & 1u) tr.h = lane_entropy<FULL>(p, m.st + col, m.act + col, T);
 }
 
 // Completes the step: output state, clock, transition count; at the end of the trajectory its
@@ -581,7 +592,7 @@ __device__ __forceinline__ void lane_step_back(const SimParams& p, const LaneSme
 }
 
 // One simulation: lanes take trajectory ids from the run's work counter.
-template <bool COOP>
+template <bool COOP, bool FULL>
 __device__ void sim_lane_body(const SimParams& p, unsigned char* smem) {
     const int T = (int)blockDim.x;
     const unsigned lane = threadIdx.x & 31u;
@@ -608,18 +619,18 @@ __device__ void sim_lane_body(const SimParams& p, unsigned char* smem) {
                 const int L = __ffs(init) - 1;
                 init &= init - 1u;
                 const unsigned long long jl = __shfl_sync(MBG_FULL, tr.j, L);
-                const unsigned long long tot = lane_coop_init(p, m, T, wbase + L, p.traj_base + jl, lane);
+                const unsigned long long tot = lane_coop_init<FULL>(p, m, T, wbase + L, p.traj_base + jl, lane);
                 if ((int)lane == L) tr.total = tot;
             }
-            if (start) lane_begin(p, m, T, col, tr);
+            if (start) lane_begin<FULL>(p, m, T, col, tr);
         }
         if (__all_sync(MBG_FULL, tr.done)) break;
         if (!COOP && !tr.have) continue;
-        const int k = tr.have ? lane_step_front<false>(p, m, T, col, tr, COOP) : -1;
+        const int k = tr.have ? lane_step_front<false, FULL>(p, m, T, col, tr, COOP) : -1;
         if (COOP) {
             const unsigned touched =
-                lane_coop_update(p, [&](int) -> const SimParams& { return p; }, m, T, wbase, lane, k);
-            if (k >= 0) lane_after_coop(p, m, T, col, touched, lane, tr);
+                lane_coop_update<FULL>(p, [&](int) -> const SimParams& { return p; }, m, T, wbase, lane, k);
+            if (k >= 0) lane_after_coop<FULL>(p, m, T, col, touched, lane, tr);
         }
         if (tr.have) lane_step_back(p, m, T, col, tr, k, c);
     }
@@ -630,7 +641,7 @@ __device__ void sim_lane_body(const SimParams& p, unsigned char* smem) {
 // instances' trajectory counts; each lane runs its item with its instance's model and adds its
 // counts to that instance's counters when it moves to another instance. Shared memory has rows
 // for the largest instance of the launch (b.rows groups).
-template <bool COOP>
+template <bool COOP, bool FULL>
 __device__ void sim_lane_batch_body(const BatchDesc& b, unsigned char* smem) {
     const int T = (int)blockDim.x;
     const unsigned lane = threadIdx.x & 31u;
@@ -677,24 +688,24 @@ __device__ void sim_lane_batch_body(const BatchDesc& b, unsigned char* smem) {
                 const SimParams* pl = reinterpret_cast<const SimParams*>(
                     __shfl_sync(MBG_FULL, reinterpret_cast<unsigned long long>(pp), L));
                 const unsigned long long jl = __shfl_sync(MBG_FULL, tr.j, L);
-                const unsigned long long tot = lane_coop_init(*pl, m, T, wbase + L, pl->traj_base + jl, lane);
+                const unsigned long long tot = lane_coop_init<FULL>(*pl, m, T, wbase + L, pl->traj_base + jl, lane);
                 if ((int)lane == L) tr.total = tot;
             }
-            if (start) lane_begin(*pp, m, T, col, tr);
+            if (start) lane_begin<FULL>(*pp, m, T, col, tr);
         }
         if (__all_sync(MBG_FULL, tr.done)) break;
         if (!COOP && !tr.have) continue;
         const SimParams& p = *pp;
-        const int k = tr.have ? lane_step_front<true>(p, m, T, col, tr, COOP) : -1;
+        const int k = tr.have ? lane_step_front<true, FULL>(p, m, T, col, tr, COOP) : -1;
         if (COOP) {
-            const unsigned touched = lane_coop_update(
+            const unsigned touched = lane_coop_update<FULL>(
                 p,
                 [&](int o) -> const SimParams& {
                     return *reinterpret_cast<const SimParams*>(
                         __shfl_sync(MBG_FULL, reinterpret_cast<unsigned long long>(pp), o));
                 },
                 m, T, wbase, lane, k);
-            if (k >= 0) lane_after_coop(p, m, T, col, touched, lane, tr);
+            if (k >= 0) lane_after_coop<FULL>(p, m, T, col, touched, lane, tr);
         }
         if (tr.have) lane_step_back(p, m, T, col, tr, k, c);
     }

@@ -105,6 +105,8 @@ void Batch::create(const std::vector<const CompiledModel*>& models, const std::v
         Class& k = all[batch_size_class(x.cm.n)];
         k.members.push_back((int)i);
         k.max_n = std::max(k.max_n, x.cm.n);
+        for (const auto& nd : x.cm.nodes) k.full |= nd.kind == NODE_PALETTE;
+        k.full |= x.cm.max_k > 12;
         k.traj += x.n_traj;
     }
     for (Class& k : all)
@@ -299,7 +301,7 @@ void Batch::configure(int c, int lay, int blk, bool variant) {
     if (lay == MBG_LAYOUT_LANE) {
         sm = sim_lane_smem(k.max_n, blk);
         if (sm > kSmemLimit) throw ModelError("largest instance of a size class too large for the batched lane layout");
-        ck(sim_lane_batch_configure(variant, sm, blk, &bps), "batched lane kernel occupancy");
+        ck(sim_lane_batch_configure(variant, k.full, sm, blk, &bps), "batched lane kernel occupancy");
     } else {
         const unsigned slice = sim_warp_batch_slice_bytes(k.max_n, variant);
         sm = (size_t)(blk / 32) * slice;
@@ -317,7 +319,7 @@ void Batch::configure(int c, int lay, int blk, bool variant) {
 }
 
 cudaError_t Batch::launch_class(const Class& k, const BatchDesc& d, cudaStream_t s) const {
-    if (k.layout == MBG_LAYOUT_LANE) return launch_sim_lane_batch(d, k.variant, k.grid, k.block, k.smem, s);
+    if (k.layout == MBG_LAYOUT_LANE) return launch_sim_lane_batch(d, k.variant, k.full, k.grid, k.block, k.smem, s);
     return launch_sim_warp_batch(d, k.variant, k.grid, k.block, k.smem, s);
 }
 
@@ -447,12 +449,12 @@ void Batch::apply_limits() {
     // classes that share a kernel need its largest shared-memory size and a carve-out that keeps
     // every class's resident blocks; kernel attributes are process-wide, so they are re-applied
     // before each launch of the graph
-    for (int kern : {1, 2}) {
+    for (int kern : {1, 2, 5}) {
         for (int var = 0; var < 2; ++var) {
             std::vector<int> blocks, want;
             std::vector<size_t> smems;
             for (const Class& k : classes) {
-                if ((k.layout == MBG_LAYOUT_LANE ? 1 : 2) != kern || (int)k.variant != var) continue;
+                if ((k.layout == MBG_LAYOUT_LANE ? (k.full ? 5 : 1) : 2) != kern || (int)k.variant != var) continue;
                 blocks.push_back(k.block);
                 smems.push_back(k.smem);
                 want.push_back(std::max(1, k.grid / std::max(1, sms)));

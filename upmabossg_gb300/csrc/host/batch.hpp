@@ -32,6 +32,7 @@ public:
     // Instances of one size class and the launch that runs them.
     struct Class {
         int max_n = 0;                      // nodes of the largest member
+        bool full = false;                  // a member has palette rates or nodes over 12 regulators
         std::vector<int> members;           // instance indices, ascending
         uint64_t traj = 0;                  // trajectories of all members
         size_t first = 0;                   // position of the first member in the class-ordered arrays

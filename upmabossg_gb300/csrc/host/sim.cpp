@@ -255,6 +255,7 @@ void Sim::create(const CompiledModel& model, const std::vector<std::string>& nod
     prm.out_pos = upload(dl.out_pos, owned);
     prm.istate_thr = upload(dl.istate_thr, owned);
     set_model_constants(prm, cm);
+    lane_full = prm.has_palette || cm.max_k > 12;
     prm.max_steps = o.max_steps ? o.max_steps : 0xFFFFFFFFu;
     prm.seed = seed;
     prm.n_traj = n_traj;
@@ -434,7 +435,7 @@ void Sim::setup_layout(int lay, int blk, bool coop) {
     } else if (layout == MBG_LAYOUT_LANE) {
         smem = sim_lane_smem(cm.n, block);
         if (smem > 227 * 1024) throw ModelError("model too large for the lane layout's shared memory at this block size");
-        ck(sim_lane_configure(lane_coop, smem, block, &bps), "configuring mbg_sim_lane");
+        ck(sim_lane_configure(lane_coop, lane_full, smem, block, &bps), "configuring mbg_sim_lane");
     } else {
         // keep every node's regulator index in shared memory while a block's share stays small
         // enough for several resident blocks per SM; otherwise re-gather it on each update
@@ -475,8 +476,8 @@ void Sim::run(cudaStream_t stream) {
         std::lock_guard<std::mutex> lock(kernel_attr_mutex());
         const int want = std::max(1, grid / std::max(1, sms));
         if (layout == MBG_LAYOUT_LANE) {
-            ck(sim_kernel_limits(0, lane_coop, &block, &smem, &want, 1), "mbg_sim_lane attributes");
-            ck(launch_sim_lane(prm, lane_coop, grid, block, smem, stream), "launch mbg_sim_lane");
+            ck(sim_kernel_limits(lane_full ? 4 : 0, lane_coop, &block, &smem, &want, 1), "mbg_sim_lane attributes");
+            ck(launch_sim_lane(prm, lane_coop, lane_full, grid, block, smem, stream), "launch mbg_sim_lane");
         } else {
             ck(sim_kernel_limits(3, cached_index, &block, &smem, &want, 1), "mbg_sim_warp attributes");
             ck(launch_sim_warp(prm, cached_index, grid, block, smem, stream), "launch mbg_sim_warp");

@@ -37,6 +37,7 @@ public:
     size_t smem = 0;
     bool cached_index = false;
     bool lane_coop = true;
+    bool lane_full = false;  // palette rates or nodes over 12 regulators: the `_full` lane kernels
     double jit_ms = 0;
     void* thread_kernel = nullptr;
     DeviceLayout dl;
