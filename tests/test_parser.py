@@ -3,6 +3,7 @@ driver.cpp, expressions.cpp), checked through the compiled per-node rate tables.
 import itertools
 import math
 
+import numpy as np
 import pytest
 
 import upmabossg_gb300 as mbg
@@ -165,3 +166,65 @@ def test_fixed_point_rate_quantisation():
     q, r = m.rate(0, (0,))
     F = m.info.frac_bits
     assert r == 0.123456 and q == round(math.ldexp(0.123456, F))
+
+
+class _Gen:
+    """Random rate expressions over nodes A..E mixing logic, comparisons, arithmetic on node
+    values and ternaries, as text and as a Python function of the node values (the grammar's
+    double semantics: logical operators and comparisons give 1.0 or 0.0)."""
+
+    NAMES = ("A", "B", "C", "D", "E")
+
+    def __init__(self, rng):
+        self.rng = rng
+
+    def expr(self, depth):
+        r = self.rng
+        if depth == 0 or r.random() < 0.2:
+            if r.random() < 0.7:
+                i = int(r.integers(0, len(self.NAMES)))
+                return self.NAMES[i], (lambda s, i=i: float(s[i]))
+            c = float(r.choice([0.0, 1.0, 0.5, 2.0, 3.25]))
+            return repr(c), (lambda s, c=c: c)
+        kind = int(r.integers(0, 5))
+        a, fa = self.expr(depth - 1)
+        if kind == 0:  # NOT
+            return f"!({a})", (lambda s, fa=fa: 1.0 if fa(s) == 0 else 0.0)
+        b, fb = self.expr(depth - 1)
+        if kind == 1:
+            op = str(r.choice(["&", "|", "^"]))
+            f = {"&": lambda x, y: x != 0 and y != 0, "|": lambda x, y: x != 0 or y != 0,
+                 "^": lambda x, y: (x != 0) != (y != 0)}[op]
+            return f"({a} {op} {b})", (lambda s, fa=fa, fb=fb, f=f: 1.0 if f(fa(s), fb(s)) else 0.0)
+        if kind == 2:
+            op = str(r.choice(["<", "<=", ">", ">=", "==", "!="]))
+            f = {"<": lambda x, y: x < y, "<=": lambda x, y: x <= y, ">": lambda x, y: x > y,
+                 ">=": lambda x, y: x >= y, "==": lambda x, y: x == y, "!=": lambda x, y: x != y}[op]
+            return f"({a} {op} {b})", (lambda s, fa=fa, fb=fb, f=f: 1.0 if f(fa(s), fb(s)) else 0.0)
+        if kind == 3:
+            op = str(r.choice(["+", "-", "*"]))
+            f = {"+": lambda x, y: x + y, "-": lambda x, y: x - y, "*": lambda x, y: x * y}[op]
+            return f"({a} {op} {b})", (lambda s, fa=fa, fb=fb, f=f: f(fa(s), fb(s)))
+        c, fc = self.expr(depth - 1)
+        return f"({a} ? {b} : {c})", (lambda s, fa=fa, fb=fb, fc=fc: fb(s) if fa(s) != 0 else fc(s))
+
+
+@pytest.mark.parametrize("seed", range(12))
+def test_random_expressions_tabulate_exactly(seed):
+    """Every node's rate table, built 64 assignments at a time, equals a direct evaluation of its
+    rate expressions (squared plus a constant, so that every rate is positive and finite) for every
+    state of the model, value for value."""
+    g = _Gen(np.random.default_rng(seed))
+    blocks, funcs = [], []
+    for name in g.NAMES:
+        up, fu = g.expr(4)
+        down, fd = g.expr(4)
+        blocks.append(node_block(name, "A", up=f"({up}) * ({up}) + 0.25", down=f"({down}) * ({down}) / 2 + 0.125"))
+        funcs.append((fu, fd))
+    m = mbg.Model.from_strings("".join(blocks), "")
+    n = len(g.NAMES)
+    for i in range(n):
+        fu, fd = funcs[i]
+        for bits in itertools.product((0, 1), repeat=n):
+            want = fd(bits) * fd(bits) / 2 + 0.125 if bits[i] else fu(bits) * fu(bits) + 0.25
+            assert m.rate(i, bits)[1] == want, (i, bits)
