@@ -170,6 +170,15 @@ def test_cli_mutants_overrides_and_final_states(tmp_path):
     sim.write_csv(lib_prefix, final_states=True)
     for suffix in ("_probtraj.csv", "_fp.csv", "_final_states.csv"):
         assert open(prefix + suffix).read() == open(lib_prefix + suffix).read(), suffix
-    bad = subprocess.run([mbg.CLI_PATH, str(tmp_path / "m.bnd"), str(tmp_path / "m.cfg")], capture_output=True,
-                         text=True, env=dict(os.environ, MBG_MUTANTS="Q:ON"), timeout=600)
-    assert bad.returncode == 1 and "MBG_MUTANTS" in bad.stderr
+
+
+def test_cli_rejects_bad_mutant_and_override_specs(tmp_path):
+    """Both are read before any device work: an unknown node or value, or an override that does not
+    parse, ends the run with status 1 and a message."""
+    (tmp_path / "m.bnd").write_text(_bnd())
+    (tmp_path / "m.cfg").write_text(_cfg())
+    args = [mbg.CLI_PATH, str(tmp_path / "m.bnd"), str(tmp_path / "m.cfg")]
+    for env, text in (({"MBG_MUTANTS": "Q:ON"}, "MBG_MUTANTS"), ({"MBG_MUTANTS": "A:UP"}, "MBG_MUTANTS"),
+                      ({"MBG_CONFIG_EXPR": "$ka = ;"}, "<overrides>")):
+        r = subprocess.run(args, capture_output=True, text=True, env=dict(os.environ, **env), timeout=600)
+        assert r.returncode == 1 and text in r.stderr, (env, r.stderr)
