@@ -2,7 +2,7 @@
 // master weights) mapping a sweep point's parameters to an output-state distribution. Training
 // (softmax cross-entropy against simulated distributions, Adam) and inference run on the project's
 // own kernels (device/mlp.cu). The reference has no surrogate; this is an addition on top of the
-// simulator, which stays the judge: every point a screen reports is re-simulated.
+// simulator, which has the last word: every point a screen reports is re-simulated.
 #include "surrogate.hpp"
 
 #include <cmath>

@@ -5,7 +5,7 @@ outcome is the output-state distribution of the final window. The plain method s
 point with the batch engine. The screened method trains an ensemble of MLPs (mbg_surrogate_*) on
 simulated points, predicts every candidate, reports the candidates that meet the screening
 criterion, and re-simulates every reported point plus every point whose ensemble spread exceeds
-a threshold; the simulator stays the judge of every reported point, and the total-variation error
+a threshold; the simulator has the last word on every reported point, and the total-variation error
 of the surrogate against those re-simulations is reported.
 """
 from __future__ import annotations
