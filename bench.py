@@ -102,9 +102,13 @@ class Clocks:
 MBG_LAYOUTS = {"thread": 1, "warp": 2, "lane": 3}
 
 
+PROFILE_KEYS = ("traffic_bytes_per_launch", "issue_slot_utilisation", "warp_instructions_per_transition",
+                "threads_per_warp_instruction")
+
+
 def profile_figures(kernel, workload):
     """Figures of the committed ncu summary profiles/<kernel>_<workload>.md: its `key: value`
-    lines (traffic_bytes_per_launch, issue_slot_utilisation)."""
+    lines (PROFILE_KEYS)."""
     path = os.path.join(ROOT, "profiles", f"{kernel}_{workload}.md")
     out = {}
     if not os.path.exists(path):
@@ -113,7 +117,7 @@ def profile_figures(kernel, workload):
     with open(path) as f:
         for line in f:
             key, sep, val = line.strip().strip("`").partition(": ")
-            if sep and key in ("traffic_bytes_per_launch", "issue_slot_utilisation"):
+            if sep and key in PROFILE_KEYS:
                 try:
                     out[key] = float(val) if "." in val else int(val)
                 except ValueError:
@@ -142,6 +146,29 @@ def model_work_per_transition(net, info):
     return total + 2 * info.nodes + 4 * info.outputs + 40
 
 
+def issue_roofline(prof, transitions_per_s, peaks, peaks_kind, sms=152):
+    """Instruction-issue roofline of a simulation kernel: warp instructions per transition (from
+    the committed ncu summary of the kernel on this workload) x transitions/s, against the issue
+    peak of one warp instruction per scheduler per clock (sms x 4 x clock). `thread_frac` scales
+    that by the threads active per warp instruction / 32 (the SIMT lanes doing useful work)."""
+    clock = peaks.get("sm_max_mhz", 2070.0) * 1e6
+    peak = sms * 4 * clock
+    out = {"bound": "issue", "unit": "G warp-instructions/s", "peak": peak / 1e9,
+           "peak_source": f"{sms} SMs x 4 schedulers x {clock / 1e6:.0f} MHz ({peaks_kind} sm_max_mhz)",
+           "issue_slot_utilisation_ncu": prof.get("issue_slot_utilisation")}
+    wpt = prof.get("warp_instructions_per_transition")
+    if wpt:
+        achieved = wpt * transitions_per_s
+        out.update({"achieved": achieved / 1e9, "frac": achieved / peak,
+                    "warp_instructions_per_transition": wpt})
+        tpw = prof.get("threads_per_warp_instruction")
+        if tpw:
+            out.update({"threads_per_warp_instruction": tpw, "thread_frac": achieved / peak * tpw / 32.0})
+    else:
+        out.update({"achieved": None, "frac": None})
+    return out
+
+
 def make_network(name):
     from upmabossg_gb300 import synth
     return getattr(synth, name)()
@@ -166,15 +193,13 @@ def run_reference(args):
     if rank != 0:
         return 0
     import oracle  # noqa: F401
-    net = make_network(args.workload)
+    net = make_network(args.workload)  # the workload's text only: libmbg.so is never loaded here
     bnd, cfg = net.bnd(), net.cfg()
-    import upmabossg_gb300 as mbg
-    model = mbg.Model.from_strings(bnd, cfg)  # host-side parse only: the fixed-point scale
     vals, ms = [], []
     last = None
     for i in range(args.warmup + args.steps):
         t0 = time.perf_counter()
-        last = cpu_reference(net, bnd, cfg, model.info.frac_bits, args.cpu_seconds / 2)
+        last = cpu_reference(net, bnd, cfg, 0, args.cpu_seconds / 2)  # 0: the oracle derives the scale
         if i >= args.warmup:
             vals.append(last["value"])
             ms.append((time.perf_counter() - t0) * 1e3)
@@ -395,15 +420,22 @@ def run_ours(args):
 
     peaks, peaks_kind = load_peaks()
     info = model.info
-    w_tr = model_work_per_transition(net, info)
-    sms = 152
-    clock = peaks.get("sm_max_mhz", 2070.0) * 1e6
-    peak_ops = sms * 128 * clock
     kms = sum(kernel_ms) / len(kernel_ms)
-    achieved = trans_step * w_tr / (kms * 1e-3)
     kernel = {MBG_LAYOUTS["thread"]: "mbg_sim_thread", MBG_LAYOUTS["warp"]: "mbg_sim_warp",
               MBG_LAYOUTS["lane"]: "mbg_sim_lane" if summary.get("lane_update") else "mbg_sim_lane_coop"}[summary["layout"]]
     prof = profile_figures(kernel, args.workload)
+    roofline = issue_roofline(prof, trans_step / (kms * 1e-3), peaks, peaks_kind)
+    # the reference algorithm's work (every rate re-evaluated, summed and scanned per transition)
+    # at this rate, against the SIMT lane peak: a work rate, not a roofline of the kernel that ran
+    w_tr = model_work_per_transition(net, info)
+    lane_peak = 152 * 128 * peaks.get("sm_max_mhz", 2070.0) * 1e6
+    roofline.update({"kernel": kernel, "kernel_ms": kms, "traffic": prof.get("traffic_bytes_per_launch"),
+                     "traffic_unit": "bytes per launch (ncu dram__bytes_read.sum + dram__bytes_write.sum)",
+                     "profile": prof.get("file"),
+                     "reference_work_rate": {
+                         "ops_per_transition": w_tr, "gops": trans_step * w_tr / (kms * 1e-3) / 1e9,
+                         "simt_lane_peak_gops": lane_peak / 1e9,
+                         "ratio_to_lane_peak": trans_step * w_tr / (kms * 1e-3) / lane_peak}})
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu:
         cpu = cpu_reference(net, bnd, cfg, info.frac_bits, args.cpu_seconds)
@@ -421,12 +453,7 @@ def run_ours(args):
                 "d2h_bytes_per_step": d2h, "ms_per_step": e2e_step_ms,
                 "path": "mbg_model_parse_strings + mbg_sim_create + mbg_sim_run + probtraj/final/fixed-point reads"},
         "gpu_launches": 3 * args.steps,
-        "roofline": {"bound": "issue", "achieved": achieved / 1e9, "peak": peak_ops / 1e9, "unit": "Gop/s",
-                     "frac": achieved / peak_ops, "traffic": prof.get("traffic_bytes_per_launch"),
-                     "kernel": kernel, "kernel_ms": kms, "ops_per_transition": w_tr,
-                     "issue_slot_utilisation_ncu": prof.get("issue_slot_utilisation"),
-                     "profile": prof.get("file"),
-                     "peak_source": f"152 SMs x 128 lanes x {clock / 1e6:.0f} MHz ({peaks_kind} sm_max_mhz)"},
+        "roofline": roofline,
         "cpu_baseline": cpu,
         "clocks": clocks,
         "summary": {k: summary[k] for k in ("transitions", "fixed_points", "finished", "errors", "fixed_point_states")},

@@ -292,7 +292,8 @@ mbg_status mbg_surrogate_gradients(mbg_surrogate* s, int32_t member, const float
  * allocated: the hash table is a 512 KiB device array inside libmbg.so that every GPU loading the
  * library keeps until exit. At most 32768 states per call (MBG_ERR_ARG beyond). The work is queued
  * on `stream`; results are valid once the stream has completed it. The first call on a device
- * looks the array's address up on that device, so make it before any stream capture. Calls share
+ * (and the first after the device's context was replaced, e.g. by cudaDeviceReset) looks the
+ * array's address up on that device, so make it before any stream capture. Calls share
  * the array and each clears it first: calls queued on one stream are safe, calls that overlap on
  * the GPU race. */
 mbg_status mbg_fixed_points_aggregate_noalloc(const uint32_t* states, uint32_t n_states, int32_t words,

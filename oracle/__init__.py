@@ -120,7 +120,7 @@ class OracleResult:
         return h
 
 
-def run(bnd: str, cfg: str, *, frac_bits: int, n_traj: int = 0, seed=None, traj_base: int = 0,
+def run(bnd: str, cfg: str, *, frac_bits: int = 0, n_traj: int = 0, seed=None, traj_base: int = 0,
         threads: int = 0, max_steps: int = 0, keep_trajectories: bool = False,
         legacy_final: bool = False) -> OracleResult:
     L = lib()

@@ -167,7 +167,8 @@ extern "C" orc_result* orc_run(const char* bnd_text, const char* cfg_text, const
         res->n_traj = o->n_traj ? o->n_traj : (uint64_t)(sc > 0 ? sc : 0);
         double cs = m.constant("seed_pseudorandom");
         const uint64_t seed = o->use_cfg_seed ? (uint64_t)(cs > 0 ? cs : 0) : o->seed;
-        const int F = o->frac_bits;
+        // the pick's fixed-point scale: the caller's, or the compiled model's rule (0)
+        const int F = o->frac_bits > 0 ? o->frac_bits : mbg::compile_model(m).frac_bits;
         const uint32_t max_steps = o->max_steps;
 
         std::vector<Prog> up(n), down(n);

@@ -37,7 +37,7 @@ typedef struct {
     uint64_t traj_base;  /* id of the first trajectory */
     uint64_t seed;
     int use_cfg_seed;    /* 1: seed_pseudorandom of the cfg */
-    int frac_bits;       /* fixed-point fraction bits of the pick (from the compiled model) */
+    int frac_bits;       /* fixed-point fraction bits of the pick; 0: the compiled model's own */
     int threads;         /* 0: hardware concurrency */
     uint32_t max_steps;  /* 0: unlimited */
     int keep_trajectories; /* store per-trajectory end records */

@@ -1,7 +1,7 @@
 """Generates the golden fixtures of tests/golden/ from the reference checkout.
 
-Run once where the reference is present:  python tests/golden/make_fixtures.py /root/reference
-It decodes the reference's pinned results test/*.res (UTF-16LE dumps of the stdout report of an
+Run once where the reference is present:  python tests/golden/make_fixtures.py <reference checkout>
+(the path is required: the directory holding the reference's test/ and data/). It decodes the reference's pinned results test/*.res (UTF-16LE dumps of the stdout report of an
 earlier MaBoSSG build: final points, fixed points, then per window the entropy, the transition
 entropy and the state probabilities) into <model>.json, and copies the four input models
 data/<model>.bnd/.cfg into models/, so the tests need neither the reference nor its build.
@@ -77,4 +77,6 @@ def main(ref: str):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_fixtures.py <reference checkout (holds test/ and data/)>")
+    main(sys.argv[1])

@@ -92,3 +92,21 @@ def test_model_info_of_workloads():
         assert m.names == net.names
         assert m.info.sample_count == net.sample_count
         assert 8 <= m.info.frac_bits <= 40
+
+
+def test_trajectory_limit_is_checked_before_any_device_work(has_gpu):
+    """A run holds at most 2^30 trajectories: the fixed-point hash table has twice as many slots
+    as trajectories, counted in 32 bits. One more is refused as an argument error before any
+    device call; exactly 2^30 passes the check (without a GPU it then fails on the device)."""
+    net = synth.small()
+    m = mbg.Model.from_strings(net.bnd(), net.cfg())
+    with pytest.raises(mbg.MbgError) as e:
+        mbg.Simulation(m, n_traj=(1 << 30) + 1)
+    assert e.value.status == 1 and "2^30" in e.value.message
+    with pytest.raises(mbg.MbgError) as e:
+        mbg.Batch([m], n_traj=[(1 << 30) + 1])
+    assert e.value.status == 1 and "2^30" in e.value.message
+    if not has_gpu:
+        with pytest.raises(mbg.MbgError) as e:
+            mbg.Simulation(m, n_traj=1 << 30)
+        assert e.value.status == 5

@@ -12,6 +12,7 @@
 // the one table; every call clears it on its own stream first, so calls queued on one stream are
 // safe, but calls that overlap on the GPU (different streams, or different host threads without
 // ordering) race on the table and give wrong counts.
+#include <cuda.h>  // driver types only: the two driver calls below come through cudaGetDriverEntryPoint
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -33,8 +34,15 @@ constexpr int kMaxDevices = 64;
 // [0, slots): representative entry per slot, [slots, 2 slots): count per slot. 512 KiB.
 static __device__ __align__(256) unsigned g_fp_scratch[2 * kNoallocSlots];
 
+// The array's device address per device, with the id of the context it was looked up in: a new
+// context on the device (after cudaDeviceReset the library's module is loaded again, possibly at
+// another address) makes the next call look it up again.
+struct ScratchAddr {
+    unsigned long long ctx_id;  // 0: unknown, look the address up on every call
+    unsigned* ptr;
+};
 std::mutex g_setup_mu;
-unsigned* g_scratch_ptr[kMaxDevices] = {};
+ScratchAddr g_scratch_addr[kMaxDevices] = {};
 
 __device__ __forceinline__ unsigned long long na_hash(const unsigned* w, int words) {
     unsigned long long h = 0x9E3779B97F4A7C15ull ^ (unsigned long long)words;
@@ -90,20 +98,52 @@ __global__ void fp_compact_noalloc(const unsigned* __restrict__ states, int word
     }
 }
 
-// Device address of the scratch array on the current device, looked up once per device.
+// Unique id of the current context (cuCtxGetCurrent + cuCtxGetId through the runtime's driver
+// entry points, so the library still needs no link against libcuda); false if unavailable.
+bool current_context_id(unsigned long long* id) {
+    using GetCurrentFn = CUresult (*)(CUcontext*);
+    using GetIdFn = CUresult (*)(CUcontext, unsigned long long*);
+    static GetCurrentFn get_current = nullptr;
+    static GetIdFn get_id = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_current = reinterpret_cast<GetCurrentFn>(p);
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_id = reinterpret_cast<GetIdFn>(p);
+    });
+    CUcontext ctx = nullptr;
+    if (!get_current || !get_id || get_current(&ctx) != CUDA_SUCCESS || !ctx) return false;
+    return get_id(ctx, id) == CUDA_SUCCESS && *id != 0;
+}
+
+// Device address of the scratch array on the current device: looked up with the device current,
+// once per device and context (the first call on a device, and the first after its context was
+// replaced, does the lookup).
 cudaError_t scratch_for_current_device(unsigned** out) {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
     if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+    unsigned long long id = 0;
+    bool have_id = current_context_id(&id);
     std::lock_guard<std::mutex> lock(g_setup_mu);
-    if (!g_scratch_ptr[dev]) {
-        void* p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_fp_scratch);
-        if (e != cudaSuccess) return e;
-        g_scratch_ptr[dev] = static_cast<unsigned*>(p);
+    ScratchAddr& a = g_scratch_addr[dev];
+    if (have_id && a.ptr && a.ctx_id == id) {
+        *out = a.ptr;
+        return cudaSuccess;
     }
-    *out = g_scratch_ptr[dev];
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_fp_scratch);  // also creates the context if it did not exist yet
+    if (e != cudaSuccess) return e;
+    if (!have_id) have_id = current_context_id(&id);
+    a.ptr = static_cast<unsigned*>(p);
+    a.ctx_id = have_id ? id : 0ull;
+    *out = a.ptr;
     return cudaSuccess;
 }
 
@@ -119,16 +159,21 @@ extern "C" mbg_status mbg_fixed_points_aggregate_noalloc(const uint32_t* states,
     if (words < 1 || !n_unique || (n_states > 0 && (!states || !unique_states || !counts)))
         return mbg::set_error(MBG_ERR_ARG, "mbg_fixed_points_aggregate_noalloc: null buffer or words < 1");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    cudaGetLastError();  // drop a stale non-sticky error of an earlier unrelated call
+    // Every status below is the return value of its own call: an error the caller left pending
+    // in the runtime's error state is neither cleared nor reported as this call's.
     unsigned* scratch = nullptr;
     cudaError_t e = scratch_for_current_device(&scratch);
     if (e == cudaSuccess) e = cudaMemsetAsync(scratch, 0xFF, sizeof(unsigned) * kNoallocSlots, st);
     if (e == cudaSuccess) e = cudaMemsetAsync(scratch + kNoallocSlots, 0, sizeof(unsigned) * kNoallocSlots, st);
     if (e == cudaSuccess) e = cudaMemsetAsync(n_unique, 0, sizeof(unsigned), st);
     if (e == cudaSuccess && n_states > 0) {
-        fp_insert_noalloc<<<128, 256, 0, st>>>(states, n_states, words, scratch);
-        fp_compact_noalloc<<<128, 256, 0, st>>>(states, words, scratch, unique_states, counts, n_unique);
-        e = cudaGetLastError();
+        void* ins[] = {(void*)&states, (void*)&n_states, (void*)&words, (void*)&scratch};
+        e = cudaLaunchKernel((const void*)fp_insert_noalloc, dim3(128), dim3(256), ins, 0, st);
+        if (e == cudaSuccess) {
+            void* cmp[] = {(void*)&states, (void*)&words, (void*)&scratch, (void*)&unique_states, (void*)&counts,
+                           (void*)&n_unique};
+            e = cudaLaunchKernel((const void*)fp_compact_noalloc, dim3(128), dim3(256), cmp, 0, st);
+        }
     }
     if (e != cudaSuccess)
         return mbg::set_error(MBG_ERR_CUDA, std::string("mbg_fixed_points_aggregate_noalloc: ") + cudaGetErrorString(e));

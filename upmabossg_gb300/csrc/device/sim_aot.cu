@@ -12,6 +12,8 @@
 #include "sim_lane.cuh"
 #include "kernels.h"
 
+#include <utility>
+
 namespace mbg {
 
 // Cached-index variant (regulator index of every node kept in shared memory).
@@ -186,13 +188,25 @@ extern "C" __global__ void mbg_fp_compact_batch(const SimParams* __restrict__ pa
 }
 
 // ---------------------------------------------------------------------------------------------
-// Host-side launchers.
+// Host-side launchers. Each returns the status of its own launches (cudaLaunchKernelEx), so that
+// an error the caller left pending in the runtime's error state is neither cleared nor reported
+// as this library's.
+
+namespace {
+template <class K, class... A>
+cudaError_t launch(K kernel, dim3 grid, dim3 block, size_t smem, cudaStream_t stream, A&&... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = stream;
+    return cudaLaunchKernelEx(&cfg, kernel, std::forward<A>(args)...);
+}
+}  // namespace
 
 cudaError_t launch_sim_warp_batch(const BatchDesc& b, bool cached_index, int grid, int block, size_t smem,
                                   cudaStream_t stream) {
-    if (cached_index) mbg_sim_warp_batch<<<grid, block, smem, stream>>>(b);
-    else mbg_sim_warp_batch_gather<<<grid, block, smem, stream>>>(b);
-    return cudaGetLastError();
+    return launch(cached_index ? mbg_sim_warp_batch : mbg_sim_warp_batch_gather, grid, block, smem, stream, b);
 }
 
 cudaError_t sim_warp_batch_configure(bool cached_index, size_t smem, int block, int* blocks_per_sm) {
@@ -209,16 +223,14 @@ unsigned sim_warp_batch_slice_bytes(int max_n, bool cached_index) {
 cudaError_t launch_fp_aggregate_batch(const SimParams* params, const FpSlots* fps, int n_inst, int blocks_x,
                                       cudaStream_t stream) {
     dim3 grid(blocks_x, n_inst);
-    mbg_fp_insert_batch<<<grid, 256, 0, stream>>>(params, fps);
-    mbg_fp_compact_batch<<<grid, 256, 0, stream>>>(params, fps);
-    return cudaGetLastError();
+    cudaError_t e = launch(mbg_fp_insert_batch, grid, 256, 0, stream, params, fps);
+    if (e != cudaSuccess) return e;
+    return launch(mbg_fp_compact_batch, grid, 256, 0, stream, params, fps);
 }
 
 cudaError_t launch_sim_warp(const SimParams& p, bool cached_index, int grid, int block, size_t smem,
                             cudaStream_t stream) {
-    if (cached_index) mbg_sim_warp<<<grid, block, smem, stream>>>(p);
-    else mbg_sim_warp_gather<<<grid, block, smem, stream>>>(p);
-    return cudaGetLastError();
+    return launch(cached_index ? mbg_sim_warp : mbg_sim_warp_gather, grid, block, smem, stream, p);
 }
 
 cudaError_t sim_warp_configure(bool cached_index, size_t smem) {
@@ -237,14 +249,8 @@ cudaError_t sim_warp_occupancy(bool cached_index, int block, size_t smem, int* b
 
 cudaError_t launch_sim_lane(const SimParams& p, bool coop, bool full, int grid, int block, size_t smem,
                             cudaStream_t stream) {
-    if (full) {
-        if (coop) mbg_sim_lane_coop_full<<<grid, block, smem, stream>>>(p);
-        else mbg_sim_lane_full<<<grid, block, smem, stream>>>(p);
-    } else {
-        if (coop) mbg_sim_lane_coop<<<grid, block, smem, stream>>>(p);
-        else mbg_sim_lane<<<grid, block, smem, stream>>>(p);
-    }
-    return cudaGetLastError();
+    auto k = full ? (coop ? mbg_sim_lane_coop_full : mbg_sim_lane_full) : (coop ? mbg_sim_lane_coop : mbg_sim_lane);
+    return launch(k, grid, block, smem, stream, p);
 }
 
 namespace {
@@ -332,14 +338,9 @@ cudaError_t sim_lane_configure(bool coop, bool full, size_t smem, int block, int
 
 cudaError_t launch_sim_lane_batch(const BatchDesc& b, bool coop, bool full, int grid, int block, size_t smem,
                                   cudaStream_t stream) {
-    if (full) {
-        if (coop) mbg_sim_lane_batch_coop_full<<<grid, block, smem, stream>>>(b);
-        else mbg_sim_lane_batch_full<<<grid, block, smem, stream>>>(b);
-    } else {
-        if (coop) mbg_sim_lane_batch_coop<<<grid, block, smem, stream>>>(b);
-        else mbg_sim_lane_batch<<<grid, block, smem, stream>>>(b);
-    }
-    return cudaGetLastError();
+    auto k = full ? (coop ? mbg_sim_lane_batch_coop_full : mbg_sim_lane_batch_full)
+                  : (coop ? mbg_sim_lane_batch_coop : mbg_sim_lane_batch);
+    return launch(k, grid, block, smem, stream, b);
 }
 
 cudaError_t sim_lane_batch_configure(bool coop, bool full, size_t smem, int block, int* blocks_per_sm) {
@@ -362,11 +363,11 @@ cudaError_t launch_fp_aggregate(const unsigned* fp_states, const unsigned* fp_co
     if (e != cudaSuccess) return e;
     e = cudaMemsetAsync(n_unique, 0, sizeof(unsigned), stream);
     if (e != cudaSuccess) return e;
-    mbg_fp_insert<<<sms * 4, 256, 0, stream>>>(fp_states, fp_count, capacity, words, slot_rep, slot_cnt,
-                                               n_slots - 1u, error_flag);
-    mbg_fp_compact<<<sms * 4, 256, 0, stream>>>(fp_states, words, slot_rep, slot_cnt, n_slots, out_states, out_cnt,
-                                                n_unique);
-    return cudaGetLastError();
+    e = launch(mbg_fp_insert, sms * 4, 256, 0, stream, fp_states, fp_count, capacity, words, slot_rep, slot_cnt,
+               n_slots - 1u, error_flag);
+    if (e != cudaSuccess) return e;
+    return launch(mbg_fp_compact, sms * 4, 256, 0, stream, fp_states, words, slot_rep, slot_cnt, n_slots, out_states,
+                  out_cnt, n_unique);
 }
 
 }  // namespace mbg

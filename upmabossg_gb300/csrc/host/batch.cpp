@@ -29,12 +29,6 @@ struct Layout {
     }
 };
 
-uint32_t next_pow2(uint64_t x) {
-    uint64_t p = 1;
-    while (p < x) p <<= 1;
-    return (uint32_t)p;
-}
-
 void* dmalloc(size_t bytes, std::vector<void*>& owned) {
     void* p = nullptr;
     cudaError_t e = cudaMalloc(&p, bytes ? bytes : 1);
@@ -80,6 +74,8 @@ void Batch::create(const std::vector<const CompiledModel*>& models, const std::v
     if (o.layout != 0 && o.layout != MBG_LAYOUT_LANE && o.layout != MBG_LAYOUT_WARP)
         throw ArgError("batch layout must be 0 (auto), MBG_LAYOUT_LANE or MBG_LAYOUT_WARP");
     opts = o;
+    for (size_t i = 0; i < models.size(); ++i)  // argument checks come before any device call
+        check_model_limits(*models[i], n_traj.empty() || n_traj[i] == 0 ? models[i]->sample_count : n_traj[i]);
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
         cudaGetLastError();
@@ -149,7 +145,7 @@ void Batch::create(const std::vector<const CompiledModel*>& models, const std::v
         f.istate = ml.add(d.istate_thr.size() * 4);
         const uint64_t S = 1ull << cm.n_out;
         const uint32_t cap = (uint32_t)x.n_traj;
-        x.fp.n_slots = std::max<uint32_t>(1024, next_pow2(2ull * cap));
+        x.fp.n_slots = fp_slot_count(cap);
         f.hist = rl.add(cm.windows * S * 8);
         f.th = rl.add(cm.windows * 8);
         f.fin = rl.add(S * 4);

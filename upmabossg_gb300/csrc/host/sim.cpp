@@ -46,13 +46,15 @@ T* upload(const std::vector<T>& v, std::vector<void*>& owned) {
     return p;
 }
 
-uint32_t next_pow2(uint64_t x) {
-    uint64_t p = 1;
-    while (p < x) p <<= 1;
-    return (uint32_t)p;
-}
-
 }  // namespace
+
+uint32_t fp_slot_count(uint64_t capacity) {
+    if (capacity > kMaxTrajectories)
+        throw ArgError("fixed-point capacity " + std::to_string(capacity) + " above the limit of 2^30 entries");
+    uint64_t p = 1024;
+    while (p < 2 * capacity) p <<= 1;
+    return (uint32_t)p;  // <= 2^31
+}
 
 DeviceLayout layout_model(const CompiledModel& cm) {
     DeviceLayout d;
@@ -202,7 +204,7 @@ void set_model_constants(SimParams& prm, const CompiledModel& cm) {
 
 void check_model_limits(const CompiledModel& cm, uint64_t n_traj) {
     if (n_traj == 0) throw ArgError("no trajectories to simulate (n_traj and sample_count are 0)");
-    if (n_traj > 0xFFFFFFFFull) throw ArgError("more than 2^32 - 1 trajectories in one run");
+    if (n_traj > kMaxTrajectories) throw ArgError("more than 2^30 trajectories in one run");
     if (cm.n_out > 24) throw ModelError("more than 24 output nodes");
     const uint64_t hist_bytes = (uint64_t)cm.windows * (1ull << cm.n_out) * 8;
     if (hist_bytes > (16ull << 30)) throw ModelError("window histogram would exceed 16 GiB");
@@ -276,7 +278,7 @@ void Sim::create(const CompiledModel& model, const std::vector<std::string>& nod
         prm.traj_transitions = dalloc<unsigned int>((size_t)n_traj, owned);
         prm.traj_status = dalloc<unsigned char>((size_t)n_traj, owned);
     }
-    n_slots = std::max<uint32_t>(1024, next_pow2(2ull * fp_capacity));
+    n_slots = fp_slot_count(fp_capacity);
     slot_rep = dalloc<unsigned int>(n_slots, owned);
     slot_cnt = dalloc<unsigned int>(n_slots, owned);
     fp_out_states = dalloc<unsigned int>((size_t)fp_capacity * cm.words, owned);
@@ -457,7 +459,6 @@ std::mutex& kernel_attr_mutex() {
 
 void Sim::run(cudaStream_t stream) {
     ck(cudaSetDevice(device), "cudaSetDevice");
-    cudaGetLastError();  // drop a stale non-sticky error of an earlier unrelated call
     const uint64_t S = 1ull << cm.n_out;
     ck(cudaEventRecord(ev0, stream), "cudaEventRecord");
     ck(cudaMemsetAsync(prm.hist, 0, cm.windows * S * 8, stream), "cudaMemsetAsync");

@@ -44,8 +44,17 @@ DeviceLayout layout_model(const CompiledModel& cm);
 void check_layout(const CompiledModel& cm, const DeviceLayout& d);
 // Model-dependent SimParams fields (sizes, clock, rate scale).
 void set_model_constants(SimParams& prm, const CompiledModel& cm);
+// Most trajectories one run (or one batched instance) may hold: the fixed-point buffer has one
+// entry per trajectory and its hash table twice as many slots, counted in 32 bits.
+constexpr uint64_t kMaxTrajectories = 1ull << 30;
+
 // Throws if a run of n_traj trajectories of cm exceeds the result representation.
 void check_model_limits(const CompiledModel& cm, uint64_t n_traj);
+
+// Slots of the fixed-point hash table for `capacity` entries: a power of two of at least twice
+// the capacity (load factor <= 1/2, so a probe always ends) and at least 1024. Throws ArgError
+// for a capacity above kMaxTrajectories, whose slot count would not fit in 32 bits.
+uint32_t fp_slot_count(uint64_t capacity);
 
 // NVRTC source of the thread-per-trajectory kernel `mbg_sim_thread` specialised to one model.
 std::string generate_thread_model(const CompiledModel& cm, const DeviceLayout& dl);
