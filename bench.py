@@ -351,7 +351,8 @@ def run_ours(args):
     base = rank * n_rank
     bnd, cfg = net.bnd(), net.cfg()
     model = mbg.Model.from_strings(bnd, cfg)
-    sim_kw = dict(layout=args.layout, block_size=args.block, lane_update=args.lane_update)
+    sim_kw = dict(layout=args.layout, block_size=args.block, lane_update=args.lane_update,
+                  window_table=args.window_table)
     sim = mbg.Simulation(model, n_traj=n_rank, traj_base=base, device=local, **sim_kw)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{local}")
 
@@ -399,16 +400,18 @@ def run_ours(args):
         m2 = mbg.Model.from_strings(bnd, cfg)
         s2 = mbg.Simulation(m2, n_traj=n_rank, traj_base=base, device=local, **sim_kw)
         s2.run()
-        P, TH = s2.probtraj()
+        bins, sums, probs = s2.probtraj_sparse()
+        TH = s2.tr_entropy()
         F = s2.final_states()
         fs, fp = s2.fixed_points()
         torch.cuda.synchronize()
         dt = time.perf_counter() - t1
         if i > 0:
             e2e_ms.append(dt * 1e3)
-        # model text in, raw u64 window sums + TH sums + u32 final counts + fixed points out
+        # model text in (the model tables are built and uploaded by mbg_sim_create); out: the
+        # reached window bins (u32 bin + u64 sum each), TH sums, u32 final counts, fixed points
         h2d = len(bnd) + len(cfg)
-        d2h = P.size * 8 + TH.size * 8 + F.size * 4 + fs.nbytes + fp.size * 4
+        d2h = bins.size * 12 + TH.size * 8 + F.size * 4 + fs.nbytes + fp.size * 4
         s2.close()
         m2.close()
     e2e_step_ms = statistics.mean(e2e_ms)
@@ -451,7 +454,8 @@ def run_ours(args):
                    "l2": "flushed between steps (256 MiB write)", "wall_s": wall},
         "e2e": {"value": e2e_value, "unit": "transitions/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "ms_per_step": e2e_step_ms,
-                "path": "mbg_model_parse_strings + mbg_sim_create + mbg_sim_run + probtraj/final/fixed-point reads"},
+                "path": "mbg_model_parse_strings + mbg_sim_create + mbg_sim_run + mbg_sim_probtraj_sparse + "
+                        "TH/final/fixed-point reads", "window_table": ["", "dense", "hash"][summary["window_table"]]},
         "gpu_launches": 3 * args.steps,
         "roofline": roofline,
         "cpu_baseline": cpu,
@@ -475,6 +479,7 @@ def main():
     ap.add_argument("--layout", type=int, default=0, help="0 autotuned, 1 thread, 2 warp, 3 lane")
     ap.add_argument("--block", type=int, default=0, help="threads per block (0: the layout's default); profiling")
     ap.add_argument("--lane-update", type=int, default=0, help="lane layout: 0 cooperative, 1 per lane; profiling")
+    ap.add_argument("--window-table", type=int, default=0, help="0 auto, 1 dense, 2 hash table; profiling")
     ap.add_argument("--cpu-seconds", type=float, default=CPU_SAMPLE_SECONDS)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--n-traj", type=int, default=0, help="trajectories (default: the workload's); profiling only")

@@ -83,6 +83,12 @@ typedef struct {
                                   per trajectory without timing; 0: autotune */
     int32_t lane_update;       /* LANE: readers of a flipped node updated 0: warp-cooperatively
                                   (default), 1: by their own lane; AUTO times both */
+    int32_t window_table;      /* where the window sums accumulate: 0 auto (the dense table while it
+                                  is at most 64 MiB or the trajectories x windows exceed 1/8 of the
+                                  bins, else the hash table), 1 the dense windows x 2^outputs table
+                                  (the reference's layout), 2 an open-addressed hash table of the
+                                  (window, output state) bins reached, grown and re-run when full */
+    int32_t window_hash_bits;  /* hash table: log2 of its initial slot count (10..31); 0 automatic */
 } mbg_sim_opts;
 
 typedef struct {
@@ -99,7 +105,10 @@ typedef struct {
     int32_t block_size;        /* threads per block of the simulation kernel */
     int32_t grid_size;         /* blocks of the simulation kernel */
     int32_t lane_update;       /* LANE: 0 cooperative, 1 per-lane reader updates */
-    int32_t reserved;
+    int32_t window_table;      /* 1 dense table, 2 hash table */
+    int32_t window_hash_bits;  /* hash table: log2 of its slot count in the last run */
+    int32_t window_reruns;     /* runs repeated with a larger hash table (results are the same) */
+    uint64_t window_entries;   /* hash table: distinct (window, output state) bins reached */
 } mbg_run_summary;
 
 const char* mbg_last_error(void);
@@ -164,6 +173,14 @@ mbg_status mbg_sim_summary(const mbg_sim* s, mbg_run_summary* out);
 mbg_status mbg_sim_probtraj(mbg_sim* s, double* probs, double* tr_entropy);
 /* Raw fixed-point sums: windows x 2^outputs (time x 2^32, or counts) and windows TH sums. */
 mbg_status mbg_sim_probtraj_raw(mbg_sim* s, uint64_t* sums, uint64_t* th_sums);
+/* The non-zero window bins only, in increasing order: bin = window x 2^outputs + output state,
+ * with its raw sum (as mbg_sim_probtraj_raw) and probability (as mbg_sim_probtraj); any of the
+ * three arrays may be NULL; `cap` entries at most, `*count` gets the number of non-zero bins. The
+ * read-back for large output spaces (20 outputs: 2^20 states per window), where the dense arrays
+ * are mostly zeros: only the bins the run reached leave the device. Replaces the host walk over the
+ * dense table, src/statistics/window_average_small.cpp:126-140. */
+mbg_status mbg_sim_probtraj_sparse(mbg_sim* s, uint64_t* bins, uint64_t* sums, double* probs, size_t cap,
+                                   size_t* count);
 /* 2^outputs final-state probabilities. */
 mbg_status mbg_sim_final_states(mbg_sim* s, double* probs);
 /* Distinct fixed points in reference order (highest state word first): states (n x words),

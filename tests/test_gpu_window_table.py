@@ -1,0 +1,121 @@
+"""Window sums in the hash table against the dense table, through the C ABI.
+
+The two tables hold the same integer sums, so every comparison here is exact: the reached bins
+and their sums, the transition entropy, the CSV and stdout reports. Covered: every layout, the
+discrete-time counts, a table too small for the run (grown and re-run until it holds), the
+automatic choice on the 20-output and 10-output workloads, and the sparse read-back against the
+dense one.
+"""
+import os
+
+import numpy as np
+import pytest
+
+import upmabossg_gb300 as mbg
+from upmabossg_gb300 import synth
+
+from helpers import compare_histograms, golden_model, run_oracle
+
+pytestmark = pytest.mark.gpu
+
+DENSE, HASH = 1, 2
+
+
+def simulate(bnd, cfg, n, table, bits=0, **kw):
+    model = mbg.Model.from_strings(bnd, cfg)
+    sim = mbg.Simulation(model, n_traj=n, window_table=table, window_hash_bits=bits, **kw).run()
+    return model, sim
+
+
+def same_windows(a, b):
+    ba, sa, pa = a.probtraj_sparse()
+    bb, sb, pb = b.probtraj_sparse()
+    assert np.array_equal(ba, bb), "reached bins differ"
+    assert np.array_equal(sa, sb), "bin sums differ"
+    assert np.array_equal(pa, pb)
+    assert np.all(np.diff(ba.astype(np.int64)) > 0), "bins not in increasing order"
+    assert np.all(sa > 0)
+    assert np.array_equal(a.tr_entropy(), b.tr_entropy())
+    assert np.array_equal(a.final_states(), b.final_states())
+
+
+@pytest.mark.parametrize("layout", [mbg.LAYOUT_THREAD, mbg.LAYOUT_WARP, mbg.LAYOUT_LANE])
+def test_hash_table_equals_dense_table(layout):
+    net = synth.small()  # 20 outputs: 2^20 states per window
+    bnd, cfg = net.bnd(), net.cfg()
+    _, dense = simulate(bnd, cfg, 20000, DENSE, layout=layout)
+    _, hashed = simulate(bnd, cfg, 20000, HASH, layout=layout)
+    assert dense.summary()["window_table"] == DENSE
+    s = hashed.summary()
+    assert s["window_table"] == HASH and s["window_reruns"] == 0
+    assert s["window_entries"] == len(hashed.probtraj_sparse()[0])
+    same_windows(dense, hashed)
+
+
+def test_full_table_grows_and_reruns():
+    """A 1024-slot table for a run that reaches ~10^5 bins: the first attempts overflow, the run
+    repeats on tables four times larger until it holds, and the result is the dense table's."""
+    net = synth.small()
+    bnd, cfg = net.bnd(), net.cfg()
+    _, dense = simulate(bnd, cfg, 20000, DENSE, layout=mbg.LAYOUT_LANE)
+    _, hashed = simulate(bnd, cfg, 20000, HASH, bits=10, layout=mbg.LAYOUT_LANE)
+    s = hashed.summary()
+    assert s["window_reruns"] >= 1 and s["window_hash_bits"] > 10
+    assert s["window_entries"] * 2 > (1 << 10)
+    same_windows(dense, hashed)
+    hashed.run()  # the next run starts on a table at most half full
+    s2 = hashed.summary()
+    assert s2["window_reruns"] == 0 and 2 * s2["window_entries"] <= (1 << s2["window_hash_bits"])
+    same_windows(dense, hashed)
+
+
+def test_discrete_time_counts():
+    bnd, cfg = golden_model("cellcycle")  # discrete_time = 1
+    _, dense = simulate(bnd, cfg, 30000, DENSE)
+    model, hashed = simulate(bnd, cfg, 30000, HASH, bits=10)
+    assert model.info.discrete_time
+    same_windows(dense, hashed)
+
+
+def test_hash_table_against_oracle():
+    net = synth.small()
+    bnd, cfg = net.bnd(), net.cfg()
+    model, sim = simulate(bnd, cfg, 4000, HASH, layout=mbg.LAYOUT_THREAD, record_trajectories=True)
+    orc = run_oracle(bnd, cfg, model, 4000)
+    compare_histograms(model, sim, orc, 4000)
+
+
+def test_automatic_choice():
+    small, medium = synth.small(), synth.medium()
+    _, s = simulate(small.bnd(), small.cfg(), 0, 0)  # 1e5 trajectories x 100 windows << 100 x 2^20 bins
+    assert s.summary()["window_table"] == HASH
+    _, m = simulate(medium.bnd(), medium.cfg(), 50000, 0)  # 100 x 2^10 bins: 800 KiB dense
+    assert m.summary()["window_table"] == DENSE
+
+
+def test_sparse_read_equals_dense_read():
+    net = synth.medium()
+    bnd, cfg = net.bnd(), net.cfg()
+    model, sim = simulate(bnd, cfg, 20000, DENSE)
+    raw, th = sim.probtraj_raw()
+    probs, _ = sim.probtraj()
+    bins, sums, p = sim.probtraj_sparse()
+    nz = np.flatnonzero(raw.ravel())
+    assert np.array_equal(nz.astype(np.uint64), bins)
+    assert np.array_equal(raw.ravel()[nz], sums)
+    assert np.array_equal(probs.ravel()[nz], p)
+
+
+def test_reports_identical(tmp_path):
+    net = synth.small()
+    bnd, cfg = net.bnd(), net.cfg()
+    _, dense = simulate(bnd, cfg, 5000, DENSE, layout=mbg.LAYOUT_LANE)
+    _, hashed = simulate(bnd, cfg, 5000, HASH, layout=mbg.LAYOUT_LANE)
+    for sim, name in ((dense, "d"), (hashed, "h")):
+        sim.write_csv(str(tmp_path / name))
+        sim.print_results(str(tmp_path / (name + ".txt")))
+    for suffix in ("_probtraj.csv", "_fp.csv"):
+        with open(tmp_path / ("d" + suffix)) as f1, open(tmp_path / ("h" + suffix)) as f2:
+            assert f1.read() == f2.read()
+    with open(tmp_path / "d.txt") as f1, open(tmp_path / "h.txt") as f2:
+        assert f1.read() == f2.read()

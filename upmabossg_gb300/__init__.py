@@ -26,7 +26,7 @@ EXPORTS = (
     "mbg_model_with_rate_scales", "mbg_model_parse_files_overrides", "mbg_model_with_mutations",
     "mbg_model_jit_check", "mbg_model_layout_check",
     "mbg_sim_opts_default", "mbg_sim_create", "mbg_sim_destroy", "mbg_sim_run", "mbg_sim_summary",
-    "mbg_sim_probtraj", "mbg_sim_probtraj_raw", "mbg_sim_final_states", "mbg_sim_fixed_points",
+    "mbg_sim_probtraj", "mbg_sim_probtraj_raw", "mbg_sim_probtraj_sparse", "mbg_sim_final_states", "mbg_sim_fixed_points",
     "mbg_sim_trajectories", "mbg_write_probtraj_csv", "mbg_write_fp_csv", "mbg_print_results",
     "mbg_write_final_states_csv", "mbg_fixed_points_aggregate_noalloc",
     "mbg_batch_opts_default", "mbg_batch_create", "mbg_batch_destroy", "mbg_batch_run", "mbg_batch_summary",
@@ -76,7 +76,8 @@ class SimOpts(ctypes.Structure):
                 ("record_trajectories", ctypes.c_int32), ("device", ctypes.c_int32),
                 ("max_steps", ctypes.c_uint32), ("block_size", ctypes.c_int32),
                 ("blocks_per_sm", ctypes.c_int32), ("thread_cutoff", ctypes.c_int32),
-                ("lane_update", ctypes.c_int32)]
+                ("lane_update", ctypes.c_int32), ("window_table", ctypes.c_int32),
+                ("window_hash_bits", ctypes.c_int32)]
 
 
 class RunSummary(ctypes.Structure):
@@ -86,7 +87,9 @@ class RunSummary(ctypes.Structure):
                 ("fixed_point_states", ctypes.c_uint64), ("device_error", ctypes.c_uint32),
                 ("layout", ctypes.c_int32), ("sim_ms", ctypes.c_double), ("kernel_ms", ctypes.c_double),
                 ("jit_ms", ctypes.c_double), ("block_size", ctypes.c_int32), ("grid_size", ctypes.c_int32),
-                ("lane_update", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+                ("lane_update", ctypes.c_int32), ("window_table", ctypes.c_int32),
+                ("window_hash_bits", ctypes.c_int32), ("window_reruns", ctypes.c_int32),
+                ("window_entries", ctypes.c_uint64)]
 
     def as_dict(self):
         return {name: getattr(self, name) for name, _ in self._fields_}
@@ -127,6 +130,8 @@ def lib():
             "mbg_sim_summary": (ctypes.c_int, [vp, ctypes.POINTER(RunSummary)]),
             "mbg_sim_probtraj": (ctypes.c_int, [vp, dp, dp]),
             "mbg_sim_probtraj_raw": (ctypes.c_int, [vp, dp, dp]),
+            "mbg_sim_probtraj_sparse": (ctypes.c_int, [vp, dp, dp, dp, ctypes.c_size_t,
+                                                        ctypes.POINTER(ctypes.c_size_t)]),
             "mbg_sim_final_states": (ctypes.c_int, [vp, dp]),
             "mbg_sim_fixed_points": (ctypes.c_int, [vp, dp, dp, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]),
             "mbg_sim_trajectories": (ctypes.c_int, [vp, dp, dp, dp, dp]),
@@ -281,7 +286,7 @@ class Simulation:
 
     def __init__(self, model: Model, n_traj=0, seed=None, layout=LAYOUT_AUTO, record_trajectories=False,
                  max_steps=0, traj_base=0, device=0, block_size=0, blocks_per_sm=0, thread_cutoff=0,
-                 lane_update=0):
+                 lane_update=0, window_table=0, window_hash_bits=0):
         o = SimOpts()
         lib().mbg_sim_opts_default(ctypes.byref(o))
         o.n_traj = int(n_traj)
@@ -297,6 +302,8 @@ class Simulation:
         o.blocks_per_sm = blocks_per_sm
         o.thread_cutoff = thread_cutoff
         o.lane_update = lane_update
+        o.window_table = window_table
+        o.window_hash_bits = window_hash_bits
         self.model = model
         h = ctypes.c_void_p()
         _check(lib().mbg_sim_create(model._h, ctypes.byref(o), ctypes.byref(h)))
@@ -325,6 +332,23 @@ class Simulation:
         TH = np.zeros(info.windows, np.uint64)
         _check(lib().mbg_sim_probtraj_raw(self._h, _p(P), _p(TH)))
         return P, TH
+
+    def probtraj_sparse(self):
+        """The reached window bins only: (bins, raw sums, probabilities), bins increasing, each
+        bin = window * 2^outputs + output state."""
+        n = ctypes.c_size_t()
+        _check(lib().mbg_sim_probtraj_sparse(self._h, None, None, None, 0, ctypes.byref(n)))
+        bins = np.zeros(n.value, np.uint64)
+        sums = np.zeros(n.value, np.uint64)
+        probs = np.zeros(n.value, np.float64)
+        _check(lib().mbg_sim_probtraj_sparse(self._h, _p(bins), _p(sums), _p(probs), n.value, ctypes.byref(n)))
+        return bins, sums, probs
+
+    def tr_entropy(self):
+        """Per-window transition entropy."""
+        TH = np.zeros(self.model.info.windows, np.float64)
+        _check(lib().mbg_sim_probtraj(self._h, None, _p(TH)))
+        return TH
 
     def final_states(self):
         F = np.zeros(1 << self.model.info.outputs, np.float64)

@@ -1,4 +1,4 @@
-// Host-callable launchers of the ahead-of-time kernels (sim_aot.cu).
+// Host-callable launchers of the ahead-of-time kernels (sim_aot.cu, window_table.cu).
 #pragma once
 
 #include <cuda_runtime.h>
@@ -43,5 +43,21 @@ cudaError_t launch_fp_aggregate(const unsigned* fp_states, const unsigned* fp_co
                                 unsigned* slot_rep, unsigned* slot_cnt, unsigned n_slots, unsigned* out_states,
                                 unsigned* out_cnt, unsigned* n_unique, unsigned* error_flag, int sms,
                                 cudaStream_t stream);
+
+// Window-sum compaction (window_table.cu) over n_bins = windows << n_out bins, from the dense
+// table `hist` (hash_bits == 0) or the hash table `hslots` (2^hash_bits slots). Count pass: marks
+// the occupied bins in `bitmap` (window_bitmap_words u32), the per-word prefixes in `wpre` (as
+// many) and the per-chunk prefixes in `chunk` (window_chunks u32); *total = occupied bins. Emit
+// pass (after the count pass, with out_bin / out_sum holding *total entries): the (bin, sum)
+// pairs in increasing bin order.
+unsigned long long window_bitmap_words(unsigned long long n_bins);
+unsigned window_chunks(unsigned long long n_bins);
+cudaError_t launch_window_count(const unsigned long long* hist, const unsigned long long* hslots, int hash_bits,
+                                unsigned long long n_bins, unsigned* bitmap, unsigned* wpre, unsigned* chunk,
+                                unsigned long long* total, int sms, cudaStream_t stream);
+cudaError_t launch_window_emit(const unsigned long long* hist, const unsigned long long* hslots, int hash_bits,
+                               unsigned long long n_bins, const unsigned* bitmap, const unsigned* wpre,
+                               const unsigned* chunk, unsigned* out_bin, unsigned long long* out_sum, int sms,
+                               cudaStream_t stream);
 
 }  // namespace mbg

@@ -70,10 +70,44 @@ __device__ __forceinline__ void win_begin(WindowAcc& a, const SimParams& p, unsi
     a.th = 0.f;
 }
 
+// Probes one insertion into the window hash table may take before it gives up (the host then
+// re-runs with a larger table). The host keeps the table at most half full.
+#define MBG_WINDOW_PROBES 512u
+
+// Slot of `key` (bin + 1) in a table of 2^bits slots: the top bits of its Fibonacci product.
+__device__ __forceinline__ unsigned long long win_hash(unsigned long long key, int bits) {
+    return (key * 0x9E3779B97F4A7C15ull) >> (64 - bits);
+}
+
+// Adds v to the window sum of bin (window w, output state s): one atomic on the dense table, or,
+// in hash mode, a claim-or-match CAS on the key followed by an atomic add on the sum. The sums are
+// integers, so the result does not depend on the order of the additions or of the claims.
+__device__ __forceinline__ void bin_add(const SimParams& p, int w, unsigned s, unsigned long long v) {
+    const unsigned long long bin = ((unsigned long long)w << p.n_out) | s;
+    if (p.hash_bits == 0) {
+        atomicAdd(p.hist + bin, v);
+        return;
+    }
+    const unsigned long long key = bin + 1ull;
+    const unsigned long long mask = (1ull << p.hash_bits) - 1ull;
+    unsigned long long h = win_hash(key, p.hash_bits);
+    for (unsigned probe = 0; probe < MBG_WINDOW_PROBES; ++probe) {
+        const unsigned long long cur = atomicCAS(p.hslots + 2 * h, 0ull, key);
+        if (cur == 0ull || cur == key) {
+            atomicAdd(p.hslots + 2 * h + 1, v);
+            if (cur == 0ull) atomicAdd(p.counters + CNT_WIN_ENTRIES, 1ull);
+            return;
+        }
+        h = (h + 1ull) & mask;
+        // once any insertion has overflowed the run is repeated anyway: stop probing early
+        if ((probe & 15u) == 15u && (*(volatile const unsigned*)p.error_flag & (unsigned)DEV_ERR_WINDOW_TABLE)) return;
+    }
+    atomicOr(p.error_flag, (unsigned)DEV_ERR_WINDOW_TABLE);
+}
+
 __device__ __forceinline__ void win_flush_run(WindowAcc& a, const SimParams& p, unsigned long long t_end,
                                               bool leader) {
-    if (leader && t_end > a.run_t0)
-        atomicAdd(p.hist + (((unsigned long long)a.w << p.n_out) | a.run_s), fx_to_bin(p, t_end - a.run_t0));
+    if (leader && t_end > a.run_t0) bin_add(p, a.w, a.run_s, fx_to_bin(p, t_end - a.run_t0));
 }
 
 __device__ __forceinline__ void win_flush_th(WindowAcc& a, const SimParams& p, bool leader) {
@@ -112,7 +146,7 @@ __device__ __forceinline__ void win_discrete(const SimParams& p, unsigned long l
                                              bool leader) {
     int w = step < (unsigned long long)p.windows ? (int)step : p.windows - 1;
     if (leader) {
-        atomicAdd(p.hist + (((unsigned long long)w << p.n_out) | s), 1ull);
+        bin_add(p, w, s, 1ull);
         if (h != 0.f) atomicAdd(p.th_hist + w, f32_to_fixed(h, 32));
     }
 }

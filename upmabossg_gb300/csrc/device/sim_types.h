@@ -18,6 +18,8 @@ enum DevError : unsigned int {
     DEV_ERR_PICK = 1u,         // no node satisfied the prefix test
     DEV_ERR_FP_OVERFLOW = 2u,  // fixed-point buffer full
     DEV_ERR_SMEM = 4u,         // launch shape does not match the model
+    DEV_ERR_WINDOW_TABLE = 8u, // window hash table: an insertion ran past the probe limit (the host
+                               // re-runs with a larger table; results are independent of the table)
 };
 
 // Indices into SimParams::counters.
@@ -29,6 +31,7 @@ enum Counter {
     CNT_STEP_LIMIT = 4,
     CNT_ERROR = 5,
     CNT_STEPS = 6,        // loop iterations (transitions + terminal steps)
+    CNT_WIN_ENTRIES = 7,  // window hash table: occupied slots (distinct (window, output state) bins)
     CNT_COUNT = 8,
 };
 
@@ -99,6 +102,11 @@ struct SimParams {
     // results
     unsigned long long* hist;        // windows x 2^n_out, time x 2^32 (counts if discrete)
     unsigned long long* th_hist;     // windows, TH x time x 2^32 (TH x 2^32 if discrete)
+    // With hash_bits > 0 the window sums go to an open-addressed hash table instead of `hist`:
+    // 2^hash_bits slots of two u64, [2i] the key (bin + 1, bin = window << n_out | output state;
+    // 0 = empty) and [2i + 1] the sum; linear probing from the key's multiplicative hash.
+    unsigned long long* hslots;
+    int hash_bits;
     unsigned int* final_hist;        // 2^n_out
     unsigned int* fp_states;         // fp_capacity x words
     unsigned int* fp_count;

@@ -282,9 +282,10 @@ mbg_status mbg_sim_probtraj(mbg_sim* s, double* probs, double* tr_entropy) {
     if (!s) return fail(MBG_ERR_ARG, "null simulation");
     return guard([&] {
         s->sim.fetch();
-        const size_t n = s->sim.hist.size();
-        if (probs)
-            for (size_t i = 0; i < n; ++i) probs[i] = mbg::window_prob(s->sim, i);
+        if (probs) {
+            std::memset(probs, 0, s->sim.n_bins * sizeof(double));
+            for (size_t e = 0; e < s->sim.wbin.size(); ++e) probs[s->sim.wbin[e]] = mbg::window_prob(s->sim, s->sim.wsum[e]);
+        }
         if (tr_entropy)
             for (int w = 0; w < s->sim.cm.windows; ++w) tr_entropy[w] = mbg::window_th(s->sim, w);
     });
@@ -294,8 +295,27 @@ mbg_status mbg_sim_probtraj_raw(mbg_sim* s, uint64_t* sums, uint64_t* th_sums) {
     if (!s) return fail(MBG_ERR_ARG, "null simulation");
     return guard([&] {
         s->sim.fetch();
-        if (sums) std::memcpy(sums, s->sim.hist.data(), s->sim.hist.size() * 8);
+        if (sums) {
+            std::memset(sums, 0, s->sim.n_bins * 8);
+            for (size_t e = 0; e < s->sim.wbin.size(); ++e) sums[s->sim.wbin[e]] = s->sim.wsum[e];
+        }
         if (th_sums) std::memcpy(th_sums, s->sim.th.data(), s->sim.th.size() * 8);
+    });
+}
+
+mbg_status mbg_sim_probtraj_sparse(mbg_sim* s, uint64_t* bins, uint64_t* sums, double* probs, size_t cap,
+                                   size_t* count) {
+    if (!s || !count) return fail(MBG_ERR_ARG, "null argument");
+    return guard([&] {
+        s->sim.fetch();
+        const size_t n = s->sim.wbin.size();
+        *count = n;
+        const size_t m = n < cap ? n : cap;
+        for (size_t e = 0; e < m; ++e) {
+            if (bins) bins[e] = s->sim.wbin[e];
+            if (sums) sums[e] = s->sim.wsum[e];
+            if (probs) probs[e] = mbg::window_prob(s->sim, s->sim.wsum[e]);
+        }
     });
 }
 

@@ -41,11 +41,11 @@ std::string out_state_string(const Sim& s, uint32_t idx) {
     return state_string(s.names, w, s.cm.n);
 }
 
-// get_single_result_prob, window_average_small.cpp:126-140
-double window_prob(const Sim& s, size_t idx) {
+// get_single_result_prob, window_average_small.cpp:126-140, for a bin with this raw sum
+double window_prob(const Sim& s, uint64_t sum) {
     const double n = (double)s.n_traj;
-    if (s.cm.discrete) return (double)s.hist[idx] / n;
-    return ((double)s.hist[idx] / 4294967296.0) / (n * s.cm.tick);
+    if (s.cm.discrete) return (double)sum / n;
+    return ((double)sum / 4294967296.0) / (n * s.cm.tick);
 }
 
 double window_th(const Sim& s, int w) {
@@ -55,12 +55,12 @@ double window_th(const Sim& s, int w) {
 
 namespace {
 
+// Walks the reached bins of window w only (the reference walks all 2^n_out states).
 double window_entropy(const Sim& s, int w, int* nonzero) {
-    const size_t S = (size_t)1 << s.cm.n_out;
     double h = 0;
     int nz = 0;
-    for (size_t x = 0; x < S; ++x) {
-        double p = window_prob(s, (size_t)w * S + x);
+    for (size_t e = s.wstart[w]; e < s.wstart[w + 1]; ++e) {
+        double p = window_prob(s, s.wsum[e]);
         if ((float)p == 0.f) continue;
         ++nz;
         h += -std::log2(p) * p;
@@ -76,7 +76,7 @@ float window_start(const Sim& s, int w) { return (float)w * (float)s.cm.tick; }
 void write_probtraj_csv(const Sim& s, const std::string& path) {
     std::ofstream ofs(path);
     if (!ofs) throw IoError("cannot write " + path);
-    const size_t S = (size_t)1 << s.cm.n_out;
+    const uint32_t smask = (uint32_t)(((uint64_t)1 << s.cm.n_out) - 1);
     int max_states = 0;
     for (int w = 0; w < s.cm.windows; ++w) {
         int nz = 0;
@@ -89,10 +89,10 @@ void write_probtraj_csv(const Sim& s, const std::string& path) {
     for (int w = 0; w < s.cm.windows; ++w) {
         ofs << window_start(s, w) << "\t";
         ofs << (float)window_th(s, w) << "\t" << 0.f << "\t" << (float)window_entropy(s, w, nullptr) << "\t" << 0.f;
-        for (size_t x = 0; x < S; ++x) {
-            double p = window_prob(s, (size_t)w * S + x);
+        for (size_t e = s.wstart[w]; e < s.wstart[w + 1]; ++e) {
+            double p = window_prob(s, s.wsum[e]);
             if ((float)p == 0.f) continue;
-            ofs << "\t" << out_state_string(s, (uint32_t)x) << "\t" << (float)p << "\t" << 0.f;
+            ofs << "\t" << out_state_string(s, s.wbin[e] & smask) << "\t" << (float)p << "\t" << 0.f;
         }
         ofs << "\n";
     }
@@ -141,6 +141,7 @@ void write_final_states_csv(const Sim& s, const std::string& path) {
 
 void print_results(const Sim& s, std::ostream& os) {
     const size_t S = (size_t)1 << s.cm.n_out;
+    const uint32_t smask = (uint32_t)(S - 1);
     os << "final points:\n";
     for (size_t x = 0; x < S; ++x)
         if (s.fin[x] != 0)
@@ -152,10 +153,10 @@ void print_results(const Sim& s, std::ostream& os) {
         os << "window (" << window_start(s, w) << ", " << window_start(s, w + 1) << "]\n";
         os << "entropy: " << (float)window_entropy(s, w, nullptr) << "\n";
         os << "transition entropy: " << (float)window_th(s, w) << "\n";
-        for (size_t x = 0; x < S; ++x) {
-            double p = window_prob(s, (size_t)w * S + x);
+        for (size_t e = s.wstart[w]; e < s.wstart[w + 1]; ++e) {
+            double p = window_prob(s, s.wsum[e]);
             if ((float)p == 0.f) continue;
-            os << (float)p << " " << out_state_string(s, (uint32_t)x) << "\n";
+            os << (float)p << " " << out_state_string(s, s.wbin[e] & smask) << "\n";
         }
     }
     os.flush();

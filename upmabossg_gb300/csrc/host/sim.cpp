@@ -15,6 +15,7 @@
 #include <cstring>
 #include <map>
 #include <mutex>
+#include <tuple>
 
 #include "../device/kernels.h"
 
@@ -212,7 +213,107 @@ void check_model_limits(const CompiledModel& cm, uint64_t n_traj) {
         throw ModelError("n_traj x time_tick too large for the 2^-32 fixed-point window sums");
 }
 
+namespace {
+
+void* raw_alloc(size_t bytes, const char* what) {
+    void* p = nullptr;
+    cudaError_t e = cudaMalloc(&p, bytes ? bytes : 1);
+    if (e != cudaSuccess) {
+        cudaGetLastError();  // the failed allocation's own error
+        throw NoMemError(std::string("cudaMalloc of ") + std::to_string(bytes) + " bytes (" + what +
+                         "): " + cudaGetErrorString(e));
+    }
+    return p;
+}
+
+int ceil_log2_u64(uint64_t x) {
+    int c = 0;
+    while (c < 63 && (1ull << c) < x) ++c;
+    return c;
+}
+
+// Window-table size learned by earlier runs of the process (auto mode), per model shape and
+// trajectory-count class: log2 of the hash slots, or 0 for the dense table. A new handle of the
+// same shape starts at the size that held, instead of growing (and re-running) again.
+std::mutex g_window_mu;
+std::map<std::tuple<int, int, int, int>, int> g_window_bits;
+
+std::tuple<int, int, int, int> window_class(const CompiledModel& cm, uint64_t n_traj) {
+    return {cm.n, cm.n_out, cm.windows, ceil_log2_u64(n_traj)};
+}
+
+constexpr uint64_t kDenseWindowAlwaysBytes = 64ull << 20;  // a dense table this small always wins
+constexpr int kDefaultHashBits = 22;                        // 4 Mi slots, 64 MiB: fits in L2
+
+}  // namespace
+
+void Sim::choose_window_table() {
+    n_bins = (uint64_t)cm.windows << cm.n_out;
+    const int mode = opts.window_table;
+    if (mode < 0 || mode > 2) throw ArgError("window_table must be 0 (auto), 1 (dense) or 2 (hash)");
+    if (opts.window_hash_bits != 0 && (opts.window_hash_bits < 10 || opts.window_hash_bits > 31))
+        throw ArgError("window_hash_bits must be 0 or within 10..31");
+    const bool hash_ok = n_bins <= (1ull << 31);  // bins as u32 in the compacted read-back
+    if (mode == 2 && !hash_ok) throw ModelError("window hash table: more than 2^31 (window, output state) bins");
+    // Every trajectory holds at least one output state per window, so trajectories x windows
+    // estimates the bins a run reaches; the hash table (16 B a slot, at most half full) pays when
+    // that is well below the dense table's bins.
+    const uint64_t est = std::min<uint64_t>(n_bins, n_traj * (uint64_t)cm.windows);
+    const bool hash = mode == 2 || (mode == 0 && hash_ok && n_bins * 8 > kDenseWindowAlwaysBytes && est * 8 <= n_bins);
+    int bits = 0;
+    if (hash) {
+        bits = std::min(kDefaultHashBits, std::max(10, ceil_log2_u64(2 * est)));
+        if (opts.window_hash_bits) {
+            bits = opts.window_hash_bits;
+        } else if (mode == 0) {
+            std::lock_guard<std::mutex> lock(g_window_mu);
+            auto it = g_window_bits.find(window_class(cm, n_traj));
+            if (it != g_window_bits.end()) bits = it->second;
+        }
+    }
+    if (bits == 0)
+        set_window_table(0);
+    else
+        grow_window_table(bits);  // dense instead when the hash table would be the larger
+}
+
+void Sim::set_window_table(int bits) {
+    if (hslots) {
+        cudaFree(hslots);
+        hslots = nullptr;
+    }
+    if (bits == 0) {
+        if (!dense_hist)
+            dense_hist = static_cast<unsigned long long*>(raw_alloc(n_bins * 8, "dense window table"));
+    } else {
+        if (dense_hist) {
+            cudaFree(dense_hist);
+            dense_hist = nullptr;
+        }
+        hslots = static_cast<unsigned long long*>(raw_alloc((size_t)16 << bits, "window hash table"));
+    }
+    hash_bits = bits;
+    prm.hist = dense_hist;
+    prm.hslots = hslots;
+    prm.hash_bits = bits;
+}
+
+// A larger hash table for the next run: 2^bits slots, or (auto mode) the dense table once the
+// hash table would take more than half of the dense table's bytes.
+void Sim::grow_window_table(int bits) {
+    const bool forced = opts.window_table == 2;
+    if (!forced && (bits > 31 || ((uint64_t)16 << bits) > n_bins * 4)) {
+        set_window_table(0);
+        return;
+    }
+    if (bits > 31) throw ModelError("window hash table: more than 2^31 slots needed");
+    set_window_table(bits);
+}
+
 Sim::~Sim() {
+    for (void* p : {(void*)dense_hist, (void*)hslots, (void*)wc_bitmap, (void*)wc_wpre, (void*)wc_chunk,
+                    (void*)wc_total, (void*)wc_bin, (void*)wc_sum})
+        if (p) cudaFree(p);
     if (ev0) cudaEventDestroy(ev0);
     if (ev1) cudaEventDestroy(ev1);
     if (evk0) cudaEventDestroy(evk0);
@@ -263,7 +364,7 @@ void Sim::create(const CompiledModel& model, const std::vector<std::string>& nod
     prm.n_traj = n_traj;
     prm.traj_base = o.traj_base;
     // results
-    prm.hist = dalloc<unsigned long long>((size_t)(cm.windows * S), owned);
+    choose_window_table();
     prm.th_hist = dalloc<unsigned long long>((size_t)cm.windows, owned);
     prm.final_hist = dalloc<unsigned int>((size_t)S, owned);
     fp_capacity = (uint32_t)n_traj;
@@ -459,9 +560,42 @@ std::mutex& kernel_attr_mutex() {
 
 void Sim::run(cudaStream_t stream) {
     ck(cudaSetDevice(device), "cudaSetDevice");
+    window_reruns = 0;
+    if (pending_hash_bits > 0) {  // the growth the last run asked for (its results are read by now)
+        grow_window_table(pending_hash_bits);
+        pending_hash_bits = 0;
+    }
+    for (;;) {
+        launch(stream);
+        const uint32_t err = summary.device_error;
+        // a full hash table: nothing else went wrong, so the same run is repeated on a table four
+        // times larger (every trajectory depends only on its id: the repeat is exact)
+        if (hash_bits > 0 && err == (uint32_t)DEV_ERR_WINDOW_TABLE) {
+            grow_window_table(hash_bits + 2);
+            ++window_reruns;
+            continue;
+        }
+        break;
+    }
+    summary.window_reruns = window_reruns;
+    if (summary.device_error) throw DeviceError("device error flags 0x" + std::to_string(summary.device_error));
+    // keep the table at most half full: the next run starts on a larger one (this run's results
+    // stay in the current table until then)
+    if (hash_bits > 0 && 2 * summary.window_entries > (1ull << hash_bits))
+        pending_hash_bits = std::max(hash_bits + 1, ceil_log2_u64(2 * summary.window_entries));
+    if (opts.window_table == 0 && opts.window_hash_bits == 0) {
+        std::lock_guard<std::mutex> lock(g_window_mu);
+        g_window_bits[window_class(cm, n_traj)] = pending_hash_bits > 0 ? pending_hash_bits : hash_bits;
+    }
+}
+
+void Sim::launch(cudaStream_t stream) {
     const uint64_t S = 1ull << cm.n_out;
     ck(cudaEventRecord(ev0, stream), "cudaEventRecord");
-    ck(cudaMemsetAsync(prm.hist, 0, cm.windows * S * 8, stream), "cudaMemsetAsync");
+    if (hash_bits > 0)
+        ck(cudaMemsetAsync(hslots, 0, (size_t)16 << hash_bits, stream), "cudaMemsetAsync");
+    else
+        ck(cudaMemsetAsync(dense_hist, 0, n_bins * 8, stream), "cudaMemsetAsync");
     ck(cudaMemsetAsync(prm.th_hist, 0, cm.windows * 8, stream), "cudaMemsetAsync");
     ck(cudaMemsetAsync(prm.final_hist, 0, S * 4, stream), "cudaMemsetAsync");
     ck(cudaMemsetAsync(prm.fp_count, 0, 4, stream), "cudaMemsetAsync");
@@ -517,9 +651,11 @@ void Sim::run(cudaStream_t stream) {
     summary.block_size = block;
     summary.grid_size = grid;
     summary.lane_update = layout == MBG_LAYOUT_LANE && !lane_coop ? 1 : 0;
+    summary.window_table = hash_bits > 0 ? 2 : 1;
+    summary.window_hash_bits = hash_bits;
+    summary.window_entries = hash_bits > 0 ? hc[CNT_WIN_ENTRIES] : 0;
     ran = true;
     fetched = false;
-    if (summary.device_error) throw DeviceError("device error flags 0x" + std::to_string(summary.device_error));
 }
 
 void Sim::fetch() {
@@ -527,12 +663,59 @@ void Sim::fetch() {
     if (fetched) return;
     ck(cudaSetDevice(device), "cudaSetDevice");
     const uint64_t S = 1ull << cm.n_out;
-    hist.resize(cm.windows * S);
     th.resize(cm.windows);
     fin.resize(S);
-    ck(cudaMemcpy(hist.data(), prm.hist, hist.size() * 8, cudaMemcpyDeviceToHost), "cudaMemcpy D2H");
     ck(cudaMemcpy(th.data(), prm.th_hist, th.size() * 8, cudaMemcpyDeviceToHost), "cudaMemcpy D2H");
     ck(cudaMemcpy(fin.data(), prm.final_hist, fin.size() * 4, cudaMemcpyDeviceToHost), "cudaMemcpy D2H");
+    // window sums: the non-zero bins in increasing order
+    wbin.clear();
+    wsum.clear();
+    if (hash_bits == 0 && n_bins <= (1ull << 20)) {
+        // a small dense table (at most 8 MiB) is read whole and compacted here
+        std::vector<uint64_t> h(n_bins);
+        ck(cudaMemcpy(h.data(), dense_hist, n_bins * 8, cudaMemcpyDeviceToHost), "cudaMemcpy D2H");
+        for (uint64_t i = 0; i < n_bins; ++i)
+            if (h[i]) {
+                wbin.push_back((uint32_t)i);
+                wsum.push_back(h[i]);
+            }
+    } else {
+        // compacted on the device: only the reached bins are copied
+        if (!wc_bitmap) {
+            const uint64_t words = window_bitmap_words(n_bins);
+            wc_bitmap = static_cast<unsigned*>(raw_alloc(words * 4, "window bitmap"));
+            wc_wpre = static_cast<unsigned*>(raw_alloc(words * 4, "window bitmap prefixes"));
+            wc_chunk = static_cast<unsigned*>(raw_alloc((size_t)window_chunks(n_bins) * 4, "window chunk prefixes"));
+            wc_total = static_cast<unsigned long long*>(raw_alloc(8, "window bin count"));
+        }
+        ck(launch_window_count(dense_hist, hslots, hash_bits, n_bins, wc_bitmap, wc_wpre, wc_chunk, wc_total, sms,
+                               nullptr),
+           "window compaction (count)");
+        unsigned long long total = 0;
+        ck(cudaMemcpy(&total, wc_total, 8, cudaMemcpyDeviceToHost), "cudaMemcpy D2H");
+        if (total > wc_cap) {
+            if (wc_bin) cudaFree(wc_bin);
+            if (wc_sum) cudaFree(wc_sum);
+            wc_bin = nullptr;
+            wc_sum = nullptr;
+            wc_cap = 0;
+            wc_bin = static_cast<unsigned*>(raw_alloc(total * 4, "compacted window bins"));
+            wc_sum = static_cast<unsigned long long*>(raw_alloc(total * 8, "compacted window sums"));
+            wc_cap = total;
+        }
+        if (total) {
+            ck(launch_window_emit(dense_hist, hslots, hash_bits, n_bins, wc_bitmap, wc_wpre, wc_chunk, wc_bin, wc_sum,
+                                  sms, nullptr),
+               "window compaction (emit)");
+            wbin.resize(total);
+            wsum.resize(total);
+            ck(cudaMemcpy(wbin.data(), wc_bin, total * 4, cudaMemcpyDeviceToHost), "cudaMemcpy D2H");
+            ck(cudaMemcpy(wsum.data(), wc_sum, total * 8, cudaMemcpyDeviceToHost), "cudaMemcpy D2H");
+        }
+    }
+    wstart.assign((size_t)cm.windows + 1, 0);
+    for (uint32_t b : wbin) ++wstart[(b >> cm.n_out) + 1];
+    for (int w = 0; w < cm.windows; ++w) wstart[w + 1] += wstart[w];
     // fixed points: representatives, counts, then their states
     const uint32_t nu = (uint32_t)summary.fixed_point_states;
     std::vector<uint32_t> words((size_t)nu * cm.words), cnt(nu);

@@ -52,9 +52,36 @@ public:
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, evk0 = nullptr, evk1 = nullptr;
     std::vector<void*> owned;
 
+    // Window sums: the dense windows x 2^n_out table, or (hash_bits > 0) the window hash table of
+    // 2^hash_bits slots (SimParams::hslots). Both are re-sized between runs, so they are owned
+    // here rather than in `owned`.
+    uint64_t n_bins = 0;               // windows << n_out
+    int hash_bits = 0;
+    unsigned long long* dense_hist = nullptr;
+    unsigned long long* hslots = nullptr;
+    int window_reruns = 0;             // runs repeated with a larger hash table by the last mbg_sim_run
+    int pending_hash_bits = 0;         // > 0: the next run starts on a hash table of this size
+    void choose_window_table();        // at create: dense or hash (mbg_sim_opts::window_table)
+    void set_window_table(int bits);   // 0: dense; allocates the table and points prm at it
+    void grow_window_table(int bits);  // hash table of 2^bits slots, or dense when that is smaller
+    void launch(cudaStream_t stream);  // one attempt of mbg_sim_run: clear, simulate, aggregate
+    // Compaction scratch (window_table.cu), allocated at the first read-back of a large table.
+    unsigned* wc_bitmap = nullptr;
+    unsigned* wc_wpre = nullptr;
+    unsigned* wc_chunk = nullptr;
+    unsigned long long* wc_total = nullptr;
+    unsigned* wc_bin = nullptr;
+    unsigned long long* wc_sum = nullptr;
+    uint64_t wc_cap = 0;
+
     bool ran = false, fetched = false;
     mbg_run_summary summary{};
-    std::vector<uint64_t> hist, th;
+    // Non-zero window bins in increasing order (bin = window << n_out | output state) with their
+    // sums (time x 2^32, or counts); entries of window w are [wstart[w], wstart[w + 1]).
+    std::vector<uint32_t> wbin;
+    std::vector<uint64_t> wsum;
+    std::vector<size_t> wstart;
+    std::vector<uint64_t> th;
     std::vector<uint32_t> fin;
     std::vector<FixedPoint> fixed;
 };
@@ -64,7 +91,7 @@ void write_probtraj_csv(const Sim& s, const std::string& path);
 void write_fp_csv(const Sim& s, const std::string& path);
 void write_final_states_csv(const Sim& s, const std::string& path);
 void print_results(const Sim& s, std::ostream& os);
-double window_prob(const Sim& s, size_t idx);
+double window_prob(const Sim& s, uint64_t sum);  // probability of a window bin with this sum
 double window_th(const Sim& s, int w);
 std::string state_string(const std::vector<std::string>& names, const std::vector<uint32_t>& words, int n);
 std::string out_state_string(const Sim& s, uint32_t idx);
