@@ -83,11 +83,11 @@ typedef struct {
                                   per trajectory without timing; 0: autotune */
     int32_t lane_update;       /* LANE: readers of a flipped node updated 0: warp-cooperatively
                                   (default), 1: by their own lane; AUTO times both */
-    int32_t window_table;      /* where the window sums accumulate: 0 auto (the dense table while it
-                                  is at most 64 MiB or the trajectories x windows exceed 1/8 of the
-                                  bins, else the hash table), 1 the dense windows x 2^outputs table
-                                  (the reference's layout), 2 an open-addressed hash table of the
-                                  (window, output state) bins reached, grown and re-run when full */
+    int32_t window_table;      /* where the window sums accumulate: 0 auto (the dense table up to
+                                  2 GiB, the faster one; the hash table beyond), 1 the dense
+                                  windows x 2^outputs table (the reference's layout), 2 an
+                                  open-addressed hash table of the (window, output state) bins
+                                  reached, grown and re-run when full */
     int32_t window_hash_bits;  /* hash table: log2 of its initial slot count (10..31); 0 automatic */
 } mbg_sim_opts;
 

@@ -121,3 +121,36 @@ def test_batch_probabilities_are_normalised():
         P, _ = batch.probtraj(i)
         assert np.allclose(P.sum(axis=1), 1.0, atol=1e-6)
         assert abs(batch.final_states(i).sum() - 1.0) < 1e-12
+
+
+def test_sweep_shaped_batch_against_oracle():
+    """Sweep instances from 50 to ~2000 nodes (the sweep workload's range, 8 outputs, lognormal
+    rates, max_time 30, tick 0.5) in one batched launch, each compared with the oracle directly:
+    window sums, TH, final states and fixed points of every instance."""
+    import oracle
+
+    from helpers import TWO32
+    nets = sorted((synth.sweep_instance(i) for i in range(64)), key=lambda net: len(net.names))
+    picked = [nets[q] for q in (0, 16, 32, 48, 63)]  # smallest, quartiles, largest of 64
+    sizes = [len(net.names) for net in picked]
+    assert min(sizes) < 100 and max(sizes) > 1500
+    texts = [(net.bnd(), net.cfg(sample_count=300)) for net in picked]
+    models = [mbg.Model.from_strings(b, c) for b, c in texts]
+    seeds = [101 + i for i in range(len(models))]
+    batch = mbg.Batch(models, n_traj=[300] * len(models), seeds=seeds).run()
+    for i, ((b, c), m) in enumerate(zip(texts, models)):
+        orc = oracle.run(b, c, frac_bits=m.info.frac_bits, n_traj=300, seed=seeds[i], keep_trajectories=True)
+        n_ties = int((orc.ties != 0).sum())
+        raw, th = batch.probtraj_raw(i)
+        dev = raw.astype(np.float64) / TWO32
+        scale = 300 * m.info.time_tick
+        tol = 1e-5 * scale + (n_ties + 1) * m.info.time_tick * 1.01
+        assert np.abs(dev - orc.dense_hist()).max() <= tol, f"instance {i} ({sizes[i]} nodes): window sums"
+        assert np.allclose(th / TWO32, orc.th, rtol=1e-4, atol=1e-4 * scale + n_ties * 5 * m.info.time_tick)
+        fin = np.rint(batch.final_states(i) * 300)
+        assert np.abs(fin - orc.final).sum() <= 2 * n_ties, f"instance {i}: final states"
+        assert batch.summary(i)["transitions"] == orc.counters["transitions"] or n_ties > 0
+        fs, fp = batch.fixed_points(i)
+        ofix = orc.states[orc.status == 2]
+        if n_ties == 0:
+            assert len(fs) == (len(np.unique(ofix, axis=0)) if len(ofix) else 0), f"instance {i}: fixed points"

@@ -114,12 +114,27 @@ def test_wide_node_parity(layout):
 
 @pytest.mark.parametrize("layout", [mbg.LAYOUT_WARP, mbg.LAYOUT_LANE])
 def test_large_network_parity(layout):
+    """The 5000-node workload at its own max_time (20) and tick (0.2): 256 trajectories of about
+    7000 transitions each, every window compared."""
     net = synth.large()
-    bnd, cfg = net.bnd(), net.cfg(sample_count=24, max_time=5)
-    model, sim = run_device(bnd, cfg, 24, layout=layout)
-    orc = run_oracle(bnd, cfg, model, 24)
+    bnd, cfg = net.bnd(), net.cfg(sample_count=256)
+    model, sim = run_device(bnd, cfg, 256, layout=layout)
+    assert model.info.max_time == 20.0 and model.info.windows == 100
+    orc = run_oracle(bnd, cfg, model, 256)
+    assert orc.counters["transitions"] > 256 * 1000
     compare_trajectories(sim, orc)
-    compare_histograms(model, sim, orc, 24)
+    compare_histograms(model, sim, orc, 256)
+
+
+@pytest.mark.parametrize("layout", [mbg.LAYOUT_AUTO, "lane-serial"])
+def test_medium_network_parity_2000(layout):
+    """2000 trajectories of the 1000-node workload, the autotuned kernel included."""
+    net = synth.medium()
+    bnd, cfg = net.bnd(), net.cfg(sample_count=2000)
+    model, sim = run_device(bnd, cfg, 2000, **layout_kw(layout))
+    orc = run_oracle(bnd, cfg, model, 2000)
+    compare_trajectories(sim, orc)
+    compare_histograms(model, sim, orc, 2000)
 
 
 @pytest.mark.parametrize("layout", [mbg.LAYOUT_AUTO, mbg.LAYOUT_WARP, mbg.LAYOUT_LANE, "lane-serial"])

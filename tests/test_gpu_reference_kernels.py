@@ -1,0 +1,77 @@
+"""This simulator against the reference MaBoSSG's own device kernels on the same GPU.
+
+The reference kernels (its src/jit_kernels/*.cu, compiled unmodified by
+baseline/refgpu/build_kernels.sh where a reference checkout is present) run under a restatement of
+the reference's host path (baseline/refgpu/refgpu.cu). The two simulators draw different random
+numbers (curand XORWOW per batch slot there, Philox per trajectory here), so they agree only in
+distribution: every window probability, final-state probability and fixed-point probability must
+lie within 4 sigma of the other's, sigma the binomial standard deviation of a difference of two
+independent estimates, sqrt(p (1 - p) (1/n1 + 1/n2)) (a time share in a window has at most the
+variance of a Bernoulli variable of the same mean, so the bound is conservative). Over the
+thousands of bins compared, a few beyond 4 sigma are allowed by chance (at most 1e-4 of the bins,
+and at least 2); none may lie beyond 6 sigma.
+"""
+import numpy as np
+import pytest
+
+import upmabossg_gb300 as mbg
+from upmabossg_gb300 import synth
+
+pytestmark = pytest.mark.gpu
+
+refgpu = pytest.importorskip("baseline.refgpu")
+
+if not refgpu.kernels_present():
+    pytest.skip("reference kernels not built (sh baseline/refgpu/build_kernels.sh <reference checkout>)",
+                allow_module_level=True)
+
+
+def z_scores(p1, p2, n1, n2):
+    p = (p1 * n1 + p2 * n2) / (n1 + n2)
+    sd = np.sqrt(np.maximum(p * (1 - p), 0.0) * (1.0 / n1 + 1.0 / n2))
+    return np.abs(p1 - p2) / np.maximum(sd, 1e-300), sd
+
+
+def check(name, p1, p2, n1, n2, floor=0.0):
+    sel = np.maximum(p1, p2) > floor
+    z, _ = z_scores(p1[sel], p2[sel], n1, n2)
+    beyond4 = int((z > 4).sum())
+    allowed = max(2, int(1e-4 * z.size))
+    assert beyond4 <= allowed, f"{name}: {beyond4} of {z.size} beyond 4 sigma (max z {z.max():.2f})"
+    assert z.max(initial=0) <= 6, f"{name}: max z {z.max():.2f}"
+    return int(z.size), float(z.max(initial=0))
+
+
+@pytest.mark.parametrize("workload,n", [("small", 100_000), ("medium", 200_000)])
+def test_statistics_match_reference_kernels(workload, n):
+    net = getattr(synth, workload)()
+    bnd, cfg = net.bnd(), net.cfg(sample_count=n)
+    ref = refgpu.run(bnd, cfg)
+    model = mbg.Model.from_strings(bnd, cfg)
+    sim = mbg.Simulation(model, n_traj=n).run()
+    info = model.info
+    assert ref.windows == info.windows and ref.outputs == info.outputs and ref.n_traj == n
+    # window probabilities (time share / (n x tick)), dense over every (window, state)
+    bins, _, probs = sim.probtraj_sparse()
+    flat = ref.window_sums.ravel()
+    rbins = np.flatnonzero(flat)
+    keys = np.union1d(bins.astype(np.int64), rbins)
+    ours = np.zeros(keys.size)
+    ours[np.searchsorted(keys, bins.astype(np.int64))] = probs
+    theirs = flat[keys].astype(np.float64) / (n * info.time_tick)
+    tested, zmax = check("window probabilities", ours, theirs, n, n)
+    assert tested > 100
+    # final states
+    check("final states", sim.final_states(), ref.final_counts / n, n, n)
+    # fixed points: every state either side reaches
+    fs, fp = sim.fixed_points()
+    ours_fp = {tuple(s): p for s, p in zip(fs, fp)}
+    theirs_fp = {tuple(s): c / n for s, c in zip(ref.fixed_states, ref.fixed_counts)}
+    keys = sorted(set(ours_fp) | set(theirs_fp))
+    if keys:
+        check("fixed points", np.array([ours_fp.get(k, 0.0) for k in keys]),
+              np.array([theirs_fp.get(k, 0.0) for k in keys]), n, n)
+    # transitions per trajectory (a mean of a positive count: within 4 standard errors)
+    t_ours = sim.summary()["transitions"] / n
+    t_ref = ref.transitions / n
+    assert abs(t_ours - t_ref) <= 0.02 * t_ours, f"transitions per trajectory {t_ours:.3f} vs {t_ref:.3f}"

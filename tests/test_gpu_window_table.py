@@ -85,12 +85,31 @@ def test_hash_table_against_oracle():
     compare_histograms(model, sim, orc, 4000)
 
 
+def wide_output_network(outputs=24, windows=40):
+    """A random network whose 24 output nodes make a 2^24-state output space: windows x 2^24 bins
+    (40 windows: 5.4 GB as a dense table), of which a few thousand trajectories reach a sliver."""
+    rng = np.random.default_rng(9)
+    n = outputs + 8
+    names = [f"W{i}" for i in range(n)]
+    lines = []
+    for i, nm in enumerate(names):
+        a, b = rng.choice([x for x in names if x != nm], size=2, replace=False)
+        logic = f"({a} & !{b})" if i % 2 else f"({a} | {b})"
+        lines.append(f"Node {nm} {{ logic = {logic}; rate_up = @logic ? 1 : 0; rate_down = @logic ? 0 : 1; }}\n")
+    cfg = "".join(f"{nm}.is_internal = {0 if i < outputs else 1};\n" for i, nm in enumerate(names))
+    cfg += f"max_time = {windows * 0.5};\ntime_tick = 0.5;\nsample_count = 3000;\nseed_pseudorandom = 5;\n"
+    return "".join(lines), cfg
+
+
 def test_automatic_choice():
-    small, medium = synth.small(), synth.medium()
-    _, s = simulate(small.bnd(), small.cfg(), 0, 0)  # 1e5 trajectories x 100 windows << 100 x 2^20 bins
-    assert s.summary()["window_table"] == HASH
-    _, m = simulate(medium.bnd(), medium.cfg(), 50000, 0)  # 100 x 2^10 bins: 800 KiB dense
-    assert m.summary()["window_table"] == DENSE
+    small = synth.small()
+    _, s = simulate(small.bnd(), small.cfg(), 2000, 0)  # 100 x 2^20 bins: 839 MB dense, the faster table
+    assert s.summary()["window_table"] == DENSE
+    bnd, cfg = wide_output_network()
+    model, h = simulate(bnd, cfg, 3000, 0)  # 40 x 2^24 bins: 5.4 GB dense, beyond the 2 GiB the auto mode allows
+    assert model.info.outputs == 24 and h.summary()["window_table"] == HASH
+    _, d = simulate(bnd, cfg, 3000, DENSE)
+    same_windows(d, h)
 
 
 def test_sparse_read_equals_dense_read():

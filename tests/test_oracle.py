@@ -86,7 +86,7 @@ def test_oracle_matches_reference_goldens(name, n):
         s = sigma(0.5 * (p_ref + p_orc), n_ref, n)
         z = abs(p_ref - p_orc) / s
         worst = max(worst, z)
-        assert z <= 4.5, f"{name} {what}: reference {p_ref} oracle {p_orc} ({z:.1f} sigma)"
+        assert z <= 4.0, f"{name} {what}: reference {p_ref} oracle {p_orc} ({z:.1f} sigma)"
 
     # final points (final_states.cpp:53-66)
     orc_final = {out_key(m, i): c / n for i, c in enumerate(r.final) if c}

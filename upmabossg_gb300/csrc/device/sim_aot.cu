@@ -230,6 +230,8 @@ cudaError_t launch_fp_aggregate_batch(const SimParams* params, const FpSlots* fp
 
 cudaError_t launch_sim_warp(const SimParams& p, bool cached_index, int grid, int block, size_t smem,
                             cudaStream_t stream) {
+    if (p.hash_bits > 0) return launch((void (*)(SimParams))sim_kernel_hash(3, cached_index), grid, block, smem,
+                                       stream, p);
     return launch(cached_index ? mbg_sim_warp : mbg_sim_warp_gather, grid, block, smem, stream, p);
 }
 
@@ -249,6 +251,8 @@ cudaError_t sim_warp_occupancy(bool cached_index, int block, size_t smem, int* b
 
 cudaError_t launch_sim_lane(const SimParams& p, bool coop, bool full, int grid, int block, size_t smem,
                             cudaStream_t stream) {
+    if (p.hash_bits > 0)
+        return launch((void (*)(SimParams))sim_kernel_hash(full ? 4 : 0, coop), grid, block, smem, stream, p);
     auto k = full ? (coop ? mbg_sim_lane_coop_full : mbg_sim_lane_full) : (coop ? mbg_sim_lane_coop : mbg_sim_lane);
     return launch(k, grid, block, smem, stream, p);
 }
@@ -317,9 +321,10 @@ cudaError_t shared_limits(const void* f, const int* blocks, const size_t* smems,
 }  // namespace
 
 cudaError_t sim_kernel_limits(int kernel, bool variant, const int* blocks, const size_t* smems, const int* want,
-                              int count) {
-    const void* f = nullptr;
-    switch (kernel) {
+                              int count, bool hash) {
+    const void* f = hash ? sim_kernel_hash(kernel, variant) : nullptr;
+    if (hash && !f) return cudaErrorInvalidValue;
+    if (!f) switch (kernel) {
         case 0: f = variant ? (const void*)mbg_sim_lane_coop : (const void*)mbg_sim_lane; break;
         case 1: f = variant ? (const void*)mbg_sim_lane_batch_coop : (const void*)mbg_sim_lane_batch; break;
         case 4: f = variant ? (const void*)mbg_sim_lane_coop_full : (const void*)mbg_sim_lane_full; break;

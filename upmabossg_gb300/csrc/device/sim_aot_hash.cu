@@ -1,0 +1,59 @@
+// The single-simulation kernels of sim_aot.cu compiled with their window sums going to the window
+// hash table (MBG_WINDOW_HASH, sim_core.cuh:bin_add) instead of the dense table. Same layouts,
+// same arithmetic; launched when a run's table is the hash table (large, sparse output spaces).
+#define MBG_WINDOW_HASH 1
+
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <utility>
+
+#include "philox.h"
+#include "sim_types.h"
+#include "sim_core.cuh"
+#include "sim_warp.cuh"
+#include "sim_lane.cuh"
+#include "kernels.h"
+
+namespace mbg {
+
+extern "C" __global__ void __launch_bounds__(256, 4) mbg_sim_warp_hash(const SimParams p) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    sim_warp_body<true>(p, smem);
+}
+
+extern "C" __global__ void __launch_bounds__(256, 4) mbg_sim_warp_gather_hash(const SimParams p) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    sim_warp_body<false>(p, smem);
+}
+
+extern "C" __global__ void __launch_bounds__(256, 3) mbg_sim_lane_hash(const SimParams p) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    sim_lane_body<false, false>(p, smem);
+}
+
+extern "C" __global__ void __launch_bounds__(256, 3) mbg_sim_lane_coop_hash(const SimParams p) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    sim_lane_body<true, false>(p, smem);
+}
+
+extern "C" __global__ void __launch_bounds__(256, 3) mbg_sim_lane_full_hash(const SimParams p) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    sim_lane_body<false, true>(p, smem);
+}
+
+extern "C" __global__ void __launch_bounds__(256, 3) mbg_sim_lane_coop_full_hash(const SimParams p) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    sim_lane_body<true, true>(p, smem);
+}
+
+const void* sim_kernel_hash(int kernel, bool variant) {
+    switch (kernel) {
+        case 0: return variant ? (const void*)mbg_sim_lane_coop_hash : (const void*)mbg_sim_lane_hash;
+        case 4: return variant ? (const void*)mbg_sim_lane_coop_full_hash : (const void*)mbg_sim_lane_full_hash;
+        case 3: return variant ? (const void*)mbg_sim_warp_hash : (const void*)mbg_sim_warp_gather_hash;
+        default: return nullptr;  // the batched kernels always use the dense tables
+    }
+}
+
+}  // namespace mbg

@@ -70,6 +70,14 @@ __device__ __forceinline__ void win_begin(WindowAcc& a, const SimParams& p, unsi
     a.th = 0.f;
 }
 
+// Window sums go to the dense table or to the hash table; which one is fixed when a kernel is
+// compiled (MBG_WINDOW_HASH 0 or 1): the dense kernels carry no trace of the hash path, whose
+// probe loop, inlined at every flush, cost the 5000-node warp kernel 6% when both were compiled in
+// behind a run-time branch. The host launches the variant that matches the run's table.
+#ifndef MBG_WINDOW_HASH
+#define MBG_WINDOW_HASH 0
+#endif
+
 // Probes one insertion into the window hash table may take before it gives up (the host then
 // re-runs with a larger table). The host keeps the table at most half full.
 #define MBG_WINDOW_PROBES 512u
@@ -80,22 +88,30 @@ __device__ __forceinline__ unsigned long long win_hash(unsigned long long key, i
 }
 
 // Adds v to the window sum of bin (window w, output state s): one atomic on the dense table, or,
-// in hash mode, a claim-or-match CAS on the key followed by an atomic add on the sum. The sums are
-// integers, so the result does not depend on the order of the additions or of the claims.
+// in the hash kernels, a claim-or-match of the bin's slot followed by an atomic add on its sum.
+// The sums are integers, so the result depends neither on the order of the additions nor on which
+// trajectory claimed a slot. A slot's key, once set, never changes during a run, so a cached load
+// that finds the key is exact and skips the CAS; a load that finds the slot empty (possibly stale)
+// falls through to the CAS, which returns the truth.
 __device__ __forceinline__ void bin_add(const SimParams& p, int w, unsigned s, unsigned long long v) {
     const unsigned long long bin = ((unsigned long long)w << p.n_out) | s;
-    if (p.hash_bits == 0) {
-        atomicAdd(p.hist + bin, v);
-        return;
-    }
+#if MBG_WINDOW_HASH
     const unsigned long long key = bin + 1ull;
     const unsigned long long mask = (1ull << p.hash_bits) - 1ull;
     unsigned long long h = win_hash(key, p.hash_bits);
     for (unsigned probe = 0; probe < MBG_WINDOW_PROBES; ++probe) {
-        const unsigned long long cur = atomicCAS(p.hslots + 2 * h, 0ull, key);
-        if (cur == 0ull || cur == key) {
-            atomicAdd(p.hslots + 2 * h + 1, v);
-            if (cur == 0ull) atomicAdd(p.counters + CNT_WIN_ENTRIES, 1ull);
+        unsigned long long* slot = p.hslots + 2 * h;
+        unsigned long long cur = __ldca(slot);
+        if (cur == 0ull) {
+            cur = atomicCAS(slot, 0ull, key);
+            if (cur == 0ull) {
+                atomicAdd(slot + 1, v);
+                atomicAdd(p.counters + CNT_WIN_ENTRIES, 1ull);
+                return;
+            }
+        }
+        if (cur == key) {
+            atomicAdd(slot + 1, v);
             return;
         }
         h = (h + 1ull) & mask;
@@ -103,6 +119,9 @@ __device__ __forceinline__ void bin_add(const SimParams& p, int w, unsigned s, u
         if ((probe & 15u) == 15u && (*(volatile const unsigned*)p.error_flag & (unsigned)DEV_ERR_WINDOW_TABLE)) return;
     }
     atomicOr(p.error_flag, (unsigned)DEV_ERR_WINDOW_TABLE);
+#else
+    atomicAdd(p.hist + bin, v);
+#endif
 }
 
 __device__ __forceinline__ void win_flush_run(WindowAcc& a, const SimParams& p, unsigned long long t_end,

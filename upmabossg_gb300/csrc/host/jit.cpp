@@ -100,8 +100,9 @@ double jit_compile_only(const std::string& model_src) {
     return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
 }
 
-void* jit_thread_kernel(const std::string& model_src, double& compile_ms) {
-    std::string src;
+void* jit_thread_kernel(const std::string& model_src, double& compile_ms, bool window_hash) {
+    // the window-table variant is chosen when the kernel is compiled (sim_core.cuh: MBG_WINDOW_HASH)
+    std::string src = window_hash ? "#define MBG_WINDOW_HASH 1\n" : "";
     for (int i = 0; i < kJitHeaderCount; ++i) src += kJitHeaders[i];
     src += model_src;
     int major = 0, minor = 0;

@@ -242,8 +242,8 @@ std::tuple<int, int, int, int> window_class(const CompiledModel& cm, uint64_t n_
     return {cm.n, cm.n_out, cm.windows, ceil_log2_u64(n_traj)};
 }
 
-constexpr uint64_t kDenseWindowAlwaysBytes = 64ull << 20;  // a dense table this small always wins
-constexpr int kDefaultHashBits = 22;                        // 4 Mi slots, 64 MiB: fits in L2
+constexpr uint64_t kDenseWindowMaxBytes = 2ull << 30;  // auto: dense tables up to 2 GiB
+constexpr int kDefaultHashBits = 22;                    // 4 Mi slots, 64 MiB: fits in L2
 
 }  // namespace
 
@@ -255,11 +255,14 @@ void Sim::choose_window_table() {
         throw ArgError("window_hash_bits must be 0 or within 10..31");
     const bool hash_ok = n_bins <= (1ull << 31);  // bins as u32 in the compacted read-back
     if (mode == 2 && !hash_ok) throw ModelError("window hash table: more than 2^31 (window, output state) bins");
-    // Every trajectory holds at least one output state per window, so trajectories x windows
-    // estimates the bins a run reaches; the hash table (16 B a slot, at most half full) pays when
-    // that is well below the dense table's bins.
+    // Measured on the GB300 (20-node workload, 100 windows x 2^20 states, 839 MB dense): the dense
+    // table's fire-and-forget atomics keep the simulation kernel at 0.9 ms, while the hash table's
+    // claim-or-match waits on an L2 round trip per flush (1.5-1.9 ms); the read-back is compacted on
+    // the device either way. So the dense table is used while it is affordable and the hash table
+    // only beyond that, where it holds what a run reaches: every trajectory holds at least one
+    // output state per window, so trajectories x windows estimates the reached bins.
     const uint64_t est = std::min<uint64_t>(n_bins, n_traj * (uint64_t)cm.windows);
-    const bool hash = mode == 2 || (mode == 0 && hash_ok && n_bins * 8 > kDenseWindowAlwaysBytes && est * 8 <= n_bins);
+    const bool hash = mode == 2 || (mode == 0 && hash_ok && n_bins * 8 > kDenseWindowMaxBytes);
     int bits = 0;
     if (hash) {
         bits = std::min(kDefaultHashBits, std::max(10, ceil_log2_u64(2 * est)));
@@ -603,18 +606,25 @@ void Sim::launch(cudaStream_t stream) {
     ck(cudaMemsetAsync(prm.error_flag, 0, 4, stream), "cudaMemsetAsync");
     ck(cudaEventRecord(evk0, stream), "cudaEventRecord");
     if (layout == MBG_LAYOUT_THREAD) {
+        if (hash_bits > 0 && !thread_kernel_hash) {
+            double ms = 0;
+            thread_kernel_hash = jit_thread_kernel(generate_thread_model(cm, dl), ms, true);
+            jit_ms += ms;
+        }
         void* args[] = {(void*)&prm};
-        ck(cudaLaunchKernel((const void*)thread_kernel, dim3(grid), dim3(block), args, 0, stream),
+        ck(cudaLaunchKernel((const void*)(hash_bits > 0 ? thread_kernel_hash : thread_kernel), dim3(grid), dim3(block),
+                            args, 0, stream),
            "cudaLaunchKernel(mbg_sim_thread)");
     } else {
         // kernel attributes are process-wide: re-apply this handle's before its launch
         std::lock_guard<std::mutex> lock(kernel_attr_mutex());
         const int want = std::max(1, grid / std::max(1, sms));
         if (layout == MBG_LAYOUT_LANE) {
-            ck(sim_kernel_limits(lane_full ? 4 : 0, lane_coop, &block, &smem, &want, 1), "mbg_sim_lane attributes");
+            ck(sim_kernel_limits(lane_full ? 4 : 0, lane_coop, &block, &smem, &want, 1, hash_bits > 0),
+               "mbg_sim_lane attributes");
             ck(launch_sim_lane(prm, lane_coop, lane_full, grid, block, smem, stream), "launch mbg_sim_lane");
         } else {
-            ck(sim_kernel_limits(3, cached_index, &block, &smem, &want, 1), "mbg_sim_warp attributes");
+            ck(sim_kernel_limits(3, cached_index, &block, &smem, &want, 1, hash_bits > 0), "mbg_sim_warp attributes");
             ck(launch_sim_warp(prm, cached_index, grid, block, smem, stream), "launch mbg_sim_warp");
         }
     }

@@ -40,6 +40,7 @@ public:
     bool lane_full = false;  // palette rates or nodes over 12 regulators: the `_full` lane kernels
     double jit_ms = 0;
     void* thread_kernel = nullptr;
+    void* thread_kernel_hash = nullptr;  // the thread layout's window-hash variant, compiled on first use
     DeviceLayout dl;
     SimParams prm{};
     uint32_t fp_capacity = 0, n_slots = 0;

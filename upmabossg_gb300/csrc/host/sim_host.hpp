@@ -62,7 +62,8 @@ std::string generate_thread_model(const CompiledModel& cm, const DeviceLayout& d
 // Compiles (or fetches from the in-process / on-disk cache) the full NVRTC program made of the
 // shared device headers and `model_src`, loads it on the current device and returns the kernel
 // handle usable with cudaLaunchKernel. `compile_ms` is 0 on a cache hit. Throws mbg::Error.
-void* jit_thread_kernel(const std::string& model_src, double& compile_ms);
+// `window_hash`: the variant whose window sums go to the window hash table.
+void* jit_thread_kernel(const std::string& model_src, double& compile_ms, bool window_hash = false);
 // Compiles without loading (no device needed); returns milliseconds. Throws JitError.
 double jit_compile_only(const std::string& model_src);
 
