@@ -535,7 +535,7 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="medium", choices=sorted(WORKLOADS) + ["sweep", "surrogate"])
+    ap.add_argument("--workload", default="medium", choices=sorted(WORKLOADS) + ["sweep", "surrogate", "l2atomics"])
     ap.add_argument("--layout", type=int, default=0, help="0 autotuned, 1 thread, 2 warp, 3 lane")
     ap.add_argument("--block", type=int, default=0, help="threads per block (0: the layout's default); profiling")
     ap.add_argument("--lane-update", type=int, default=0, help="lane layout: 0 cooperative, 1 per lane; profiling")
@@ -554,6 +554,13 @@ def main():
         line = measure_surrogate()
         line.update({"n_gpus": 1, "higher_is_better": True, "data": "synthetic", "dtype": "bf16"})
         print(json.dumps(line), flush=True)
+        return 0
+    if args.workload == "l2atomics":
+        # the secondary roofline's denominator: u64 atomic adds per second into L2-resident tables
+        import upmabossg_gb300 as mbg
+        rates = {str(d): mbg.l2_atomic_rate(d) for d in (1, 32, 1024, 1 << 16, 1 << 20, 1 << 23)}
+        print(json.dumps({"metric": "L2 u64 atomic adds/s (no return), by distinct addresses", "unit": "atomics/s",
+                          "rates": rates}), flush=True)
         return 0
     if args.workload == "sweep":
         import upmabossg_gb300 as mbg

@@ -89,6 +89,12 @@ typedef struct {
                                   open-addressed hash table of the (window, output state) bins
                                   reached, grown and re-run when full */
     int32_t window_hash_bits;  /* hash table: log2 of its initial slot count (10..31); 0 automatic */
+    uint32_t redraw_period;    /* 0 (default): the exact Gillespie process. 99: the reference build's
+                                  process, whose launches of at most 99 records end without a flip,
+                                  the next launch drawing the same state's holding time again
+                                  (src/simulation_runner.cu:51, src/jit_kernels/simulation.cu:143-147):
+                                  every 99th step draws a holding time but flips nothing. For
+                                  statistical comparison with that build; thread and warp layouts. */
 } mbg_sim_opts;
 
 typedef struct {
@@ -200,6 +206,12 @@ mbg_status mbg_write_fp_csv(mbg_sim* s, const char* prefix);
 mbg_status mbg_write_final_states_csv(mbg_sim* s, const char* prefix);
 /* The reference's stdout report (final points, fixed points, windows) to a file path or "-". */
 mbg_status mbg_print_results(mbg_sim* s, const char* path);
+
+/* Measured 64-bit atomic-add (reduction) throughput of device `device`'s L2: atomics per second
+ * when every thread of a GPU-filling grid adds to `distinct` addresses (a power of two, at most
+ * 2^26: an L2-resident table at up to 512 MiB) with no result returned, the form of the window-sum
+ * flushes. No counterpart in the reference; the denominator of the flushes' roofline. */
+mbg_status mbg_device_l2_atomic_rate(int32_t device, uint32_t distinct, double* atomics_per_s);
 
 /* ---- Batched parameter sweeps --------------------------------------------------------------
  * Many independent simulations ("instances": any models, trajectory counts and seeds) grouped by

@@ -40,6 +40,7 @@ class _Opts(ctypes.Structure):
         ("threads", ctypes.c_int),
         ("max_steps", ctypes.c_uint32),
         ("keep_trajectories", ctypes.c_int),
+        ("redraw_period", ctypes.c_uint32),
         ("legacy_final", ctypes.c_int),
     ]
 
@@ -122,7 +123,7 @@ class OracleResult:
 
 def run(bnd: str, cfg: str, *, frac_bits: int = 0, n_traj: int = 0, seed=None, traj_base: int = 0,
         threads: int = 0, max_steps: int = 0, keep_trajectories: bool = False,
-        legacy_final: bool = False) -> OracleResult:
+        legacy_final: bool = False, redraw_period: int = 0) -> OracleResult:
     L = lib()
     o = _Opts()
     o.n_traj = n_traj
@@ -134,6 +135,7 @@ def run(bnd: str, cfg: str, *, frac_bits: int = 0, n_traj: int = 0, seed=None, t
     o.max_steps = max_steps
     o.keep_trajectories = 1 if keep_trajectories else 0
     o.legacy_final = 1 if legacy_final else 0
+    o.redraw_period = redraw_period
     err = ctypes.create_string_buffer(1024)
     h = L.orc_run(bnd.encode(), cfg.encode(), ctypes.byref(o), err, 1024)
     if not h:

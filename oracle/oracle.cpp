@@ -297,6 +297,14 @@ extern "C" orc_result* orc_run(const char* bnd_text, const char* cfg_text, const
                         }
                         break;
                     }
+                    if (o->redraw_period && (step + 1) % o->redraw_period == 0) {
+                        // the reference's launch segments (simulation_runner.cu:51 with
+                        // simulation.cu:143-147): the segment's last record ends without a flip and
+                        // the next launch draws the holding time of the same state again
+                        t = t1;
+                        ++step;
+                        continue;
+                    }
                     uint64_t rt = mbg::pick_target(d.y, d.z, Q);
                     uint64_t acc = 0;
                     int k = -1;

@@ -41,6 +41,8 @@ typedef struct {
     int threads;         /* 0: hardware concurrency */
     uint32_t max_steps;  /* 0: unlimited */
     int keep_trajectories; /* store per-trajectory end records */
+    uint32_t redraw_period; /* 0: exact Gillespie. 99: the reference's launch segments, in which every
+                            99th step draws its holding time without a flip */
     int legacy_final;    /* final-state histogram after one more flip: the rule of the earlier
                             MaBoSSG build that produced the reference's test/*.res goldens (the
                             current simulation.cu:143-147 ends before that flip) */

@@ -202,3 +202,29 @@ def test_step_limit_is_counted(layout):
     assert np.all(tr[status == 3] == 50)
     orc = run_oracle(bnd, cfg, model, 64, max_steps=50)
     assert np.array_equal(status, orc.status)
+
+
+@pytest.mark.parametrize("workload,n,layout", [("medium", 192, mbg.LAYOUT_WARP), ("mid", 1000, mbg.LAYOUT_WARP),
+                                               ("mid", 1000, mbg.LAYOUT_THREAD)])
+def test_reference_segment_process_parity(workload, n, layout):
+    """redraw_period = 99 (the reference build's launch segments): trajectory for trajectory against
+    the oracle running the same process."""
+    net = synth.medium() if workload == "medium" else synth.sweep_instance(2)
+    bnd, cfg = net.bnd(), net.cfg(sample_count=n)
+    model, sim = run_device(bnd, cfg, n, layout=layout, redraw_period=99)
+    orc = run_oracle(bnd, cfg, model, n, redraw_period=99)
+    exact = run_oracle(bnd, cfg, model, n)
+    assert orc.counters["steps"] > exact.counters["steps"]  # the segment ends are extra steps
+    assert sim.summary()["steps"] == orc.counters["steps"] or orc.counters["time_ties"] > 0
+    compare_trajectories(sim, orc)
+    compare_histograms(model, sim, orc, n)
+
+
+def test_reference_segment_process_needs_thread_or_warp():
+    net = synth.small()
+    m = mbg.Model.from_strings(net.bnd(), net.cfg())
+    with pytest.raises(mbg.MbgError) as e:
+        mbg.Simulation(m, n_traj=100, layout=mbg.LAYOUT_LANE, redraw_period=99)
+    assert e.value.status == 1
+    s = mbg.Simulation(m, n_traj=1000, redraw_period=99).run()  # auto: tuned over thread and warp only
+    assert s.summary()["layout"] in (mbg.LAYOUT_THREAD, mbg.LAYOUT_WARP)

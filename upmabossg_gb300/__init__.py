@@ -35,6 +35,7 @@ EXPORTS = (
     "mbg_surrogate_create", "mbg_surrogate_destroy", "mbg_surrogate_train", "mbg_surrogate_predict",
     "mbg_surrogate_param_count", "mbg_surrogate_get_params", "mbg_surrogate_set_params", "mbg_surrogate_gradients",
     "mbg_surrogate_set_tensor_path", "mbg_surrogate_time_forward", "mbg_surrogate_predict_column",
+    "mbg_device_l2_atomic_rate",
 )
 
 
@@ -77,7 +78,7 @@ class SimOpts(ctypes.Structure):
                 ("max_steps", ctypes.c_uint32), ("block_size", ctypes.c_int32),
                 ("blocks_per_sm", ctypes.c_int32), ("thread_cutoff", ctypes.c_int32),
                 ("lane_update", ctypes.c_int32), ("window_table", ctypes.c_int32),
-                ("window_hash_bits", ctypes.c_int32)]
+                ("window_hash_bits", ctypes.c_int32), ("redraw_period", ctypes.c_uint32)]
 
 
 class RunSummary(ctypes.Structure):
@@ -130,6 +131,7 @@ def lib():
             "mbg_sim_summary": (ctypes.c_int, [vp, ctypes.POINTER(RunSummary)]),
             "mbg_sim_probtraj": (ctypes.c_int, [vp, dp, dp]),
             "mbg_sim_probtraj_raw": (ctypes.c_int, [vp, dp, dp]),
+            "mbg_device_l2_atomic_rate": (ctypes.c_int, [i32, ctypes.c_uint32, dp]),
             "mbg_sim_probtraj_sparse": (ctypes.c_int, [vp, dp, dp, dp, ctypes.c_size_t,
                                                         ctypes.POINTER(ctypes.c_size_t)]),
             "mbg_sim_final_states": (ctypes.c_int, [vp, dp]),
@@ -183,6 +185,13 @@ def _check(st):
 
 def _p(a):
     return a.ctypes.data_as(ctypes.c_void_p) if a is not None else None
+
+
+def l2_atomic_rate(distinct: int, device: int = 0) -> float:
+    """Measured u64 atomic adds per second into `distinct` L2-resident addresses."""
+    r = ctypes.c_double()
+    _check(lib().mbg_device_l2_atomic_rate(device, distinct, ctypes.byref(r)))
+    return r.value
 
 
 def device_count() -> int:
@@ -286,7 +295,7 @@ class Simulation:
 
     def __init__(self, model: Model, n_traj=0, seed=None, layout=LAYOUT_AUTO, record_trajectories=False,
                  max_steps=0, traj_base=0, device=0, block_size=0, blocks_per_sm=0, thread_cutoff=0,
-                 lane_update=0, window_table=0, window_hash_bits=0):
+                 lane_update=0, window_table=0, window_hash_bits=0, redraw_period=0):
         o = SimOpts()
         lib().mbg_sim_opts_default(ctypes.byref(o))
         o.n_traj = int(n_traj)
@@ -304,6 +313,7 @@ class Simulation:
         o.lane_update = lane_update
         o.window_table = window_table
         o.window_hash_bits = window_hash_bits
+        o.redraw_period = redraw_period
         self.model = model
         h = ctypes.c_void_p()
         _check(lib().mbg_sim_create(model._h, ctypes.byref(o), ctypes.byref(h)))

@@ -87,6 +87,8 @@ __device__ void sim_thread_body(const SimParams& p) {
             if (t1 >= p.max_time_fx) {
                 t = p.max_time_fx;
                 status = TRAJ_FINISHED;
+            } else if (p.redraw_period && step % p.redraw_period == 0ull) {
+                t = t1;  // a reference segment ends: the holding time is drawn again, no flip
             } else {
                 const unsigned long long r = pick_target(d.y, d.z, total);
                 const int k = M::pick(p, s, act, r);

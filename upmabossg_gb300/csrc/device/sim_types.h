@@ -96,6 +96,9 @@ struct SimParams {
     double max_time, tick;
     float to_real;  // 2^-frac_bits
     unsigned int max_steps;
+    // The reference's launch segments, on request (0: off): every redraw_period-th step of a
+    // trajectory draws its holding time but does not flip (thread and warp layouts).
+    unsigned int redraw_period;
     unsigned long long seed;
     unsigned long long n_traj;       // trajectories of this launch
     unsigned long long traj_base;    // id of the first trajectory (Philox key part)

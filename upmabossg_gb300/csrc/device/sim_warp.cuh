@@ -294,6 +294,10 @@ __device__ unsigned char warp_trajectory(const SimParams& p, const WarpSmem& m, 
             status = TRAJ_FINISHED;
             break;
         }
+        if (p.redraw_period && step % p.redraw_period == 0ull) {  // a reference segment ends: no flip
+            t = t1;
+            continue;
+        }
         // pick: register prefix (top level), L1 scan (N > 1024), leaf scan
         unsigned long long r = pick_target(dy, dz, total);
         const int tj = prefix_pick(pre, r);

@@ -10,9 +10,15 @@
 // and three over the bitmap (windows x 2^n_out / 8 bytes).
 #include <cuda_runtime.h>
 
+#include <string>
+
+#include "../../../include/mbg.h"
 #include "kernels.h"
 
 namespace mbg {
+
+// Records the message for mbg_last_error() and returns `st` (defined with the C ABI, capi.cpp).
+mbg_status set_error(mbg_status st, const std::string& msg);
 
 namespace {
 
@@ -209,4 +215,57 @@ cudaError_t launch_window_emit(const unsigned long long* hist, const unsigned lo
                               out_sum);
 }
 
+// ---------------------------------------------------------------------------------------------
+// L2 atomic throughput probe: the secondary bound of the simulation kernels, whose window-sum
+// flushes are fire-and-forget 64-bit atomic adds (RED) into an L2-resident table.
+
+namespace {
+
+__global__ void l2_red_probe(unsigned long long* __restrict__ buf, unsigned mask, int iters) {
+    const unsigned tid = blockIdx.x * blockDim.x + threadIdx.x;
+    unsigned a = tid * 2654435761u;
+    for (int i = 0; i < iters; ++i) {
+        atomicAdd(buf + (a & mask), 1ull);
+        a += 0x9E3779B9u;
+    }
+}
+
+}  // namespace
+
 }  // namespace mbg
+
+extern "C" mbg_status mbg_device_l2_atomic_rate(int32_t device, uint32_t distinct, double* atomics_per_s) {
+    if (!atomics_per_s || distinct == 0 || (distinct & (distinct - 1)) != 0 || distinct > (1u << 26))
+        return mbg::set_error(MBG_ERR_ARG, "mbg_device_l2_atomic_rate: distinct must be a power of two <= 2^26");
+    int sms = 0;
+    unsigned long long* buf = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    cudaError_t e = cudaSetDevice(device);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    if (e == cudaSuccess) e = cudaMalloc(&buf, (size_t)distinct * 8);
+    if (e == cudaSuccess) e = cudaMemset(buf, 0, (size_t)distinct * 8);
+    if (e == cudaSuccess) e = cudaEventCreate(&e0);
+    if (e == cudaSuccess) e = cudaEventCreate(&e1);
+    const int iters = 256, block = 256;
+    const unsigned grid = (unsigned)sms * 8u;
+    float best = 0.f;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(block);
+    for (int rep = 0; rep < 4 && e == cudaSuccess; ++rep) {  // the first is a warm-up
+        e = cudaEventRecord(e0, nullptr);
+        if (e == cudaSuccess) e = cudaLaunchKernelEx(&cfg, mbg::l2_red_probe, buf, distinct - 1u, iters);
+        if (e == cudaSuccess) e = cudaEventRecord(e1, nullptr);
+        if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+        float ms = 0.f;
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+        if (e == cudaSuccess && rep > 0 && (best == 0.f || ms < best)) best = ms;
+    }
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    if (buf) cudaFree(buf);
+    if (e != cudaSuccess)
+        return mbg::set_error(MBG_ERR_CUDA, std::string("mbg_device_l2_atomic_rate: ") + cudaGetErrorString(e));
+    *atomics_per_s = (double)grid * block * iters / (best * 1e-3);
+    return mbg::set_error(MBG_OK, "");
+}

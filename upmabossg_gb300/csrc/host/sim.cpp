@@ -363,6 +363,9 @@ void Sim::create(const CompiledModel& model, const std::vector<std::string>& nod
     set_model_constants(prm, cm);
     lane_full = prm.has_palette || cm.max_k > 12;
     prm.max_steps = o.max_steps ? o.max_steps : 0xFFFFFFFFu;
+    prm.redraw_period = o.redraw_period;
+    if (o.redraw_period && o.layout == MBG_LAYOUT_LANE)
+        throw ArgError("redraw_period is supported by the thread and warp layouts");
     prm.seed = seed;
     prm.n_traj = n_traj;
     prm.traj_base = o.traj_base;
@@ -417,14 +420,14 @@ void Sim::create(const CompiledModel& model, const std::vector<std::string>& nod
 }
 
 namespace {
-// Autotuned launch shapes per (model size class ceil(log2 N), pilot size class ceil(log2 pilot)),
-// shared by all simulations of the process: layout and threads per block.
+// Autotuned launch shapes per (model size class ceil(log2 N), pilot size class ceil(log2 pilot),
+// redraw_period set), shared by all simulations of the process: layout and threads per block.
 std::mutex g_tune_mu;
 struct Shape {
     int layout, block;
     bool coop;
 };
-std::map<std::pair<int, int>, Shape> g_tuned;
+std::map<std::tuple<int, int, int>, Shape> g_tuned;
 
 int ceil_log2(uint64_t x) {
     int c = 0;
@@ -437,7 +440,8 @@ void Sim::autotune() {
     // the pilot is large enough to fill the GPU in every layout (or the whole run when smaller),
     // so that the choice reflects occupancy as well as per-transition cost
     const uint64_t pilot = std::min<uint64_t>(n_traj, 1u << 17);
-    const std::pair<int, int> cls{ceil_log2((uint64_t)cm.n), ceil_log2(pilot)};
+    // the lane layout has no redraw_period: such runs are tuned (and cached) apart
+    const std::tuple<int, int, int> cls{ceil_log2((uint64_t)cm.n), ceil_log2(pilot), opts.redraw_period ? 1 : 0};
     {
         std::lock_guard<std::mutex> lock(g_tune_mu);
         auto it = g_tuned.find(cls);
@@ -465,7 +469,7 @@ void Sim::autotune() {
                 if (opts.block_size > 0 && blk != opts.block_size) continue;
                 if (lay != MBG_LAYOUT_LANE && (blk == 64 || coop)) continue;
                 if (lay == MBG_LAYOUT_THREAD && cm.words > 16) continue;
-                if (lay == MBG_LAYOUT_LANE && sim_lane_smem(cm.n, blk) > 227 * 1024) continue;
+                if (lay == MBG_LAYOUT_LANE && (opts.redraw_period || sim_lane_smem(cm.n, blk) > 227 * 1024)) continue;
                 try {
                     setup_layout(lay, blk, coop != 0);
                 } catch (const JitError&) {
