@@ -103,13 +103,13 @@ MBG_LAYOUTS = {"thread": 1, "warp": 2, "lane": 3}
 
 
 PROFILE_KEYS = ("traffic_bytes_per_launch", "issue_slot_utilisation", "warp_instructions_per_transition",
-                "threads_per_warp_instruction")
+                "threads_per_warp_instruction", "branch_uniform_pct", "l2_red_per_transition", "l2_red_peak_per_s")
 
 
-def profile_figures(kernel, workload):
-    """Figures of the committed ncu summary profiles/<kernel>_<workload>.md: its `key: value`
-    lines (PROFILE_KEYS)."""
-    path = os.path.join(ROOT, "profiles", f"{kernel}_{workload}.md")
+def profile_figures(kernel, workload=None):
+    """Figures of the committed ncu summary profiles/<kernel>_<workload>.md (or profiles/<kernel>.md):
+    its `key: value` lines (PROFILE_KEYS)."""
+    path = os.path.join(ROOT, "profiles", f"{kernel}_{workload}.md" if workload else f"{kernel}.md")
     out = {}
     if not os.path.exists(path):
         return out
@@ -119,7 +119,7 @@ def profile_figures(kernel, workload):
             key, sep, val = line.strip().strip("`").partition(": ")
             if sep and key in PROFILE_KEYS:
                 try:
-                    out[key] = float(val) if "." in val else int(val)
+                    out[key] = float(val) if ("." in val or "e" in val) else int(val)
                 except ValueError:
                     pass
     return out
@@ -155,7 +155,15 @@ def issue_roofline(prof, transitions_per_s, peaks, peaks_kind, sms=152):
     peak = sms * 4 * clock
     out = {"bound": "issue", "unit": "G warp-instructions/s", "peak": peak / 1e9,
            "peak_source": f"{sms} SMs x 4 schedulers x {clock / 1e6:.0f} MHz ({peaks_kind} sm_max_mhz)",
-           "issue_slot_utilisation_ncu": prof.get("issue_slot_utilisation")}
+           "issue_slot_utilisation_ncu": prof.get("issue_slot_utilisation"),
+           "branch_efficiency_ncu": (prof["branch_uniform_pct"] / 100.0) if "branch_uniform_pct" in prof else None}
+    # the secondary bound: the window flushes' L2 reductions against the measured L2 peak
+    l2 = profile_figures("l2_atomics_probe")
+    if prof.get("l2_red_per_transition") and l2.get("l2_red_peak_per_s"):
+        red = prof["l2_red_per_transition"] * transitions_per_s
+        out["l2_atomics"] = {"achieved": red, "peak": l2["l2_red_peak_per_s"], "unit": "u64 reductions/s",
+                             "frac": red / l2["l2_red_peak_per_s"], "per_transition": prof["l2_red_per_transition"],
+                             "peak_source": l2.get("file")}
     wpt = prof.get("warp_instructions_per_transition")
     if wpt:
         achieved = wpt * transitions_per_s

@@ -59,9 +59,12 @@ Batch::~Batch() {
     if (capture_stream) cudaStreamDestroy(capture_stream);
     for (cudaEvent_t e : {ev0, ev1})
         if (e) cudaEventDestroy(e);
-    for (Class& k : classes)
-        for (cudaEvent_t e : {k.e0, k.e1})
+    for (Class& k : classes) {
+        for (cudaEvent_t e : {k.e0, k.e1, k.join})
             if (e) cudaEventDestroy(e);
+        if (k.stream) cudaStreamDestroy(k.stream);
+    }
+    if (fork) cudaEventDestroy(fork);
     if (small_host) cudaFreeHost(small_host);
     for (void* p : owned) cudaFree(p);
 }
@@ -272,9 +275,12 @@ void Batch::create(const std::vector<const CompiledModel*>& models, const std::v
         k.pilot_long.prefix = dq4;
         ck(cudaEventCreate(&k.e0), "cudaEventCreate");
         ck(cudaEventCreate(&k.e1), "cudaEventCreate");
+        ck(cudaEventCreateWithFlags(&k.join, cudaEventDisableTiming), "cudaEventCreate");
+        ck(cudaStreamCreateWithFlags(&k.stream, cudaStreamNonBlocking), "cudaStreamCreate");
     }
 
     ck(cudaStreamCreateWithFlags(&capture_stream, cudaStreamNonBlocking), "cudaStreamCreate");
+    ck(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming), "cudaEventCreate");
     for (cudaEvent_t* e : {&ev0, &ev1}) ck(cudaEventCreate(e), "cudaEventCreate");
     // default shapes (the autotuner replaces them on the first run): the lane layout at 128
     // threads per block where its shared memory fits, else the warp layout
@@ -333,12 +339,19 @@ void Batch::build_graph() {
     ck(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture");
     cudaError_t e = cudaMemsetAsync(result_arena, 0, result_bytes, s);
     if (e == cudaSuccess) e = cudaMemsetAsync(rep_arena, 0xFF, rep_bytes, s);
-    // one launch per size class, bracketed by external event-record nodes so that each class's
-    // kernel time can be read after every replay
-    for (const Class& k : classes) {
-        if (e == cudaSuccess) e = cudaEventRecordWithFlags(k.e0, s, cudaEventRecordExternal);
-        if (e == cudaSuccess) e = launch_class(k, k.desc, s);
-        if (e == cudaSuccess) e = cudaEventRecordWithFlags(k.e1, s, cudaEventRecordExternal);
+    // one launch per size class, each on its own branch of the graph so that a class starts on the
+    // SMs the previous one's last blocks leave instead of waiting for its whole tail; the largest
+    // class first. Each launch is bracketed by external event-record nodes so that its kernel time
+    // can be read after every replay.
+    if (e == cudaSuccess) e = cudaEventRecord(fork, s);
+    for (size_t ci = classes.size(); ci-- > 0;) {
+        const Class& k = classes[ci];
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(k.stream, fork, 0);
+        if (e == cudaSuccess) e = cudaEventRecordWithFlags(k.e0, k.stream, cudaEventRecordExternal);
+        if (e == cudaSuccess) e = launch_class(k, k.desc, k.stream);
+        if (e == cudaSuccess) e = cudaEventRecordWithFlags(k.e1, k.stream, cudaEventRecordExternal);
+        if (e == cudaSuccess) e = cudaEventRecord(k.join, k.stream);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(s, k.join, 0);
     }
     if (e == cudaSuccess) e = launch_fp_aggregate_batch(d_params, d_fps, (int)inst.size(), 8, s);
     if (e == cudaSuccess) e = cudaMemcpyAsync(small_host, small_dev, small_bytes, cudaMemcpyDeviceToHost, s);

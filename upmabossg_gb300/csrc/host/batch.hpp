@@ -46,6 +46,8 @@ public:
         size_t smem = 0;
         int grid = 0;
         cudaEvent_t e0 = nullptr, e1 = nullptr;
+        cudaStream_t stream = nullptr;      // the class's branch of the graph
+        cudaEvent_t join = nullptr;         // end of that branch
         float kernel_ms = 0.f;
         std::vector<mbg_batch_class_timing> timings;  // every shape the autotuner timed
     };
@@ -74,6 +76,7 @@ public:
     size_t small_bytes = 0;
     char* small_host = nullptr;
     cudaStream_t capture_stream = nullptr;
+    cudaEvent_t fork = nullptr;             // start of the class branches
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
