@@ -38,13 +38,6 @@ uint64_t fnv1a(const std::string& s) {
     return h;
 }
 
-std::string cache_dir() {
-    const char* e = std::getenv("MBG_JIT_CACHE");
-    if (e && *e) return e;
-    const char* home = std::getenv("HOME");
-    return std::string(home && *home ? home : "/tmp") + "/.cache/mbg_gb300";
-}
-
 void mkdirs(const std::string& d) {
     std::string cur;
     std::stringstream ss(d);
@@ -90,6 +83,15 @@ std::string compile(const std::string& src) {
 }
 
 }  // namespace
+
+std::string cache_dir() {
+    const char* e = std::getenv("MBG_JIT_CACHE");
+    if (e && *e) return e;
+    const char* home = std::getenv("HOME");
+    return std::string(home && *home ? home : "/tmp") + "/.cache/mbg_gb300";
+}
+
+void cache_mkdirs(const std::string& d) { mkdirs(d); }
 
 double jit_compile_only(const std::string& model_src) {
     std::string src;

@@ -13,6 +13,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <fstream>
 #include <map>
 #include <mutex>
 #include <tuple>
@@ -434,6 +435,43 @@ int ceil_log2(uint64_t x) {
     while ((1ull << c) < x) ++c;
     return c;
 }
+
+// Tuned shapes also persist on disk, one line per (GPU, library build, class), so that a new
+// process (a command-line run, say) finds them without timing the pilots again. A line from
+// another GPU model or another build of the library never matches.
+std::string tune_key(int device, const std::tuple<int, int, int>& cls) {
+    cudaDeviceProp prop{};
+    if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) return std::string();
+    std::string name = prop.name;
+    for (char& c : name)
+        if (c == ' ' || c == '|') c = '_';
+    return name + "|" + std::to_string(prop.multiProcessorCount) + "|" + __DATE__ + "_" + __TIME__ + "|" +
+           std::to_string(std::get<0>(cls)) + "|" + std::to_string(std::get<1>(cls)) + "|" +
+           std::to_string(std::get<2>(cls));
+}
+
+std::string tune_path() { return cache_dir() + "/autotune_v1.txt"; }
+
+bool tune_lookup_disk(const std::string& key, Shape& out) {
+    if (key.empty() || std::getenv("MBG_AUTOTUNE_NOCACHE")) return false;
+    std::ifstream f(tune_path());
+    std::string k;
+    int lay = 0, blk = 0, coop = 0;
+    bool found = false;
+    while (f >> k >> lay >> blk >> coop)  // the last line for a key wins
+        if (k == key) {
+            out = Shape{lay, blk, coop != 0};
+            found = true;
+        }
+    return found;
+}
+
+void tune_store_disk(const std::string& key, const Shape& s) {
+    if (key.empty() || std::getenv("MBG_AUTOTUNE_NOCACHE")) return;
+    cache_mkdirs(cache_dir());
+    std::ofstream f(tune_path(), std::ios::app);
+    f << key << " " << s.layout << " " << s.block << " " << (s.coop ? 1 : 0) << "\n";
+}
 }  // namespace
 
 void Sim::autotune() {
@@ -442,9 +480,12 @@ void Sim::autotune() {
     const uint64_t pilot = std::min<uint64_t>(n_traj, 1u << 17);
     // the lane layout has no redraw_period: such runs are tuned (and cached) apart
     const std::tuple<int, int, int> cls{ceil_log2((uint64_t)cm.n), ceil_log2(pilot), opts.redraw_period ? 1 : 0};
+    const std::string key = tune_key(device, cls);
     {
         std::lock_guard<std::mutex> lock(g_tune_mu);
         auto it = g_tuned.find(cls);
+        Shape disk{};
+        if (it == g_tuned.end() && tune_lookup_disk(key, disk)) it = g_tuned.emplace(cls, disk).first;
         if (it != g_tuned.end()) {
             setup_layout(it->second.layout, opts.block_size > 0 ? opts.block_size : it->second.block,
                          it->second.coop);
@@ -528,6 +569,7 @@ void Sim::autotune() {
     setup_layout(best_shape.layout, best_shape.block, best_shape.coop);
     std::lock_guard<std::mutex> lock(g_tune_mu);
     g_tuned[cls] = best_shape;
+    tune_store_disk(key, best_shape);
 }
 
 void Sim::setup_layout(int lay, int blk, bool coop) {

@@ -62,6 +62,10 @@ std::string generate_thread_model(const CompiledModel& cm, const DeviceLayout& d
 // Compiles (or fetches from the in-process / on-disk cache) the full NVRTC program made of the
 // shared device headers and `model_src`, loads it on the current device and returns the kernel
 // handle usable with cudaLaunchKernel. `compile_ms` is 0 on a cache hit. Throws mbg::Error.
+// Directory of the on-disk caches (compiled kernels, tuned launch shapes): MBG_JIT_CACHE, default
+// ~/.cache/mbg_gb300; cache_mkdirs creates it.
+std::string cache_dir();
+void cache_mkdirs(const std::string& dir);
 // `window_hash`: the variant whose window sums go to the window hash table.
 void* jit_thread_kernel(const std::string& model_src, double& compile_ms, bool window_hash = false);
 // Compiles without loading (no device needed); returns milliseconds. Throws JitError.
