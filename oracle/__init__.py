@@ -1,8 +1,9 @@
 """ctypes binding of the host FP64 oracle: TEST INFRASTRUCTURE ONLY.
 
 Only tests/, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline leg import this module. The
-product (``upmabossg_gb300``) never imports or links it. The oracle library is built by
-``build()`` from oracle.cpp plus the product's parser sources.
+product (``upmabossg_gb300``) never imports or links it, and it shares no code with the product:
+the oracle library is built by ``build()`` from oracle.cpp and its own front end (front.h: parser,
+expression evaluation, Philox streams, fixed-point rules).
 """
 from __future__ import annotations
 
@@ -14,11 +15,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "build", "liboracle.so")
-SOURCES = [
-    os.path.join(HERE, "oracle.cpp"),
-    os.path.join(HERE, "..", "upmabossg_gb300", "csrc", "host", "parser.cpp"),
-    os.path.join(HERE, "..", "upmabossg_gb300", "csrc", "host", "model.cpp"),
-]
+SOURCES = [os.path.join(HERE, "oracle.cpp")]
 
 
 def build(verbose: bool = False) -> str:

@@ -1,6 +1,6 @@
 // Host FP64 Gillespie oracle: TEST INFRASTRUCTURE ONLY (see oracle.h for what it restates).
-// The product never links this file. It shares the product's parser (the grammar is tested on
-// its own) but evaluates rates from the expression trees with its own evaluator.
+// The product never links this file, and this file uses nothing of the product: its parser,
+// expression evaluation, random streams and fixed-point rules are its own (front.h).
 #include "oracle.h"
 
 #include <algorithm>
@@ -14,16 +14,14 @@
 #include <unordered_map>
 #include <vector>
 
-#include "../upmabossg_gb300/csrc/device/philox.h"
-#include "../upmabossg_gb300/csrc/device/sim_types.h"
-#include "../upmabossg_gb300/csrc/host/model.hpp"
+#include "front.h"
 
 namespace {
 
-using mbg::Expr;
-using mbg::Op;
+using orc::Expr;
+using orc::Op;
 
-// Expression with node names and @aliases resolved for one node.
+// Expression with node names and @aliases resolved for one node, as postfix instructions.
 struct Prog {
     struct Ins {
         int code;  // 0 const, 1 node bit, 2 unary, 3 binary, 4 ternary
@@ -34,43 +32,42 @@ struct Prog {
     std::vector<Ins> ins;
 };
 
-void build(const Expr& e, const mbg::Model& m, int cur, Prog& p, int depth) {
-    if (depth > 64) throw mbg::Error("alias recursion too deep");
+void build(const Expr& e, const orc::ModelDef& m, int cur, Prog& p, int depth) {
+    if (depth > 64) throw orc::Error("alias recursion too deep");
     switch (e.kind) {
-        case Expr::Kind::Literal: p.ins.push_back({0, e.value, 0, Op::Plus}); break;
-        case Expr::Kind::Var: {
-            auto it = m.variables.find(e.name);
-            if (it == m.variables.end()) throw mbg::Error("unknown variable " + e.name);
-            p.ins.push_back({0, it->second, 0, Op::Plus});
+        case Expr::Num: p.ins.push_back({0, e.value, 0, Op::Add}); break;
+        case Expr::Var: {
+            auto it = m.vars.find(e.name);
+            if (it == m.vars.end()) throw orc::Error("unknown variable " + e.name);
+            p.ins.push_back({0, it->second, 0, Op::Add});
             break;
         }
-        case Expr::Kind::Ident: {
-            int i = m.node_index(e.name);
-            if (i < 0) throw mbg::Error("unknown node name: " + e.name);
-            p.ins.push_back({1, 0, i, Op::Plus});
+        case Expr::Node: {
+            auto it = m.index.find(e.name);
+            if (it == m.index.end()) throw orc::Error("unknown node name: " + e.name);
+            p.ins.push_back({1, 0, it->second, Op::Add});
             break;
         }
-        case Expr::Kind::Alias: {
+        case Expr::Alias: {  // src/parser/expressions.cpp:223-231: the current node's attribute
             const Expr* a = m.nodes[cur].attr(e.name.substr(1));
-            if (!a) throw mbg::Error("missing attribute " + e.name);
+            if (!a) throw orc::Error("missing attribute " + e.name);
             build(*a, m, cur, p, depth + 1);
             break;
         }
-        case Expr::Kind::Paren: build(*e.a, m, cur, p, depth); break;
-        case Expr::Kind::Unary:
+        case Expr::Unary:
             build(*e.a, m, cur, p, depth);
             p.ins.push_back({2, 0, 0, e.op});
             break;
-        case Expr::Kind::Binary:
+        case Expr::Binary:
             build(*e.a, m, cur, p, depth);
             build(*e.b, m, cur, p, depth);
             p.ins.push_back({3, 0, 0, e.op});
             break;
-        case Expr::Kind::Ternary:
+        case Expr::Ternary:
             build(*e.a, m, cur, p, depth);
             build(*e.b, m, cur, p, depth);
             build(*e.c, m, cur, p, depth);
-            p.ins.push_back({4, 0, 0, Op::Plus});
+            p.ins.push_back({4, 0, 0, Op::Add});
             break;
     }
 }
@@ -81,33 +78,11 @@ double run(const Prog& p, const uint8_t* s, double* st) {
         switch (in.code) {
             case 0: st[sp++] = in.c; break;
             case 1: st[sp++] = s[in.node] ? 1.0 : 0.0; break;
-            case 2: {
-                double x = st[sp - 1];
-                st[sp - 1] = in.op == Op::Minus ? -x : in.op == Op::Not ? (x == 0 ? 1.0 : 0.0) : x;
-                break;
-            }
-            case 3: {
-                double l = st[sp - 2], r = st[sp - 1], v = 0;
-                switch (in.op) {
-                    case Op::Plus: v = l + r; break;
-                    case Op::Minus: v = l - r; break;
-                    case Op::Star: v = l * r; break;
-                    case Op::Slash: v = l / r; break;
-                    case Op::And: v = (l != 0 && r != 0); break;
-                    case Op::Or: v = (l != 0 || r != 0); break;
-                    case Op::Xor: v = ((l != 0) != (r != 0)); break;
-                    case Op::Eq: v = l == r; break;
-                    case Op::Ne: v = l != r; break;
-                    case Op::Le: v = l <= r; break;
-                    case Op::Lt: v = l < r; break;
-                    case Op::Ge: v = l >= r; break;
-                    case Op::Gt: v = l > r; break;
-                    default: break;
-                }
-                st[sp - 2] = v;
+            case 2: st[sp - 1] = orc::apply(in.op, 0, st[sp - 1]); break;
+            case 3:
+                st[sp - 2] = orc::apply(in.op, st[sp - 2], st[sp - 1]);
                 --sp;
                 break;
-            }
             case 4: {
                 double c = st[sp - 3];
                 st[sp - 3] = c != 0 ? st[sp - 2] : st[sp - 1];
@@ -144,19 +119,18 @@ struct orc_result {
 extern "C" orc_result* orc_run(const char* bnd_text, const char* cfg_text, const orc_opts* o, char* err,
                                size_t errlen) {
     try {
-        mbg::Model m;
-        mbg::parse_bnd(m, bnd_text, "model.bnd");
-        mbg::parse_cfg(m, cfg_text, "model.cfg");
+        orc::ModelDef m;
+        orc::parse_model(m, bnd_text, cfg_text);
         const int n = (int)m.nodes.size();
-        if (n == 0) throw mbg::Error("model has no nodes");
+        if (n == 0) throw orc::Error("model has no nodes");
         auto* res = new orc_result();
         res->n = n;
         res->words = (n + 31) / 32;
         std::vector<int> out_nodes;
         for (int i = 0; i < n; ++i)
-            if (!m.is_internal(i)) out_nodes.push_back(i);
+            if (!orc::is_internal(m, i)) out_nodes.push_back(i);
         res->n_out = (int)out_nodes.size();
-        if (res->n_out > 24) throw mbg::Error("too many output nodes for the oracle");
+        if (res->n_out > 24) throw orc::Error("too many output nodes for the oracle");
         const bool discrete = m.constant("discrete_time") != 0;
         const double max_time = m.constant("max_time"), tick = m.constant("time_tick");
         res->discrete = discrete;
@@ -167,8 +141,6 @@ extern "C" orc_result* orc_run(const char* bnd_text, const char* cfg_text, const
         res->n_traj = o->n_traj ? o->n_traj : (uint64_t)(sc > 0 ? sc : 0);
         double cs = m.constant("seed_pseudorandom");
         const uint64_t seed = o->use_cfg_seed ? (uint64_t)(cs > 0 ? cs : 0) : o->seed;
-        // the pick's fixed-point scale: the caller's, or the compiled model's rule (0)
-        const int F = o->frac_bits > 0 ? o->frac_bits : mbg::compile_model(m).frac_bits;
         const uint32_t max_steps = o->max_steps;
 
         std::vector<Prog> up(n), down(n);
@@ -180,6 +152,29 @@ extern "C" orc_result* orc_run(const char* bnd_text, const char* cfg_text, const
         }
         size_t depth = 0;
         for (int i = 0; i < n; ++i) depth = std::max({depth, up[i].ins.size(), down[i].ins.size()});
+        // the pick's fixed-point scale: the caller's, or the rule of the simulator (every node's
+        // largest rate over all states of the nodes its rates read, summed)
+        int F = o->frac_bits;
+        if (F <= 0) {
+            std::vector<uint8_t> st(n, 0);
+            std::vector<double> stack(depth + 2);
+            double sum_max = 0;
+            for (int i = 0; i < n; ++i) {
+                std::vector<int> sup{i};
+                for (const Prog* pg : {&up[i], &down[i]})
+                    for (const auto& in : pg->ins)
+                        if (in.code == 1 && std::find(sup.begin(), sup.end(), in.node) == sup.end()) sup.push_back(in.node);
+                if (sup.size() > 26) throw orc::Error("a rate reads more than 25 other nodes");
+                double mx = 0;
+                for (uint64_t a = 0; a < (1ull << sup.size()); ++a) {
+                    for (size_t q = 0; q < sup.size(); ++q) st[sup[q]] = (uint8_t)((a >> q) & 1u);
+                    mx = std::max(mx, run(st[i] ? down[i] : up[i], st.data(), stack.data()));
+                }
+                for (int x : sup) st[x] = 0;
+                sum_max += mx;
+            }
+            F = orc::frac_bits_for(sum_max);
+        }
 
         int T = o->threads > 0 ? o->threads : (int)std::thread::hardware_concurrency();
         if (T < 1) T = 1;
@@ -223,7 +218,7 @@ extern "C" orc_result* orc_run(const char* bnd_text, const char* cfg_text, const
                 if (j >= res->n_traj) break;
                 const uint64_t traj = o->traj_base + j;
                 for (int b = 0; 4 * b < n; ++b) {
-                    mbg::u32x4 d = mbg::philox_init(seed, traj, (unsigned)b);
+                    orc::W4 d = orc::init_draws(seed, traj, (uint32_t)b);
                     unsigned w4[4] = {d.x, d.y, d.z, d.w};
                     for (int c = 0; c < 4 && 4 * b + c < n; ++c) s[4 * b + c] = (w4[c] >> 8) < thr[4 * b + c];
                 }
@@ -237,7 +232,7 @@ extern "C" orc_result* orc_run(const char* bnd_text, const char* cfg_text, const
                     double R = 0, Rout = 0;
                     for (int i = 0; i < n; ++i) {
                         r[i] = run(s[i] ? down[i] : up[i], s.data(), stack.data());
-                        q[i] = mbg::quantize_rate(r[i], F);
+                        q[i] = orc::quantize(r[i], F);
                         Q += q[i];
                         R += r[i];
                     }
@@ -254,11 +249,11 @@ extern "C" orc_result* orc_run(const char* bnd_text, const char* cfg_text, const
                             add_slice(t, max_time, so, 0.0);
                         }
                         t = max_time;
-                        status = mbg::TRAJ_FIXED_POINT;
+                        status = orc::FIXED_POINT;
                         break;
                     }
                     if (max_steps && step >= max_steps) {
-                        status = mbg::TRAJ_STEP_LIMIT;
+                        status = orc::STEP_LIMIT;
                         break;
                     }
                     double h = 0;
@@ -267,7 +262,7 @@ extern "C" orc_result* orc_run(const char* bnd_text, const char* cfg_text, const
                             double pr = r[p] / Rout;
                             if (pr != 0) h -= std::log2(pr) * pr;
                         }
-                    mbg::u32x4 d = mbg::philox_step(seed, traj, step);
+                    orc::W4 d = orc::step_draws(seed, traj, step);
                     double t1;
                     if (discrete) {
                         t1 = (double)(step + 1) * tick;
@@ -276,7 +271,7 @@ extern "C" orc_result* orc_run(const char* bnd_text, const char* cfg_text, const
                         L.hist[((uint64_t)w << 32) | so] += 1.0;
                         L.th[w] += h;
                     } else {
-                        double dt = -std::log(mbg::u01_open0_d(d.x)) / R;
+                        double dt = -std::log(orc::unit_open0(d.x)) / R;
                         t1 = t + dt;
                         if (std::fabs(t1 - max_time) <= 1e-6 * max_time) tie |= 2;
                         t1 = std::min(t1, max_time);
@@ -284,9 +279,9 @@ extern "C" orc_result* orc_run(const char* bnd_text, const char* cfg_text, const
                     }
                     if (t1 >= max_time) {
                         t = max_time;
-                        status = mbg::TRAJ_FINISHED;
+                        status = orc::FINISHED;
                         if (o->legacy_final) {
-                            uint64_t rt = mbg::pick_target(d.y, d.z, Q), acc = 0;
+                            uint64_t rt = orc::pick_target(d.y, d.z, Q), acc = 0;
                             for (int i = 0; i < n; ++i) {
                                 acc += q[i];
                                 if (acc > rt) {
@@ -305,7 +300,7 @@ extern "C" orc_result* orc_run(const char* bnd_text, const char* cfg_text, const
                         ++step;
                         continue;
                     }
-                    uint64_t rt = mbg::pick_target(d.y, d.z, Q);
+                    uint64_t rt = orc::pick_target(d.y, d.z, Q);
                     uint64_t acc = 0;
                     int k = -1;
                     for (int i = 0; i < n; ++i) {
@@ -327,7 +322,7 @@ extern "C" orc_result* orc_run(const char* bnd_text, const char* cfg_text, const
                     }
                     if (kk != k) tie |= 1;
                     if (k < 0) {
-                        status = mbg::TRAJ_ERROR;
+                        status = orc::FAILED;
                         break;
                     }
                     s[k] ^= 1;
@@ -340,13 +335,13 @@ extern "C" orc_result* orc_run(const char* bnd_text, const char* cfg_text, const
                 for (size_t p = 0; p < out_nodes.size(); ++p) so |= (uint32_t)s[out_nodes[p]] << p;
                 if (legacy_flip >= 0) s[legacy_flip] ^= 1;
                 L.cnt[0] += trans;
-                L.cnt[6] += step + (status == mbg::TRAJ_STEP_LIMIT ? 0 : 1);
-                if (status == mbg::TRAJ_FINISHED) ++L.cnt[1];
-                if (status == mbg::TRAJ_FIXED_POINT) ++L.cnt[2];
-                if (status == mbg::TRAJ_STEP_LIMIT) ++L.cnt[3];
+                L.cnt[6] += step + (status == orc::STEP_LIMIT ? 0 : 1);
+                if (status == orc::FINISHED) ++L.cnt[1];
+                if (status == orc::FIXED_POINT) ++L.cnt[2];
+                if (status == orc::STEP_LIMIT) ++L.cnt[3];
                 if (tie & 1) ++L.cnt[4];
                 if (tie & 2) ++L.cnt[5];
-                if (status == mbg::TRAJ_FINISHED || status == mbg::TRAJ_FIXED_POINT) L.fin[so] += 1.0;
+                if (status == orc::FINISHED || status == orc::FIXED_POINT) L.fin[so] += 1.0;
                 if (keep) {
                     for (int w = 0; w < W; ++w) {
                         uint32_t word = 0;
@@ -427,8 +422,7 @@ extern "C" double orc_seconds(const orc_result* r) { return r->seconds; }
 extern "C" int orc_threads(const orc_result* r) { return r->threads; }
 
 extern "C" void orc_philox(const uint32_t* ctr, const uint32_t* key, uint32_t* out) {
-    mbg::u32x4 c = {ctr[0], ctr[1], ctr[2], ctr[3]};
-    mbg::u32x4 d = mbg::philox4x32_10(c, key[0], key[1]);
+    const orc::W4 d = orc::philox10({ctr[0], ctr[1], ctr[2], ctr[3]}, key[0], key[1]);
     out[0] = d.x;
     out[1] = d.y;
     out[2] = d.z;

@@ -13,9 +13,10 @@
  *   discrete-time windows                               src/jit_kernels/window_average_small.cu:101-136
  *   final states / fixed points                         src/jit_kernels/final_states.cu:17-20,
  *                                                       src/statistics/fixed_states.cu:26-33,118-124
- * with the project's Philox4x32-10 streams in place of curand XORWOW, so the GPU path can be
- * compared trajectory by trajectory. Rates are evaluated from the expression trees directly (not
- * from the GPU path's truth tables). The node pick uses the same exact fixed-point prefix rule as
+ * with the simulator's Philox4x32-10 streams in place of curand XORWOW, so the GPU path can be
+ * compared trajectory by trajectory. It shares no code with the product: its parser, expression
+ * evaluation, Philox and fixed-point rules are its own (front.h), and rates are evaluated from
+ * its own expression trees, not from the GPU path's truth tables. The node pick uses the same exact fixed-point prefix rule as
  * the GPU path and, beside it, the FP64 prefix rule; steps where the two disagree are counted as
  * pick ties. Final steps whose FP64 time lands within 1e-6 relative of max_time are counted as
  * time ties (an FP32 dt may land on the other side).

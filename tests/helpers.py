@@ -34,7 +34,10 @@ def run_device(bnd, cfg, n_traj, layout=mbg.LAYOUT_AUTO, seed=None, record=True,
 
 
 def run_oracle(bnd, cfg, model, n_traj, seed=None, **kw):
-    return oracle.run(bnd, cfg, frac_bits=model.info.frac_bits, n_traj=n_traj, seed=seed,
+    """The oracle on the same texts. It derives its fixed-point scale on its own (frac_bits 0), so a
+    scale the product got wrong shows as differing trajectories; `model` (the product's parse) is
+    not passed to it."""
+    return oracle.run(bnd, cfg, frac_bits=0, n_traj=n_traj, seed=seed,
                       keep_trajectories=True, **kw)
 
 

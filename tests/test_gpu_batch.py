@@ -139,7 +139,7 @@ def test_sweep_shaped_batch_against_oracle():
     seeds = [101 + i for i in range(len(models))]
     batch = mbg.Batch(models, n_traj=[300] * len(models), seeds=seeds).run()
     for i, ((b, c), m) in enumerate(zip(texts, models)):
-        orc = oracle.run(b, c, frac_bits=m.info.frac_bits, n_traj=300, seed=seeds[i], keep_trajectories=True)
+        orc = oracle.run(b, c, n_traj=300, seed=seeds[i], keep_trajectories=True)
         n_ties = int((orc.ties != 0).sum())
         raw, th = batch.probtraj_raw(i)
         dev = raw.astype(np.float64) / TWO32

@@ -142,3 +142,22 @@ def test_bf16_rounding_is_nearest_even():
     assert mlp.bf16_round(np.float32(1.0 + 2 ** -8)) == 1.0          # tie -> even
     assert mlp.bf16_round(np.float32(1.0 + 3 * 2 ** -8)) == 1.0 + 2 ** -6
     assert mlp.bf16_round(np.float32(-2.5)) == -2.5
+
+
+@pytest.mark.parametrize("which", ["small", "medium", "mixed", "cellcycle", "montagud"])
+def test_oracle_front_end_agrees_with_the_product_tables(which):
+    """The oracle parses, evaluates and scales on its own (it shares no code with the product): the
+    fixed-point scale it derives (frac_bits 0) gives the same trajectories as the product's."""
+    from helpers import golden_model, mixed_network
+    if which in ("small", "medium"):
+        net = getattr(synth, which)()
+        bnd, cfg = net.bnd(), net.cfg(sample_count=64)
+    elif which == "mixed":
+        bnd, cfg = mixed_network(seed=3)
+    else:
+        bnd, cfg = golden_model(which)
+    m = mbg.Model.from_strings(bnd, cfg)
+    a = oracle.run(bnd, cfg, n_traj=48, keep_trajectories=True)
+    b = oracle.run(bnd, cfg, frac_bits=m.info.frac_bits, n_traj=48, keep_trajectories=True)
+    assert np.array_equal(a.states, b.states) and np.array_equal(a.transitions, b.transitions)
+    assert np.array_equal(a.times, b.times)
