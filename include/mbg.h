@@ -215,7 +215,8 @@ mbg_status mbg_device_l2_atomic_rate(int32_t device, uint32_t distinct, double* 
 
 /* ---- Batched parameter sweeps --------------------------------------------------------------
  * Many independent simulations ("instances": any models, trajectory counts and seeds) grouped by
- * model size into classes (<= 32, 64, 128, ..., 4096 nodes, larger); each class is one persistent
+ * model size into classes (<= 32, 64, 96, 128, 192, 256, 384, ..., 4096 nodes, larger: about 1.4x
+ * apart); each class is one persistent
  * launch in the lane or the warp layout with its own block size, and all classes, the fixed-point
  * aggregation and the counter read-back are captured once into a CUDA graph replayed by every
  * mbg_batch_run. Replaces one reference CLI run per instance (src/main.cpp:101-169), each of which
