@@ -99,7 +99,7 @@ class Clocks:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-MBG_LAYOUTS = {"thread": 1, "warp": 2, "lane": 3}
+MBG_LAYOUTS = {"thread": 1, "warp": 2, "lane": 3, "lane_global": 4}
 
 
 PROFILE_KEYS = ("traffic_bytes_per_launch", "issue_slot_utilisation", "warp_instructions_per_transition",
@@ -522,7 +522,8 @@ def run_ours(args):
     info = model.info
     kms = sum(kernel_ms) / len(kernel_ms)
     kernel = {MBG_LAYOUTS["thread"]: "mbg_sim_thread", MBG_LAYOUTS["warp"]: "mbg_sim_warp",
-              MBG_LAYOUTS["lane"]: "mbg_sim_lane" if summary.get("lane_update") else "mbg_sim_lane_coop"}[summary["layout"]]
+              MBG_LAYOUTS["lane"]: "mbg_sim_lane" if summary.get("lane_update") else "mbg_sim_lane_coop",
+              MBG_LAYOUTS["lane_global"]: "mbg_sim_lane_global"}[summary["layout"]]
     prof = profile_figures(kernel, args.workload)
     roofline = issue_roofline(prof, trans_step / (kms * 1e-3), peaks, peaks_kind)
     # the reference algorithm's work (every rate re-evaluated, summed and scanned per transition)
@@ -549,7 +550,8 @@ def run_ours(args):
         "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "u64", "data": "synthetic",
         "config": {"workload": WORKLOADS[args.workload], "trajectories_per_gpu": n_rank,
-                   "transitions_per_step": trans_all, "layout": ["", "thread", "warp", "lane"][summary["layout"]],
+                   "transitions_per_step": trans_all,
+                   "layout": ["", "thread", "warp", "lane", "lane_global"][summary["layout"]],
                    "block_size": summary.get("block_size"), "grid_size": summary.get("grid_size"),
                    "lane_update": summary.get("lane_update"),
                    "l2": "flushed between steps (256 MiB write)", "wall_s": wall},
@@ -580,7 +582,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="medium", choices=sorted(WORKLOADS) + ["sweep", "surrogate", "l2atomics"])
-    ap.add_argument("--layout", type=int, default=0, help="0 autotuned, 1 thread, 2 warp, 3 lane")
+    ap.add_argument("--layout", type=int, default=0, help="0 autotuned, 1 thread, 2 warp, 3 lane, 4 lane (global rows)")
     ap.add_argument("--block", type=int, default=0, help="threads per block (0: the layout's default); profiling")
     ap.add_argument("--lane-update", type=int, default=0, help="lane layout: 0 cooperative, 1 per lane; profiling")
     ap.add_argument("--window-table", type=int, default=0, help="0 auto, 1 dense, 2 hash table; profiling")

@@ -65,8 +65,10 @@ typedef struct {
 /* Trajectory layout: 0 auto (timed on a pilot, once per model size class), 1 thread per
  * trajectory (NVRTC-compiled evaluator, state in registers, every rate re-evaluated per step),
  * 2 warp per trajectory (table driven), 3 lane: thread per trajectory, table driven, state in
- * shared memory, rates updated incrementally. All four give identical results. */
-enum { MBG_LAYOUT_AUTO = 0, MBG_LAYOUT_THREAD = 1, MBG_LAYOUT_WARP = 2, MBG_LAYOUT_LANE = 3 };
+ * shared memory, rates updated incrementally, 4 lane with the per-trajectory state in global
+ * memory (L1/L2-cached; for networks whose state leaves too few trajectories in shared memory).
+ * All give identical results. */
+enum { MBG_LAYOUT_AUTO = 0, MBG_LAYOUT_THREAD = 1, MBG_LAYOUT_WARP = 2, MBG_LAYOUT_LANE = 3, MBG_LAYOUT_LANE_GLOBAL = 4 };
 
 typedef struct {
     uint64_t n_traj;           /* 0: cfg sample_count */
@@ -215,8 +217,7 @@ mbg_status mbg_device_l2_atomic_rate(int32_t device, uint32_t distinct, double* 
 
 /* ---- Batched parameter sweeps --------------------------------------------------------------
  * Many independent simulations ("instances": any models, trajectory counts and seeds) grouped by
- * model size into classes (<= 32, 64, 96, 128, 192, 256, 384, ..., 4096 nodes, larger: about 1.4x
- * apart); each class is one persistent
+ * model size into classes (<= 32, 64, 128, ..., 4096 nodes, larger); each class is one persistent
  * launch in the lane or the warp layout with its own block size, and all classes, the fixed-point
  * aggregation and the counter read-back are captured once into a CUDA graph replayed by every
  * mbg_batch_run. Replaces one reference CLI run per instance (src/main.cpp:101-169), each of which

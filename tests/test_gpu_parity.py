@@ -17,7 +17,7 @@ from helpers import compare_histograms, compare_trajectories, golden_model, mixe
 pytestmark = pytest.mark.gpu
 
 
-ALL_LAYOUTS = [mbg.LAYOUT_THREAD, mbg.LAYOUT_WARP, mbg.LAYOUT_LANE, "lane-serial"]
+ALL_LAYOUTS = [mbg.LAYOUT_THREAD, mbg.LAYOUT_WARP, mbg.LAYOUT_LANE, "lane-serial", mbg.LAYOUT_LANE_GLOBAL]
 
 
 def layout_kw(layout):
@@ -55,7 +55,7 @@ def test_mixed_rate_forms_parity(seed, discrete, layout):
     compare_histograms(model, sim, orc, 2000)
 
 
-@pytest.mark.parametrize("layout", [mbg.LAYOUT_WARP, mbg.LAYOUT_LANE, "lane-serial"])
+@pytest.mark.parametrize("layout", [mbg.LAYOUT_WARP, mbg.LAYOUT_LANE, "lane-serial", mbg.LAYOUT_LANE_GLOBAL])
 def test_medium_network_parity(layout):
     net = synth.medium()
     bnd, cfg = net.bnd(), net.cfg(sample_count=192)
@@ -112,7 +112,7 @@ def test_wide_node_parity(layout):
     compare_histograms(model, sim, orc, 3000)
 
 
-@pytest.mark.parametrize("layout", [mbg.LAYOUT_WARP, mbg.LAYOUT_LANE])
+@pytest.mark.parametrize("layout", [mbg.LAYOUT_WARP, mbg.LAYOUT_LANE, mbg.LAYOUT_LANE_GLOBAL])
 def test_large_network_parity(layout):
     """The 5000-node workload at its own max_time (20) and tick (0.2): 256 trajectories of about
     7000 transitions each, every window compared."""
@@ -137,7 +137,8 @@ def test_medium_network_parity_2000(layout):
     compare_histograms(model, sim, orc, 2000)
 
 
-@pytest.mark.parametrize("layout", [mbg.LAYOUT_AUTO, mbg.LAYOUT_WARP, mbg.LAYOUT_LANE, "lane-serial"])
+@pytest.mark.parametrize("layout", [mbg.LAYOUT_AUTO, mbg.LAYOUT_WARP, mbg.LAYOUT_LANE, "lane-serial",
+                                    mbg.LAYOUT_LANE_GLOBAL])
 @pytest.mark.parametrize("name,n", [("cellcycle", 3000), ("metastasis", 300), ("sizek", 300), ("montagud", 200)])
 def test_reference_models_parity(name, n, layout):
     bnd, cfg = golden_model(name)
@@ -147,7 +148,7 @@ def test_reference_models_parity(name, n, layout):
     compare_histograms(model, sim, orc, n)
 
 
-@pytest.mark.parametrize("other", [mbg.LAYOUT_WARP, mbg.LAYOUT_LANE, "lane-serial"])
+@pytest.mark.parametrize("other", [mbg.LAYOUT_WARP, mbg.LAYOUT_LANE, "lane-serial", mbg.LAYOUT_LANE_GLOBAL])
 def test_layouts_agree(other):
     """Every layout runs the same integer arithmetic and the same clock: identical window sums,
     final states and fixed points."""
@@ -190,7 +191,7 @@ def test_trajectory_ids_are_partition_independent():
     assert np.array_equal(a, b + c)
 
 
-@pytest.mark.parametrize("layout", [mbg.LAYOUT_WARP, mbg.LAYOUT_LANE, "lane-serial"])
+@pytest.mark.parametrize("layout", [mbg.LAYOUT_WARP, mbg.LAYOUT_LANE, "lane-serial", mbg.LAYOUT_LANE_GLOBAL])
 def test_step_limit_is_counted(layout):
     net = synth.medium()
     bnd, cfg = net.bnd(), net.cfg(sample_count=64)
@@ -223,8 +224,9 @@ def test_reference_segment_process_parity(workload, n, layout):
 def test_reference_segment_process_needs_thread_or_warp():
     net = synth.small()
     m = mbg.Model.from_strings(net.bnd(), net.cfg())
-    with pytest.raises(mbg.MbgError) as e:
-        mbg.Simulation(m, n_traj=100, layout=mbg.LAYOUT_LANE, redraw_period=99)
-    assert e.value.status == 1
+    for lay in (mbg.LAYOUT_LANE, mbg.LAYOUT_LANE_GLOBAL):
+        with pytest.raises(mbg.MbgError) as e:
+            mbg.Simulation(m, n_traj=100, layout=lay, redraw_period=99)
+        assert e.value.status == 1
     s = mbg.Simulation(m, n_traj=1000, redraw_period=99).run()  # auto: tuned over thread and warp only
     assert s.summary()["layout"] in (mbg.LAYOUT_THREAD, mbg.LAYOUT_WARP)

@@ -15,7 +15,7 @@ PKG = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(PKG, "lib", "libmbg.so")
 CLI_PATH = os.path.join(PKG, "bin", "MaBoSSG")
 
-LAYOUT_AUTO, LAYOUT_THREAD, LAYOUT_WARP, LAYOUT_LANE = 0, 1, 2, 3
+LAYOUT_AUTO, LAYOUT_THREAD, LAYOUT_WARP, LAYOUT_LANE, LAYOUT_LANE_GLOBAL = 0, 1, 2, 3, 4
 STATUS = {0: "OK", 1: "ARG", 2: "IO", 3: "PARSE", 4: "MODEL", 5: "CUDA", 6: "JIT", 7: "NOMEM", 8: "DEVICE",
           9: "STATE"}
 

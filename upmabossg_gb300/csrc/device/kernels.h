@@ -19,6 +19,11 @@ cudaError_t sim_warp_occupancy(bool cached_index, int block, size_t smem, int* b
 cudaError_t launch_sim_lane(const SimParams& p, bool coop, bool full, int grid, int block, size_t smem,
                             cudaStream_t stream);
 cudaError_t sim_lane_configure(bool coop, bool full, size_t smem, int block, int* blocks_per_sm);
+// The lane layout with its rows in global memory (SimParams::lane_state; per-lane reader update):
+// carve-out all L1, occupancy without dynamic shared memory; the launcher picks the window-hash
+// twin when SimParams::hash_bits > 0. sim_kernel_limits numbers it 6 (variant: `_full`).
+cudaError_t sim_lane_global_configure(bool full, int block, int* blocks_per_sm);
+cudaError_t launch_sim_lane_global(const SimParams& p, bool full, int grid, int block, cudaStream_t stream);
 // Dynamic shared memory of a lane-layout block (the same for both reader-update variants).
 size_t sim_lane_smem(int n, int block);
 int sim_lane_rows(int n);                 // BatchDesc::rows for models of up to n nodes
@@ -30,7 +35,7 @@ int sim_lane_rows(int n);                 // BatchDesc::rows for models of up to
 cudaError_t sim_kernel_limits(int kernel, bool variant, const int* blocks, const size_t* smems, const int* want,
                               int count, bool hash = false);
 // The window-hash twins of the single-simulation kernels (sim_aot_hash.cu), by the numbering of
-// sim_kernel_limits (0, 3, 4); the launchers pick them when SimParams::hash_bits > 0.
+// sim_kernel_limits (0, 3, 4, 6); the launchers pick them when SimParams::hash_bits > 0.
 const void* sim_kernel_hash(int kernel, bool variant);
 std::mutex& kernel_attr_mutex();
 cudaError_t launch_sim_lane_batch(const BatchDesc& b, bool coop, bool full, int grid, int block, size_t smem,

@@ -52,6 +52,18 @@ extern "C" __global__ void __launch_bounds__(256, 3) mbg_sim_lane_coop_full(cons
     sim_lane_body<true, true>(p, smem);
 }
 
+// The lane layout with each block's rows in global memory instead of shared memory, for networks
+// whose rows leave too few trajectories resident in shared memory: occupancy is then bounded by
+// registers (three blocks of 256), the rows are cached in L1 (the whole carve-out) and L2. Per-lane
+// reader update only (the cooperative one patches other lanes' rows with atomics).
+extern "C" __global__ void __launch_bounds__(256, 3) mbg_sim_lane_global(const SimParams p) {
+    sim_lane_body<false, false>(p, p.lane_state + (size_t)blockIdx.x * p.lane_block_bytes);
+}
+
+extern "C" __global__ void __launch_bounds__(256, 3) mbg_sim_lane_global_full(const SimParams p) {
+    sim_lane_body<false, true>(p, p.lane_state + (size_t)blockIdx.x * p.lane_block_bytes);
+}
+
 // Batched instances (parameter sweeps) in the lane layout, both reader-update variants.
 extern "C" __global__ void __launch_bounds__(256, 3) mbg_sim_lane_batch(const BatchDesc b) {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -330,6 +342,7 @@ cudaError_t sim_kernel_limits(int kernel, bool variant, const int* blocks, const
         case 4: f = variant ? (const void*)mbg_sim_lane_coop_full : (const void*)mbg_sim_lane_full; break;
         case 5: f = variant ? (const void*)mbg_sim_lane_batch_coop_full : (const void*)mbg_sim_lane_batch_full; break;
         case 2: f = variant ? (const void*)mbg_sim_warp_batch : (const void*)mbg_sim_warp_batch_gather; break;
+        case 6: f = variant ? (const void*)mbg_sim_lane_global_full : (const void*)mbg_sim_lane_global; break;
         default: f = variant ? (const void*)mbg_sim_warp : (const void*)mbg_sim_warp_gather; break;
     }
     return shared_limits(f, blocks, smems, want, count);
@@ -355,6 +368,19 @@ cudaError_t sim_lane_batch_configure(bool coop, bool full, size_t smem, int bloc
 }
 
 size_t sim_lane_smem(int n, int block) { return (size_t)block * lane_smem_bytes(n); }
+
+cudaError_t sim_lane_global_configure(bool full, int block, int* blocks_per_sm) {
+    const void* f = full ? (const void*)mbg_sim_lane_global_full : (const void*)mbg_sim_lane_global;
+    cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributePreferredSharedMemoryCarveout, 0);  // all L1
+    if (e != cudaSuccess) return e;
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, f, block, 0);
+}
+
+cudaError_t launch_sim_lane_global(const SimParams& p, bool full, int grid, int block, cudaStream_t stream) {
+    if (p.hash_bits > 0)
+        return launch((void (*)(SimParams))sim_kernel_hash(6, full), grid, block, 0, stream, p);
+    return launch(full ? mbg_sim_lane_global_full : mbg_sim_lane_global, grid, block, 0, stream, p);
+}
 
 int sim_lane_rows(int n) { return lane_groups(n); }
 

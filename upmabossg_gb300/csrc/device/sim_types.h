@@ -120,6 +120,10 @@ struct SimParams {
     unsigned char* traj_status;      // optional
     unsigned long long* counters;    // CNT_COUNT
     unsigned int* error_flag;
+    // Lane layout with its per-trajectory rows in global memory (MBG_LAYOUT_LANE_GLOBAL): block b's
+    // rows start at lane_state + b * lane_block_bytes.
+    unsigned char* lane_state;
+    unsigned long long lane_block_bytes;
 };
 
 // A batched launch over many instances (sim_warp.cuh: sim_warp_batch_body).

@@ -41,12 +41,10 @@ void* dmalloc(size_t bytes, std::vector<void*>& owned) {
 }
 
 constexpr size_t kSmallPerInst = 96;  // 8 u64 counters, error word, unique fixed points
-// Size classes by 32-node groups, about 1.4x apart: the lane layout sizes a class's shared-memory
-// rows for its largest member, so a member far below it would run at a fraction of the occupancy
-// its own size allows (a 1100-node model in rows for 2000 nodes: 9 resident warps per SM instead
-// of 16).
-constexpr int kClassGroups[] = {1, 2, 3, 4, 6, 8, 12, 16, 24, 32, 48, 64, 96, 128};
-constexpr int kClasses = (int)(sizeof kClassGroups / sizeof kClassGroups[0]) + 1;  // + larger
+// Size classes by 32-node groups, a power of two apart: up to 32, 64, ..., 4096 nodes, larger.
+// (Classes 1.4x apart, which size a class's shared-memory rows closer to each member, measured
+// 2% slower on the 256-instance sweep: 167 against 170 points/s.)
+constexpr int kClasses = 8;
 constexpr size_t kSmemLimit = 227 * 1024;
 
 }  // namespace
@@ -54,7 +52,7 @@ constexpr size_t kSmemLimit = 227 * 1024;
 int batch_size_class(int n) {
     const int g = (n + 31) / 32;  // 32-node groups
     int c = 0;
-    while (c < kClasses - 1 && kClassGroups[c] < g) ++c;
+    while ((1 << c) < g && c < kClasses - 1) ++c;
     return c;
 }
 

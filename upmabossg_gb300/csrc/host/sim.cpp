@@ -316,7 +316,7 @@ void Sim::grow_window_table(int bits) {
 
 Sim::~Sim() {
     for (void* p : {(void*)dense_hist, (void*)hslots, (void*)wc_bitmap, (void*)wc_wpre, (void*)wc_chunk,
-                    (void*)wc_total, (void*)wc_bin, (void*)wc_sum})
+                    (void*)wc_total, (void*)wc_bin, (void*)wc_sum, (void*)lane_state})
         if (p) cudaFree(p);
     if (ev0) cudaEventDestroy(ev0);
     if (ev1) cudaEventDestroy(ev1);
@@ -365,7 +365,7 @@ void Sim::create(const CompiledModel& model, const std::vector<std::string>& nod
     lane_full = prm.has_palette || cm.max_k > 12;
     prm.max_steps = o.max_steps ? o.max_steps : 0xFFFFFFFFu;
     prm.redraw_period = o.redraw_period;
-    if (o.redraw_period && o.layout == MBG_LAYOUT_LANE)
+    if (o.redraw_period && (o.layout == MBG_LAYOUT_LANE || o.layout == MBG_LAYOUT_LANE_GLOBAL))
         throw ArgError("redraw_period is supported by the thread and warp layouts");
     prm.seed = seed;
     prm.n_traj = n_traj;
@@ -400,7 +400,7 @@ void Sim::create(const CompiledModel& model, const std::vector<std::string>& nod
 
     if (o.block_size && (o.block_size % 32 != 0 || o.block_size > 256))
         throw ArgError("block_size must be a multiple of 32, at most 256");
-    if (o.layout < MBG_LAYOUT_AUTO || o.layout > MBG_LAYOUT_LANE) throw ArgError("unknown layout");
+    if (o.layout < MBG_LAYOUT_AUTO || o.layout > MBG_LAYOUT_LANE_GLOBAL) throw ArgError("unknown layout");
     if (o.lane_update < 0 || o.lane_update > 1) throw ArgError("lane_update must be 0 or 1");
     if (o.layout == MBG_LAYOUT_THREAD && cm.words > 16) throw ModelError("thread layout supports at most 512 nodes");
     if (o.layout != MBG_LAYOUT_AUTO) {
@@ -504,11 +504,12 @@ void Sim::autotune() {
     double best = -1;
     Shape best_shape{MBG_LAYOUT_WARP, 256, false};
     std::vector<std::pair<double, Shape>> timed;
-    for (int lay : {MBG_LAYOUT_THREAD, MBG_LAYOUT_WARP, MBG_LAYOUT_LANE}) {
+    for (int lay : {MBG_LAYOUT_THREAD, MBG_LAYOUT_WARP, MBG_LAYOUT_LANE, MBG_LAYOUT_LANE_GLOBAL}) {
         for (int blk : {64, 128, 256}) {
             for (int coop = 0; coop < 2; ++coop) {
                 if (opts.block_size > 0 && blk != opts.block_size) continue;
                 if (lay != MBG_LAYOUT_LANE && (blk == 64 || coop)) continue;
+                if (lay == MBG_LAYOUT_LANE_GLOBAL && opts.redraw_period) continue;
                 if (lay == MBG_LAYOUT_THREAD && cm.words > 16) continue;
                 if (lay == MBG_LAYOUT_LANE && (opts.redraw_period || sim_lane_smem(cm.n, blk) > 227 * 1024)) continue;
                 try {
@@ -584,6 +585,10 @@ void Sim::setup_layout(int lay, int blk, bool coop) {
         smem = 0;
         ck(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, (const void*)thread_kernel, block, 0),
            "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
+    } else if (layout == MBG_LAYOUT_LANE_GLOBAL) {
+        smem = 0;
+        lane_coop = false;  // per-lane reader update only
+        ck(sim_lane_global_configure(lane_full, block, &bps), "configuring mbg_sim_lane_global");
     } else if (layout == MBG_LAYOUT_LANE) {
         smem = sim_lane_smem(cm.n, block);
         if (smem > 227 * 1024) throw ModelError("model too large for the lane layout's shared memory at this block size");
@@ -600,6 +605,26 @@ void Sim::setup_layout(int lay, int blk, bool coop) {
     if (bps < 1) throw CudaError("kernel cannot be resident with this block size");
     if (opts.blocks_per_sm > 0) bps = std::min(bps, (int)opts.blocks_per_sm);
     grid = sms * bps;
+    if (layout == MBG_LAYOUT_LANE_GLOBAL) {
+        // every resident block's rows, each block's share 256-byte aligned
+        const uint64_t block_bytes = (sim_lane_smem(cm.n, block) + 255) & ~(uint64_t)255;
+        const uint64_t need = block_bytes * (uint64_t)grid;
+        if (need > lane_state_bytes) {
+            if (lane_state) cudaFree(lane_state);
+            lane_state = nullptr;
+            lane_state_bytes = 0;
+            void* p = nullptr;
+            cudaError_t e = cudaMalloc(&p, need);
+            if (e != cudaSuccess) {
+                cudaGetLastError();  // the failed allocation's own error
+                throw NoMemError("cudaMalloc of the lane layout's rows: " + std::string(cudaGetErrorString(e)));
+            }
+            lane_state = static_cast<unsigned char*>(p);
+            lane_state_bytes = need;
+        }
+        prm.lane_state = lane_state;
+        prm.lane_block_bytes = block_bytes;
+    }
 }
 
 std::mutex& kernel_attr_mutex() {
@@ -665,7 +690,10 @@ void Sim::launch(cudaStream_t stream) {
         // kernel attributes are process-wide: re-apply this handle's before its launch
         std::lock_guard<std::mutex> lock(kernel_attr_mutex());
         const int want = std::max(1, grid / std::max(1, sms));
-        if (layout == MBG_LAYOUT_LANE) {
+        if (layout == MBG_LAYOUT_LANE_GLOBAL) {
+            ck(sim_kernel_limits(6, lane_full, &block, &smem, &want, 1, hash_bits > 0), "mbg_sim_lane_global attributes");
+            ck(launch_sim_lane_global(prm, lane_full, grid, block, stream), "launch mbg_sim_lane_global");
+        } else if (layout == MBG_LAYOUT_LANE) {
             ck(sim_kernel_limits(lane_full ? 4 : 0, lane_coop, &block, &smem, &want, 1, hash_bits > 0),
                "mbg_sim_lane attributes");
             ck(launch_sim_lane(prm, lane_coop, lane_full, grid, block, smem, stream), "launch mbg_sim_lane");
@@ -706,7 +734,7 @@ void Sim::launch(cudaStream_t stream) {
     summary.jit_ms = jit_ms;
     summary.block_size = block;
     summary.grid_size = grid;
-    summary.lane_update = layout == MBG_LAYOUT_LANE && !lane_coop ? 1 : 0;
+    summary.lane_update = (layout == MBG_LAYOUT_LANE && !lane_coop) || layout == MBG_LAYOUT_LANE_GLOBAL ? 1 : 0;
     summary.window_table = hash_bits > 0 ? 2 : 1;
     summary.window_hash_bits = hash_bits;
     summary.window_entries = hash_bits > 0 ? hc[CNT_WIN_ENTRIES] : 0;

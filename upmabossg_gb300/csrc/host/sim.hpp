@@ -41,6 +41,8 @@ public:
     double jit_ms = 0;
     void* thread_kernel = nullptr;
     void* thread_kernel_hash = nullptr;  // the thread layout's window-hash variant, compiled on first use
+    unsigned char* lane_state = nullptr;  // MBG_LAYOUT_LANE_GLOBAL: every resident block's rows
+    uint64_t lane_state_bytes = 0;
     DeviceLayout dl;
     SimParams prm{};
     uint32_t fp_capacity = 0, n_slots = 0;
