@@ -35,11 +35,13 @@ def test_forward_matches_reference():
     assert np.all(spread == 0.0)  # one member: no spread
 
 
-@pytest.mark.parametrize("dims,rows", [((32, 512, 512, 512, 256), 300), ((24, 136, 136, 100), 129)])
+@pytest.mark.parametrize("dims,rows", [((32, 512, 512, 512, 256), 300), ((24, 136, 136, 100), 129),
+                                       ((32, 512, 512, 512, 256), 40000), ((24, 136, 136, 100), 40003)])
 def test_tcgen05_forward_matches_mma_sync(dims, rows):
     """The tcgen05 GEMM (TMEM accumulator) and the mma.sync GEMM compute the same BF16 products with
     FP32 accumulation; only the summation order differs. Odd sizes exercise the partial tiles (rows
-    and columns outside M and N, K not a multiple of the 16-wide MMA step)."""
+    and columns outside M and N, K not a multiple of the 16-wide MMA step); 40 000 rows make
+    hundreds of 128 x 256 tiles, which run on the persistent kernel with two accumulators."""
     rng = np.random.default_rng(3)
     s = mbg.Surrogate(dims[0], dims[-1], hidden=dims[1], hidden_layers=len(dims) - 2, ensemble=1, seed=9)
     p = mlp.init_params(list(dims), rng)

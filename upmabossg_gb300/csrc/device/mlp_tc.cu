@@ -270,6 +270,221 @@ __global__ void __launch_bounds__(128) mlp_gemm_tma_kernel(const __grid_constant
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TN) : "memory");
 }
 
+// ---------------------------------------------------------------------------------------------
+// Persistent form for products of many tiles (the surrogate's prediction chunks): one CTA per SM
+// walks the 128 x 256 output tiles i = blockIdx.x, + gridDim.x, ... with three roles on separate
+// warps that meet only through mbarriers — warp 0 issues the TMA copies into a 4-stage ring,
+// warp 1 issues the MMAs, warps 2-5 run the epilogue — and two accumulators of 256 TMEM columns
+// each (the whole 512-column tensor memory), so that the epilogue of tile i (TMEM -> registers ->
+// bias/ReLU -> global) overlaps the MMAs of tile i + 1. acc_full[a] is committed by the MMAs of
+// a tile that used accumulator a; acc_empty[a] collects one arrival per epilogue warp once it
+// has read accumulator a out. Every wait is bounded and also gives up as soon as another role
+// has failed (a shared flag), so a failed wait ends the kernel quickly with the error flag set.
+
+namespace {
+
+constexpr int kPStages = 4, kPTN = 256;
+constexpr int kPStageBytes = kTileBytesA + kPTN * TK * 2;  // 48 KiB
+constexpr int kPSmemBytes = kPStages * kPStageBytes + 1024;
+constexpr uint32_t kPIdesc = TcShape<kPTN, 2>::kIdesc;
+
+__device__ __forceinline__ bool mbar_wait_or_fail(uint64_t* bar, unsigned parity, volatile unsigned* fail) {
+    const uint32_t a = smem_u32(bar);
+    for (unsigned i = 0; i < kSpinLimit; ++i) {
+        uint32_t done = 0;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(done)
+            : "r"(a), "r"(parity)
+            : "memory");
+        if (done) return true;
+        if ((i & 255u) == 255u && *fail) return false;
+    }
+    *fail = 1u;
+    return false;
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+}  // namespace
+
+__global__ void __launch_bounds__(192, 1) mlp_gemm_tma_persistent(const __grid_constant__ CUtensorMap tmA,
+                                                                  const __grid_constant__ CUtensorMap tmB,
+                                                                  const GemmArgs g, unsigned* error_flag,
+                                                                  int tiles_n, int tiles) {
+    extern __shared__ unsigned char smem_raw[];
+    __shared__ __align__(8) uint64_t full[kPStages], empty[kPStages], acc_full[2], acc_empty[2], drain;
+    __shared__ uint32_t tmem_slot;
+    __shared__ unsigned fail;
+    unsigned char* smem = reinterpret_cast<unsigned char*>(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    const uint32_t sbase = smem_u32(smem);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int nk = (g.K + TK - 1) / TK;
+    volatile unsigned* vfail = &fail;
+
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_slot)),
+                     "r"(2 * kPTN)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < kPStages; ++i) {
+            mbar_init(&full[i], 1);
+            mbar_init(&empty[i], 1);
+        }
+        for (int i = 0; i < 2; ++i) {
+            mbar_init(&acc_full[i], 1);
+            mbar_init(&acc_empty[i], 4);  // one arrival per epilogue warp
+        }
+        mbar_init(&drain, 1);
+        fail = 0u;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = tmem_slot;
+
+    if (warp == 0) {
+        if (lane == 0) {  // producer: K block `it` of this CTA's run goes to stage it % kPStages
+            int it = 0;
+            for (int tile = blockIdx.x; tile < tiles && !*vfail; tile += gridDim.x) {
+                const int m0 = (tile / tiles_n) * TM, n0 = (tile % tiles_n) * kPTN;
+                for (int kb = 0; kb < nk; ++kb, ++it) {
+                    const int st = it % kPStages;
+                    if (it >= kPStages && !mbar_wait_or_fail(&empty[st], (unsigned)(((it / kPStages) - 1) & 1), vfail))
+                        break;
+                    const uint32_t a = sbase + st * kPStageBytes;
+                    mbar_expect_tx(&full[st], (uint32_t)kPStageBytes);
+                    tma_load_2d(a, &tmA, kb * TK, m0, &full[st]);
+                    tma_load_2d(a + kTileBytesA, &tmB, kb * TK, n0, &full[st]);
+                }
+            }
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {  // MMA issuer: tile j of this CTA accumulates in accumulator j & 1
+            int it = 0, j = 0;
+            for (int tile = blockIdx.x; tile < tiles && !*vfail; tile += gridDim.x, ++j) {
+                const int acc = j & 1;
+                if (j >= 2 && !mbar_wait_or_fail(&acc_empty[acc], (unsigned)(((j >> 1) - 1) & 1), vfail)) break;
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                const uint32_t d = tmem + (uint32_t)(acc * kPTN);
+                bool ok = true;
+                for (int kb = 0; kb < nk; ++kb, ++it) {
+                    const int st = it % kPStages;
+                    if (!mbar_wait_or_fail(&full[st], (unsigned)((it / kPStages) & 1), vfail)) {
+                        ok = false;
+                        break;
+                    }
+                    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                    const uint32_t a = sbase + st * kPStageBytes, b = a + kTileBytesA;
+                    const int steps = (min(TK, g.K - kb * TK) + 15) / 16;
+                    for (int s = 0; s < steps; ++s)
+                        mma_bf16_tc(d, smem_desc_sw128(a + 32u * s), smem_desc_sw128(b + 32u * s), kPIdesc,
+                                    (kb > 0 || s > 0) ? 1u : 0u);
+                    mma_commit(&empty[st]);
+                }
+                if (!ok) break;
+                mma_commit(&acc_full[acc]);
+            }
+            // every MMA issued here has completed before the tensor memory is released, even when
+            // a failed wait cut the loop short
+            mma_commit(&drain);
+            mbar_wait(&drain, 0u);
+        }
+    } else {  // epilogue: warp w reads TMEM lanes 32 (w % 4) .. + 31, the tile's rows of that quarter
+        const int q = warp & 3;
+        const bool vec_b = g.Cb && (g.ldcb % 8) == 0 && ((uintptr_t)g.Cb & 15u) == 0;
+        const bool vec_f = g.C && !g.accumulate && (g.ldc % 4) == 0 && ((uintptr_t)g.C & 15u) == 0;
+        int j = 0;
+        for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x, ++j) {
+            const int acc = j & 1;
+            bool ok = mbar_wait_or_fail(&acc_full[acc], (unsigned)((j >> 1) & 1), vfail);
+            ok = __all_sync(0xffffffffu, ok);
+            if (!ok) break;
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const int m0 = (tile / tiles_n) * TM, n0 = (tile % tiles_n) * kPTN;
+            const int row = m0 + q * 32 + lane;
+            const uint32_t lane_addr = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(acc * kPTN);
+            const bool vec_bias = ((uintptr_t)g.bias & 15u) == 0 && (n0 % 4) == 0;
+#pragma unroll 1
+            for (int c0 = 0; c0 < kPTN; c0 += 32) {
+                float v[32];
+                __syncwarp();
+                tmem_ld32(lane_addr + (uint32_t)c0, v);
+                const int col0 = n0 + c0;
+                if (row >= g.M || col0 >= g.N) continue;
+                const bool full_cols = col0 + 32 <= g.N;
+                float bias[32];
+                if (g.bias && full_cols && vec_bias) {
+#pragma unroll
+                    for (int k4 = 0; k4 < 8; ++k4) {
+                        const float4 b4 = __ldg(reinterpret_cast<const float4*>(g.bias + col0) + k4);
+                        bias[4 * k4] = b4.x;
+                        bias[4 * k4 + 1] = b4.y;
+                        bias[4 * k4 + 2] = b4.z;
+                        bias[4 * k4 + 3] = b4.w;
+                    }
+                } else {
+#pragma unroll
+                    for (int i = 0; i < 32; ++i) bias[i] = g.bias && col0 + i < g.N ? __ldg(g.bias + col0 + i) : 0.f;
+                }
+#pragma unroll
+                for (int i = 0; i < 32; ++i) {
+                    float x = g.alpha * v[i] + bias[i];
+                    if (g.relu) x = x > 0.f ? x : 0.f;
+                    v[i] = x;
+                }
+                if (g.Cb) {
+                    __nv_bfloat16* dst = g.Cb + (long long)row * g.ldcb + col0;
+                    if (full_cols && vec_b) {
+#pragma unroll
+                        for (int k4 = 0; k4 < 4; ++k4) {
+                            uint4 w;
+                            unsigned* wp = reinterpret_cast<unsigned*>(&w);
+#pragma unroll
+                            for (int h = 0; h < 4; ++h) {
+                                const __nv_bfloat162 b2 = __floats2bfloat162_rn(v[8 * k4 + 2 * h], v[8 * k4 + 2 * h + 1]);
+                                wp[h] = *reinterpret_cast<const unsigned*>(&b2);
+                            }
+                            reinterpret_cast<uint4*>(dst)[k4] = w;
+                        }
+                    } else {
+#pragma unroll
+                        for (int i = 0; i < 32; ++i)
+                            if (col0 + i < g.N) dst[i] = __float2bfloat16(v[i]);
+                    }
+                }
+                if (g.C) {
+                    float* dst = g.C + (long long)row * g.ldc + col0;
+                    if (full_cols && vec_f) {
+#pragma unroll
+                        for (int k4 = 0; k4 < 8; ++k4)
+                            reinterpret_cast<float4*>(dst)[k4] =
+                                make_float4(v[4 * k4], v[4 * k4 + 1], v[4 * k4 + 2], v[4 * k4 + 3]);
+                    } else {
+#pragma unroll
+                        for (int i = 0; i < 32; ++i)
+                            if (col0 + i < g.N) dst[i] = g.accumulate ? dst[i] + v[i] : v[i];
+                    }
+                }
+            }
+            // the accumulator is read out: the MMAs of tile j + 2 may overwrite it
+            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&acc_empty[acc]);
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (threadIdx.x == 0 && fail) atomicOr(error_flag, 1u);
+    if (warp == 1)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * kPTN) : "memory");
+}
+
 namespace {
 
 using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
@@ -320,8 +535,23 @@ cudaError_t mlp_gemm_tc_configure() {
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(mlp_gemm_tma_kernel<256, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  TcShape<256, 2>::kSmemBytes);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(mlp_gemm_tma_persistent, cudaFuncAttributeMaxDynamicSharedMemorySize, kPSmemBytes);
     return e;
 }
+
+namespace {
+int sm_count() {
+    static int n = 0;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        int dev = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+            n = 0;
+    });
+    return n;
+}
+}  // namespace
 
 cudaError_t mlp_gemm_tc(const GemmArgs& g, unsigned* error_flag, cudaStream_t s) {
     if (!mlp_gemm_tc_supported(g)) return cudaErrorInvalidValue;
@@ -334,6 +564,17 @@ cudaError_t mlp_gemm_tc(const GemmArgs& g, unsigned* error_flag, cudaStream_t s)
     CUtensorMap ma, mb;
     if (!encode_kmajor(&ma, g.A, g.M, g.K, g.a_m, TM) || !encode_kmajor(&mb, g.B, g.N, g.K, g.b_n, tn))
         return cudaErrorInvalidValue;
+    // many 128 x 256 tiles (at least two per SM): the persistent CTAs with two accumulators
+    const int sms = sm_count();
+    const int tiles_n = (g.N + kPTN - 1) / kPTN, tiles = tiles_n * mt;
+    if (tn == 256 && !g.accumulate && sms > 0 && tiles >= 2 * sms) {
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3((unsigned)sms);
+        cfg.blockDim = dim3(192);
+        cfg.dynamicSmemBytes = kPSmemBytes;
+        cfg.stream = s;
+        return cudaLaunchKernelEx(&cfg, mlp_gemm_tma_persistent, ma, mb, g, error_flag, tiles_n, tiles);
+    }
     if (tn == 256)
         mlp_gemm_tma_kernel<256, 2><<<dim3((g.N + 255) / 256, mt), 128, TcShape<256, 2>::kSmemBytes, s>>>(
             ma, mb, g, error_flag);
