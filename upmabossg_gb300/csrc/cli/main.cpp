@@ -7,7 +7,7 @@
 // (main.cpp:148-152) is lifted to the library's own limits.
 //
 // Environment (the argument list stays the reference's): MBG_DEVICE (CUDA ordinal),
-// MBG_LAYOUT (auto | thread | warp | lane), MBG_TIMINGS=1 (JSON run summary on stderr),
+// MBG_LAYOUT (auto | thread | warp | lane | lane_global), MBG_TIMINGS=1 (JSON run summary on stderr),
 // MBG_CONFIG_EXPR (cfg statements applied after the cfg file, e.g. "$k = 2; max_time = 50;"),
 // MBG_MUTANTS (comma-separated NODE:ON / NODE:OFF clamps), MBG_FINAL_STATES_CSV=1 (with -o,
 // also <prefix>_final_states.csv).
@@ -87,6 +87,7 @@ int main(int argc, char** argv) {
         if (!std::strcmp(l, "thread")) opts.layout = MBG_LAYOUT_THREAD;
         else if (!std::strcmp(l, "warp")) opts.layout = MBG_LAYOUT_WARP;
         else if (!std::strcmp(l, "lane")) opts.layout = MBG_LAYOUT_LANE;
+        else if (!std::strcmp(l, "lane_global")) opts.layout = MBG_LAYOUT_LANE_GLOBAL;
     }
     mbg_sim* sim = nullptr;
     int rc = 0;

@@ -31,23 +31,26 @@ extern "C" __global__ void __launch_bounds__(256, 4) mbg_sim_warp_gather(const S
 // One trajectory per lane, state in shared memory, incremental rates; the readers of a flipped
 // node are updated by their own lane, or dealt out over the warp (cooperative variant). The
 // `_full` kernels also handle multi-valued (palette) rates and nodes over more than 12
-// regulators; the others leave those paths out (a smaller loop body, 11-18% faster).
-extern "C" __global__ void __launch_bounds__(256, 3) mbg_sim_lane(const SimParams p) {
+// regulators; the others leave those paths out (a smaller loop body, 11-18% faster). Shared
+// memory, not registers, bounds their residency where they are fastest (512 trajectories per SM
+// at 1000 nodes), so they may use up to 128 registers: at 106 instead of 80 the 1000-node
+// workload runs 4% faster (6.95e9 against 6.66e9 transitions/s).
+extern "C" __global__ void __launch_bounds__(256, 2) mbg_sim_lane(const SimParams p) {
     extern __shared__ __align__(16) unsigned char smem[];
     sim_lane_body<false, false>(p, smem);
 }
 
-extern "C" __global__ void __launch_bounds__(256, 3) mbg_sim_lane_coop(const SimParams p) {
+extern "C" __global__ void __launch_bounds__(256, 2) mbg_sim_lane_coop(const SimParams p) {
     extern __shared__ __align__(16) unsigned char smem[];
     sim_lane_body<true, false>(p, smem);
 }
 
-extern "C" __global__ void __launch_bounds__(256, 3) mbg_sim_lane_full(const SimParams p) {
+extern "C" __global__ void __launch_bounds__(256, 2) mbg_sim_lane_full(const SimParams p) {
     extern __shared__ __align__(16) unsigned char smem[];
     sim_lane_body<false, true>(p, smem);
 }
 
-extern "C" __global__ void __launch_bounds__(256, 3) mbg_sim_lane_coop_full(const SimParams p) {
+extern "C" __global__ void __launch_bounds__(256, 2) mbg_sim_lane_coop_full(const SimParams p) {
     extern __shared__ __align__(16) unsigned char smem[];
     sim_lane_body<true, true>(p, smem);
 }

@@ -27,22 +27,22 @@ extern "C" __global__ void __launch_bounds__(256, 4) mbg_sim_warp_gather_hash(co
     sim_warp_body<false>(p, smem);
 }
 
-extern "C" __global__ void __launch_bounds__(256, 3) mbg_sim_lane_hash(const SimParams p) {
+extern "C" __global__ void __launch_bounds__(256, 2) mbg_sim_lane_hash(const SimParams p) {
     extern __shared__ __align__(16) unsigned char smem[];
     sim_lane_body<false, false>(p, smem);
 }
 
-extern "C" __global__ void __launch_bounds__(256, 3) mbg_sim_lane_coop_hash(const SimParams p) {
+extern "C" __global__ void __launch_bounds__(256, 2) mbg_sim_lane_coop_hash(const SimParams p) {
     extern __shared__ __align__(16) unsigned char smem[];
     sim_lane_body<true, false>(p, smem);
 }
 
-extern "C" __global__ void __launch_bounds__(256, 3) mbg_sim_lane_full_hash(const SimParams p) {
+extern "C" __global__ void __launch_bounds__(256, 2) mbg_sim_lane_full_hash(const SimParams p) {
     extern __shared__ __align__(16) unsigned char smem[];
     sim_lane_body<false, true>(p, smem);
 }
 
-extern "C" __global__ void __launch_bounds__(256, 3) mbg_sim_lane_coop_full_hash(const SimParams p) {
+extern "C" __global__ void __launch_bounds__(256, 2) mbg_sim_lane_coop_full_hash(const SimParams p) {
     extern __shared__ __align__(16) unsigned char smem[];
     sim_lane_body<true, true>(p, smem);
 }
