@@ -75,22 +75,44 @@ def test_predict_column_matches_full_prediction():
         s.predict_column(x[:10], 256)
 
 
-def test_gradients_match_reference():
+@pytest.mark.parametrize("rows", [96, 64, 1, 200])
+def test_gradients_match_reference(rows):
+    """Loss and gradients of every member of a 3-member ensemble (distinct parameters), computed by
+    the training step's member-batched kernels, against the FP32 reference. Row counts below, at
+    and across the 64-row tile, and a single row."""
     rng = np.random.default_rng(1)
-    s = make()
-    p = mlp.init_params(DIMS, rng)
-    s.set_params(0, p)
-    x, y = data(rng, 96)
-    loss, g = s.gradients(0, x, y)
-    ref_loss, ref_g = mlp.loss_and_grad(p, DIMS, x, y)
+    s = make(ensemble=3)
+    ps = [mlp.init_params(DIMS, rng) for _ in range(3)]
+    for e, p in enumerate(ps):
+        s.set_params(e, p)
+    x, y = data(rng, rows)
+    for e, p in enumerate(ps):
+        loss, g = s.gradients(e, x, y)
+        ref_loss, ref_g = mlp.loss_and_grad(p, DIMS, x, y)
+        assert abs(loss - ref_loss) <= 1e-3 * abs(ref_loss)
+        o = 0
+        for i, j in zip(DIMS[:-1], DIMS[1:]):
+            for size in (i * j, j):
+                a, b = g[o:o + size], ref_g[o:o + size]
+                rel = np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-12)
+                assert rel < 2e-2, f"member {e}, layer {i}x{j} block of {size}: relative gradient error {rel}"
+                o += size
+
+
+def test_gradients_of_odd_widths_match_reference():
+    """Widths that are not multiples of 8 (no 16-byte loads) take the element-wise tile loads."""
+    dims = [20, 100, 100, 90]
+    rng = np.random.default_rng(6)
+    s = mbg.Surrogate(dims[0], dims[-1], hidden=dims[1], hidden_layers=2, ensemble=2, seed=2)
+    p = mlp.init_params(dims, rng)
+    s.set_params(1, p)
+    x = rng.uniform(-1, 1, size=(77, dims[0])).astype(np.float32)
+    y = rng.dirichlet(np.full(dims[-1], 0.3), size=77).astype(np.float32)
+    loss, g = s.gradients(1, x, y)
+    ref_loss, ref_g = mlp.loss_and_grad(p, dims, x, y)
     assert abs(loss - ref_loss) <= 1e-3 * abs(ref_loss)
-    o = 0
-    for i, j in zip(DIMS[:-1], DIMS[1:]):
-        for size in (i * j, j):
-            a, b = g[o:o + size], ref_g[o:o + size]
-            rel = np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-12)
-            assert rel < 2e-2, f"layer {i}x{j} block of {size}: relative gradient error {rel}"
-            o += size
+    rel = np.linalg.norm(g - ref_g) / np.linalg.norm(ref_g)
+    assert rel < 2e-2
 
 
 def test_training_reduces_loss_and_ensemble_spread_is_informative():

@@ -27,7 +27,8 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 HOST_SOURCES = ["parser.cpp", "model.cpp", "codegen.cpp", "jit.cpp", "sim.cpp", "batch.cpp", "surrogate.cpp",
                 "output.cpp", "capi.cpp"]
-DEVICE_SOURCES = ["sim_aot.cu", "sim_aot_hash.cu", "window_table.cu", "noalloc.cu", "mlp.cu", "mlp_tc.cu"]
+DEVICE_SOURCES = ["sim_aot.cu", "sim_aot_hash.cu", "window_table.cu", "noalloc.cu", "mlp.cu", "mlp_tc.cu",
+                  "mlp_train.cu"]
 JIT_HEADERS = ["sim_types.h", "philox.h", "sim_core.cuh", "sim_thread.cuh"]
 
 

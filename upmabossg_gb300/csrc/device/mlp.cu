@@ -1,12 +1,13 @@
 // Kernels of the learned surrogate: a BF16 multilayer perceptron (FP32 accumulation) that maps a
 // sweep point's rate-scaling parameters to the output-state distribution of the final window.
-// Forward, backward and Adam steps are all here; the host side is surrogate.cpp.
+// Here: the general mma.sync product, softmax / cross-entropy, ensemble statistics and small
+// helpers; the training step's member-batched products, gather and Adam are in mlp_train.cu, the
+// tcgen05 forward product in mlp_tc.cu; the host side is surrogate.cpp.
 //
-// GEMM: C[M x N] = A[M x K] . B[K x N] with arbitrary element strides for A and B, so the same
-// kernel computes forward products (activations . W), data gradients (dZ . W^T) and weight
-// gradients (A^T . dZ). Tiles of 64 x 64 x 32 are staged in shared memory as BF16 and multiplied
-// with the m16n8k16 BF16 tensor-core instruction; the epilogue adds a bias, applies ReLU and
-// stores FP32 and/or BF16.
+// GEMM: C[M x N] = A[M x K] . B[K x N] with arbitrary element strides for A and B (the forward
+// product when the tcgen05 path is off or does not apply). Tiles of 64 x 64 x 32 are staged in
+// shared memory as BF16 and multiplied with the m16n8k16 BF16 tensor-core instruction; the
+// epilogue adds a bias, applies ReLU and stores FP32 and/or BF16.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -109,13 +110,20 @@ cudaError_t mlp_gemm(const GemmArgs& g, cudaStream_t s) {
     return cudaGetLastError();
 }
 
-// One warp per row.
+// One warp per row; blockIdx.y selects a stacked [rows x cols] block (member), whose loss goes to
+// loss[blockIdx.y].
 __global__ void mlp_softmax_xent_kernel(const float* __restrict__ logits, int rows, int cols,
                                         const float* __restrict__ target, float scale, float* __restrict__ probs,
                                         __nv_bfloat16* __restrict__ dlogits, float* __restrict__ loss) {
     const int lane = threadIdx.x & 31;
     const int row = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     if (row >= rows) return;
+    const long long zo = (long long)blockIdx.y * rows * cols;
+    logits += zo;
+    if (target) target += zo;
+    if (probs) probs += zo;
+    if (dlogits) dlogits += zo;
+    if (loss) loss += blockIdx.y;
     const float* z = logits + (long long)row * cols;
     float mx = -3.4e38f;
     for (int c = lane; c < cols; c += 32) mx = fmaxf(mx, z[c]);
@@ -151,58 +159,16 @@ cudaError_t mlp_softmax_xent(const float* logits, int rows, int cols, const floa
     return cudaGetLastError();
 }
 
-__global__ void mlp_relu_backward_kernel(const float* __restrict__ da, const __nv_bfloat16* __restrict__ act,
-                                         __nv_bfloat16* __restrict__ dh, long long n) {
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-        dh[i] = __float2bfloat16(__bfloat162float(act[i]) > 0.f ? da[i] : 0.f);
-}
-
-cudaError_t mlp_relu_backward(const float* da, const __nv_bfloat16* act, __nv_bfloat16* dh, long long n,
-                              cudaStream_t s) {
-    mlp_relu_backward_kernel<<<1024, 256, 0, s>>>(da, act, dh, n);
+cudaError_t mlp_softmax_xent_members(const float* logits, int rows, int cols, int members, const float* target,
+                                     float scale, __nv_bfloat16* dlogits, float* loss, cudaStream_t s) {
+    const int warps = 8;
+    mlp_softmax_xent_kernel<<<dim3((rows + warps - 1) / warps, members), warps * 32, 0, s>>>(
+        logits, rows, cols, target, scale, nullptr, dlogits, loss);
     return cudaGetLastError();
 }
 
-// One thread per column, rows summed in order (deterministic).
-__global__ void mlp_bias_grad_kernel(const __nv_bfloat16* __restrict__ d, int rows, int cols, float* __restrict__ db) {
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= cols) return;
-    float s = 0.f;
-    for (int r = 0; r < rows; ++r) s += __bfloat162float(d[(long long)r * cols + c]);
-    db[c] = s;
-}
 
-cudaError_t mlp_bias_grad(const __nv_bfloat16* d, int rows, int cols, float* db, cudaStream_t s) {
-    mlp_bias_grad_kernel<<<(cols + 127) / 128, 128, 0, s>>>(d, rows, cols, db);
-    return cudaGetLastError();
-}
 
-// Adam with the step's learning rate and bias corrections read from per-step tables at the step
-// counter *t (for replayed training graphs).
-__global__ void mlp_adam_sched_kernel(float* __restrict__ w, const float* __restrict__ g, float* __restrict__ m,
-                                      float* __restrict__ v, __nv_bfloat16* __restrict__ wb, long long n,
-                                      const float* __restrict__ sched, const int* __restrict__ t, float beta1,
-                                      float beta2, float eps) {
-    const int k = *t;
-    const float lr = sched[3 * k], c1 = sched[3 * k + 1], c2 = sched[3 * k + 2];
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
-         i += (long long)gridDim.x * blockDim.x) {
-        const float gi = g[i];
-        const float mi = beta1 * m[i] + (1.f - beta1) * gi;
-        const float vi = beta2 * v[i] + (1.f - beta2) * gi * gi;
-        m[i] = mi;
-        v[i] = vi;
-        const float wi = w[i] - lr * (mi * c1) / (sqrtf(vi * c2) + eps);
-        w[i] = wi;
-        if (wb) wb[i] = __float2bfloat16(wi);
-    }
-}
-
-cudaError_t mlp_adam_sched(float* w, const float* g, float* m, float* v, __nv_bfloat16* wb, long long n,
-                           const float* sched, const int* t, float beta1, float beta2, float eps, cudaStream_t s) {
-    mlp_adam_sched_kernel<<<512, 256, 0, s>>>(w, g, m, v, wb, n, sched, t, beta1, beta2, eps);
-    return cudaGetLastError();
-}
 
 __global__ void mlp_step_advance_kernel(int* t) { *t += 1; }
 
@@ -265,43 +231,5 @@ cudaError_t mlp_ensemble_stats(const float* probs, int members, int rows, int co
     return cudaGetLastError();
 }
 
-__global__ void mlp_gather_rows_kernel(const float* __restrict__ x, const int* __restrict__ idx, int rows, int cols,
-                                       float* __restrict__ y, __nv_bfloat16* __restrict__ yb) {
-    const long long total = (long long)rows * cols;
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
-         i += (long long)gridDim.x * blockDim.x) {
-        const long long r = i / cols, c = i % cols;
-        const float v = x[(long long)idx[r] * cols + c];
-        if (y) y[i] = v;
-        if (yb) yb[i] = __float2bfloat16(v);
-    }
-}
-
-// The rows of minibatch (*t mod steps) of a permutation: idx + (*t % steps) * rows.
-__global__ void mlp_gather_rows_step_kernel(const float* __restrict__ x, const int* __restrict__ perm,
-                                            const int* __restrict__ t, int steps, int rows, int cols,
-                                            float* __restrict__ y, __nv_bfloat16* __restrict__ yb) {
-    const int* idx = perm + (long long)(*t % steps) * rows;
-    const long long total = (long long)rows * cols;
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
-         i += (long long)gridDim.x * blockDim.x) {
-        const long long r = i / cols, c = i % cols;
-        const float v = x[(long long)idx[r] * cols + c];
-        if (y) y[i] = v;
-        if (yb) yb[i] = __float2bfloat16(v);
-    }
-}
-
-cudaError_t mlp_gather_rows_step(const float* x, const int* perm, const int* t, int steps, int rows, int cols,
-                                 float* y, __nv_bfloat16* yb, cudaStream_t s) {
-    mlp_gather_rows_step_kernel<<<512, 256, 0, s>>>(x, perm, t, steps, rows, cols, y, yb);
-    return cudaGetLastError();
-}
-
-cudaError_t mlp_gather_rows(const float* x, const int* idx, int rows, int cols, float* y, __nv_bfloat16* yb,
-                            cudaStream_t s) {
-    mlp_gather_rows_kernel<<<512, 256, 0, s>>>(x, idx, rows, cols, y, yb);
-    return cudaGetLastError();
-}
 
 }  // namespace mbg

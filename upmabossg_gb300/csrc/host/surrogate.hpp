@@ -15,13 +15,13 @@ namespace mbg {
 
 class Surrogate {
 public:
+    // A layer's tensors point into its member's parameter block (see `per_member`).
     struct Layer {
         int in = 0, out = 0;
         float *w = nullptr, *b = nullptr;  // FP32 master weights, W row-major [in][out]
         __nv_bfloat16* wb = nullptr;       // BF16 copy used by the GEMMs
         __nv_bfloat16* wtb = nullptr;      // BF16 W^T [out][in]: the K-major operand of the tcgen05 GEMM
         float *gw = nullptr, *gb = nullptr;
-        float *mw = nullptr, *vw = nullptr, *mb = nullptr, *vb = nullptr;  // Adam moments
     };
     struct Member {
         std::vector<Layer> layers;
@@ -43,37 +43,53 @@ public:
     void set_params(int member, const float* src);
 
     int in_dim = 0, hidden = 0, hidden_layers = 0, out_dim = 0, ensemble = 0, device = 0;
+    // Parameter blocks: member e's tensors of one kind (weights, gradients, Adam moments, BF16
+    // weights) are elements [e * per_member, (e + 1) * per_member) of one allocation per kind, layer
+    // l's W at off_w[l] and its bias at off_b[l] (multiples of 8 elements, zero padding between), so
+    // that one launch updates every member and every layer.
+    long long per_member = 0;
+    std::vector<long long> off_w, off_b;
     // forward products on the tcgen05 tensor cores (true) or on the mma.sync kernel
     bool tensor_tc = true;
     std::vector<Member> members;
 
 private:
-    // Activations, gradients and the stream of one forward/backward pass. Prediction uses `main`;
-    // training gives every member its own, so that the members train concurrently.
+    // Activations of one member's forward pass over a chunk of prediction rows.
     struct Work {
-        cudaStream_t stream = nullptr;
+        int cap_rows = 0;
+        __nv_bfloat16* xb = nullptr;
+        std::vector<__nv_bfloat16*> acts;
+        float* logits = nullptr;
+    };
+    // Buffers of a training step for every member at once, member z's rows after z * rows * width:
+    // inputs, targets, activations, logits, output-layer and hidden-layer gradients, losses.
+    struct StepWork {
         int cap_rows = 0;
         __nv_bfloat16* xb = nullptr;
         float* yt = nullptr;
         std::vector<__nv_bfloat16*> acts;
         float* logits = nullptr;
         __nv_bfloat16* dlogits = nullptr;
-        float* da = nullptr;
-        __nv_bfloat16 *dh = nullptr, *dh2 = nullptr;
+        __nv_bfloat16* dh[2] = {nullptr, nullptr};
         float* loss = nullptr;
     };
     template <class T>
     T* alloc(size_t n);
-    void ensure_work(Work& w, int rows);
     void ensure_batch(int rows);
+    void ensure_step(int rows);
     void forward(int member, int rows, Work& w);
-    void backward(int member, int rows, Work& w);
+    // One training step's products for members m0 .. m0 + count - 1 over `rows` rows in step work
+    // slots 0 .. count - 1: forward (activations, logits), then loss, weight, bias and data gradients.
+    void step_forward(int rows, int m0, int count, cudaStream_t s);
+    void step_backward(int rows, int m0, int count, cudaStream_t s);
     void refresh_transposed(int member, cudaStream_t s);
     void check_tc_error();
 
     cudaStream_t stream = nullptr;
     Work main;
-    std::vector<Work> train_work;
+    StepWork sw;
+    float *w_all = nullptr, *g_all = nullptr, *m_all = nullptr, *v_all = nullptr;
+    __nv_bfloat16* wb_all = nullptr;
     int cap_rows = 0;  // prediction buffers below
     float* xf = nullptr;
     float* probs = nullptr;
