@@ -71,7 +71,9 @@ struct MemberGemm {
     bool vec_a = false, vec_b = false;
 };
 // Supported (a_kc, b_kc, epilogue): (1, 0, bias+ReLU BF16), (1, 0, bias FP32), (1, 1, mask BF16),
-// (0, 0, FP32 with bias gradient): the forward, data-gradient and weight-gradient products.
+// (0, 0, FP32 with bias gradient): the forward, data-gradient and weight-gradient products. With
+// vec_a and vec_b the operands stream through a 4-stage cp.async ring, and products of at least 8
+// k-tiles without a bias gradient split K over a 4-CTA cluster.
 cudaError_t mlp_member_gemm(const MemberGemm& g, int members, int epi, bool a_kc, bool b_kc, cudaStream_t s);
 // Member e's minibatch (*t mod steps): rows perm[e * n + (*t mod steps) * rows + r] of x (to BF16,
 // xb [members][rows][cols_x]) and of y (yt [members][rows][cols_y]).

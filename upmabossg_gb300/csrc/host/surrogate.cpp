@@ -238,6 +238,29 @@ void Surrogate::step_backward(int rows, int m0, int count, cudaStream_t s) {
     for (int l = hidden_layers; l >= 0; --l) {
         const Layer& L = members[m0].layers[l];
         const __nv_bfloat16* a_in = l == 0 ? sw.xb : sw.acts[l - 1];
+        __nv_bfloat16* next = sw.dh[l & 1];
+        if (l > 0) {
+            // da[r][i] = sum over o of d[r][o] W[i][o], through the ReLU of the layer below
+            MemberGemm gd;
+            gd.M = rows;
+            gd.N = L.in;
+            gd.K = L.out;
+            gd.A = d;
+            gd.lda = d_cols;
+            gd.a_z = (long long)rows * d_cols;
+            gd.B = wb_all + pb + off_w[l];  // B(o, i) at W[i * out + o]
+            gd.ldb = L.out;
+            gd.b_z = per_member;
+            gd.act = sw.acts[l - 1];
+            gd.ldact = L.in;
+            gd.act_z = (long long)rows * L.in;
+            gd.Cb = next;
+            gd.ldc = L.in;
+            gd.c_z = (long long)rows * L.in;
+            gd.vec_a = aligned16(d) && d_cols % 8 == 0 && gd.a_z % 8 == 0;
+            gd.vec_b = aligned16(gd.B) && L.out % 8 == 0 && per_member % 8 == 0;
+            ck(mlp_member_gemm(gd, count, kMemberGemmMaskBf16, true, true, s), "mlp_member_gemm data gradient");
+        }
         // dW[i][o] = sum over rows of a_in[r][i] d[r][o], db[o] = sum over rows of d[r][o]
         MemberGemm gw;
         gw.M = L.in;
@@ -258,27 +281,6 @@ void Surrogate::step_backward(int rows, int m0, int count, cudaStream_t s) {
         gw.vec_b = aligned16(d) && d_cols % 8 == 0 && gw.b_z % 8 == 0;
         ck(mlp_member_gemm(gw, count, kMemberGemmF32, false, false, s), "mlp_member_gemm weight gradient");
         if (l > 0) {
-            // da[r][i] = sum over o of d[r][o] W[i][o], through the ReLU of the layer below
-            __nv_bfloat16* next = sw.dh[l & 1];
-            MemberGemm gd;
-            gd.M = rows;
-            gd.N = L.in;
-            gd.K = L.out;
-            gd.A = d;
-            gd.lda = d_cols;
-            gd.a_z = (long long)rows * d_cols;
-            gd.B = wb_all + pb + off_w[l];  // B(o, i) at W[i * out + o]
-            gd.ldb = L.out;
-            gd.b_z = per_member;
-            gd.act = sw.acts[l - 1];
-            gd.ldact = L.in;
-            gd.act_z = (long long)rows * L.in;
-            gd.Cb = next;
-            gd.ldc = L.in;
-            gd.c_z = (long long)rows * L.in;
-            gd.vec_a = aligned16(d) && d_cols % 8 == 0 && gd.a_z % 8 == 0;
-            gd.vec_b = aligned16(gd.B) && L.out % 8 == 0 && per_member % 8 == 0;
-            ck(mlp_member_gemm(gd, count, kMemberGemmMaskBf16, true, true, s), "mlp_member_gemm data gradient");
             d = next;
             d_cols = L.in;
         }

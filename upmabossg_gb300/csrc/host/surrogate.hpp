@@ -79,7 +79,7 @@ private:
     void ensure_step(int rows);
     void forward(int member, int rows, Work& w);
     // One training step's products for members m0 .. m0 + count - 1 over `rows` rows in step work
-    // slots 0 .. count - 1: forward (activations, logits), then loss, weight, bias and data gradients.
+    // slots 0 .. count - 1: forward (activations, logits), then loss, data, weight and bias gradients.
     void step_forward(int rows, int m0, int count, cudaStream_t s);
     void step_backward(int rows, int m0, int count, cudaStream_t s);
     void refresh_transposed(int member, cudaStream_t s);
