@@ -287,17 +287,23 @@ def measure_surrogate(n_train=20000, n_traj=10000, n_cand=1_000_000, epochs=120,
     y_held = sim.final_window(held, ids=np.arange(n_train, n_train + 1000))
     p_held, spread_held = s.predict(screen.encode(held))
     tv_held = screen.total_variation(p_held, y_held)
-    # uncertainty gate calibrated on the held-out points: candidates whose ensemble spread exceeds
-    # the held-out 99.9th percentile are re-simulated (about 0.1% of in-distribution candidates,
-    # and every candidate the ensemble disagrees on more than on almost all held-out points)
-    spread_cut = float(np.quantile(spread_held, 0.999))
+    target = int(np.argmax(y.var(axis=0)))
+    # uncertainty gate: candidates whose ensemble spread exceeds the 99.9th percentile of the spread
+    # over 100 000 unlabelled draws of the sweep space (in distribution by construction; a spread
+    # needs no simulation) are re-simulated: about 0.1% of in-distribution candidates, and every
+    # candidate the members disagree on more than on almost all in-distribution points. The 1000
+    # labelled held-out points alone would put the cut at their largest spread, which moves the
+    # number of re-simulated candidates several-fold between trainings.
+    n_calib = 100_000
+    _, spread_calib = s.predict_column(screen.encode(space.sample(rng, n_calib)), target)
+    spread_cut = float(np.quantile(spread_calib, 0.999))
     hi = spread_held >= np.quantile(spread_held, 0.9)
-    gate = {"spread_cut": spread_cut, "quantile": 0.999,
+    gate = {"spread_cut": spread_cut, "quantile": 0.999, "calibration_points": n_calib,
+            "held_out_above_cut": int((spread_held > spread_cut).sum()),
             "tv_held_out_top_decile_spread": float(tv_held[hi].mean()),
             "tv_held_out_rest": float(tv_held[~hi].mean()),
             "spearman_spread_tv": float(np.corrcoef(np.argsort(np.argsort(spread_held)),
                                                     np.argsort(np.argsort(tv_held)))[0, 1])}
-    target = int(np.argmax(y.var(axis=0)))
     threshold = 0.9
     cands = space.sample(rng, n_cand)
     rep = screen.screen(s, sim, cands, target, threshold=threshold, spread_cut=spread_cut, plain_points_per_s=plain,
