@@ -232,12 +232,13 @@ typedef struct {
     int32_t autotune;      /* 1: on the first run, time every shape of every class on a pilot subset
                               of its trajectories and keep the fastest per class */
     int32_t layout;        /* 0: autotuned per class (without autotune: lane where it fits);
-                              MBG_LAYOUT_LANE or MBG_LAYOUT_WARP: that layout for every class */
+                              MBG_LAYOUT_LANE, MBG_LAYOUT_LANE_GLOBAL or MBG_LAYOUT_WARP: that
+                              layout for every class (global rows: per-lane reader update) */
 } mbg_batch_opts;
 
 /* One launch shape the autotuner timed for a class. */
 typedef struct {
-    int32_t layout;        /* MBG_LAYOUT_LANE or MBG_LAYOUT_WARP */
+    int32_t layout;        /* MBG_LAYOUT_LANE, MBG_LAYOUT_LANE_GLOBAL or MBG_LAYOUT_WARP */
     int32_t block_size;
     int32_t variant;       /* lane: 1 cooperative reader update; warp: 1 regulator-index cache */
     int32_t reserved;

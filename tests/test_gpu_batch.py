@@ -62,14 +62,15 @@ def test_batch_matches_single_runs():
 
 
 @pytest.mark.parametrize("layout,block", [(mbg.LAYOUT_LANE, 64), (mbg.LAYOUT_LANE, 256), (mbg.LAYOUT_WARP, 64),
-                                          (mbg.LAYOUT_WARP, 256)])
+                                          (mbg.LAYOUT_WARP, 256), (mbg.LAYOUT_LANE_GLOBAL, 128),
+                                          (mbg.LAYOUT_LANE_GLOBAL, 256)])
 def test_batch_shape_does_not_change_results(layout, block):
     texts = instances()[:4]
     models = [mbg.Model.from_strings(b, c) for b, c in texts]
     ref = mbg.Batch(models, n_traj=[1500] * 4).run()
     other = mbg.Batch(models, n_traj=[1500] * 4, block_size=block, layout=layout).run()
-    assert all(k["layout"] == {mbg.LAYOUT_LANE: "lane", mbg.LAYOUT_WARP: "warp"}[layout] and k["block_size"] == block
-               for k in other.classes())
+    name = {mbg.LAYOUT_LANE: "lane", mbg.LAYOUT_WARP: "warp", mbg.LAYOUT_LANE_GLOBAL: "lane_global"}[layout]
+    assert all(k["layout"] == name and k["block_size"] == block for k in other.classes())
     for i in range(4):
         assert np.array_equal(ref.probtraj_raw(i)[0], other.probtraj_raw(i)[0])
         assert np.array_equal(ref.final_states(i), other.final_states(i))
@@ -107,8 +108,11 @@ def test_graph_replay_and_autotune():
         assert np.array_equal(first[i], batch.probtraj_raw(i)[0])
     assert batch.summary()["transitions"] == s1["transitions"]
     for k in batch.classes():
-        # the autotuner timed lane and warp shapes and kept the fastest
-        assert {t["layout"] for t in k["timings"]} == {"lane", "warp"}
+        # the autotuner timed lane and warp shapes (and global-row lane shapes for large classes)
+        # and kept the fastest
+        tried = {t["layout"] for t in k["timings"]}
+        assert {"lane", "warp"} <= tried <= {"lane", "warp", "lane_global"}
+        assert ("lane_global" in tried) == (k["max_nodes"] > 1184)  # rows over 454 B a trajectory
         best = min(k["timings"], key=lambda t: t["kernel_ms"])
         assert (k["layout"], k["block_size"], k["variant"]) == (best["layout"], best["block_size"], best["variant"])
 

@@ -449,10 +449,10 @@ class Batch:
             cnt = ctypes.c_int32()
             _check(lib().mbg_batch_class_timings(self._h, c, t, k.timings, ctypes.byref(cnt)))
             out.append({"max_nodes": k.max_nodes, "instances": k.instances, "trajectories": k.trajectories,
-                        "layout": {LAYOUT_LANE: "lane", LAYOUT_WARP: "warp"}.get(k.layout, k.layout),
+                        "layout": {LAYOUT_LANE: "lane", LAYOUT_WARP: "warp", LAYOUT_LANE_GLOBAL: "lane_global"}.get(k.layout, k.layout),
                         "block_size": k.block_size, "variant": k.variant, "grid": k.grid,
                         "kernel_ms": k.kernel_ms,
-                        "timings": [{"layout": {LAYOUT_LANE: "lane", LAYOUT_WARP: "warp"}.get(x.layout, x.layout),
+                        "timings": [{"layout": {LAYOUT_LANE: "lane", LAYOUT_WARP: "warp", LAYOUT_LANE_GLOBAL: "lane_global"}.get(x.layout, x.layout),
                                      "block_size": x.block_size, "variant": x.variant, "kernel_ms": x.kernel_ms}
                                     for x in t[:cnt.value]]})
         return out

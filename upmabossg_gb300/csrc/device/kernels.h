@@ -41,6 +41,10 @@ std::mutex& kernel_attr_mutex();
 cudaError_t launch_sim_lane_batch(const BatchDesc& b, bool coop, bool full, int grid, int block, size_t smem,
                                   cudaStream_t stream);
 cudaError_t sim_lane_batch_configure(bool coop, bool full, size_t smem, int block, int* blocks_per_sm);
+// Batched lane layout with global rows (BatchDesc::lane_state, lane_block_bytes; per-lane reader
+// update); sim_kernel_limits numbers it 7 (variant: `_full`).
+cudaError_t launch_sim_lane_batch_global(const BatchDesc& b, bool full, int grid, int block, cudaStream_t stream);
+cudaError_t sim_lane_batch_global_configure(bool full, int block, int* blocks_per_sm);
 cudaError_t launch_sim_warp_batch(const BatchDesc& b, bool cached_index, int grid, int block, size_t smem,
                                   cudaStream_t stream);
 cudaError_t sim_warp_batch_configure(bool cached_index, size_t smem, int block, int* blocks_per_sm);

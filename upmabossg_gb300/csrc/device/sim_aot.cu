@@ -88,6 +88,16 @@ extern "C" __global__ void __launch_bounds__(256, 3) mbg_sim_lane_batch_coop_ful
     sim_lane_batch_body<true, true>(b, smem);
 }
 
+// Batched instances in the lane layout with each block's rows in global memory (per-lane reader
+// update): for size classes whose rows leave few trajectories resident in shared memory.
+extern "C" __global__ void __launch_bounds__(256, 3) mbg_sim_lane_batch_global(const BatchDesc b) {
+    sim_lane_batch_body<false, false>(b, b.lane_state + (size_t)blockIdx.x * b.lane_block_bytes);
+}
+
+extern "C" __global__ void __launch_bounds__(256, 3) mbg_sim_lane_batch_global_full(const BatchDesc b) {
+    sim_lane_batch_body<false, true>(b, b.lane_state + (size_t)blockIdx.x * b.lane_block_bytes);
+}
+
 // Batched instances (parameter sweeps) in the warp layout, both variants.
 extern "C" __global__ void __launch_bounds__(256, 4) mbg_sim_warp_batch(const BatchDesc b) {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -346,6 +356,7 @@ cudaError_t sim_kernel_limits(int kernel, bool variant, const int* blocks, const
         case 5: f = variant ? (const void*)mbg_sim_lane_batch_coop_full : (const void*)mbg_sim_lane_batch_full; break;
         case 2: f = variant ? (const void*)mbg_sim_warp_batch : (const void*)mbg_sim_warp_batch_gather; break;
         case 6: f = variant ? (const void*)mbg_sim_lane_global_full : (const void*)mbg_sim_lane_global; break;
+        case 7: f = variant ? (const void*)mbg_sim_lane_batch_global_full : (const void*)mbg_sim_lane_batch_global; break;
         default: f = variant ? (const void*)mbg_sim_warp : (const void*)mbg_sim_warp_gather; break;
     }
     return shared_limits(f, blocks, smems, want, count);
@@ -371,6 +382,17 @@ cudaError_t sim_lane_batch_configure(bool coop, bool full, size_t smem, int bloc
 }
 
 size_t sim_lane_smem(int n, int block) { return (size_t)block * lane_smem_bytes(n); }
+
+cudaError_t sim_lane_batch_global_configure(bool full, int block, int* blocks_per_sm) {
+    const void* f = full ? (const void*)mbg_sim_lane_batch_global_full : (const void*)mbg_sim_lane_batch_global;
+    cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributePreferredSharedMemoryCarveout, 0);  // all L1
+    if (e != cudaSuccess) return e;
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, f, block, 0);
+}
+
+cudaError_t launch_sim_lane_batch_global(const BatchDesc& b, bool full, int grid, int block, cudaStream_t stream) {
+    return launch(full ? mbg_sim_lane_batch_global_full : mbg_sim_lane_batch_global, grid, block, 0, stream, b);
+}
 
 cudaError_t sim_lane_global_configure(bool full, int block, int* blocks_per_sm) {
     const void* f = full ? (const void*)mbg_sim_lane_global_full : (const void*)mbg_sim_lane_global;

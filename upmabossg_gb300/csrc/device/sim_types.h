@@ -134,6 +134,8 @@ struct BatchDesc {
     unsigned long long* work;          // work-item counter
     unsigned slice_bytes;              // warp layout, per warp: SimParams copy (16-byte padded) + largest slice
     int rows;                          // lane layout: 32-node groups of the largest instance
+    unsigned char* lane_state;         // lane layout with global rows: block b's rows at
+    unsigned long long lane_block_bytes;  // lane_state + b * lane_block_bytes
 };
 
 // Fixed-point hash table and compacted output of one batched instance.

@@ -66,6 +66,7 @@ Batch::~Batch() {
         for (cudaEvent_t e : {k.e0, k.e1, k.join})
             if (e) cudaEventDestroy(e);
         if (k.stream) cudaStreamDestroy(k.stream);
+        if (k.lane_buf) cudaFree(k.lane_buf);
     }
     if (fork) cudaEventDestroy(fork);
     if (small_host) cudaFreeHost(small_host);
@@ -77,8 +78,9 @@ void Batch::create(const std::vector<const CompiledModel*>& models, const std::v
     if (models.empty()) throw ArgError("empty batch");
     if (o.block_size && (o.block_size % 32 != 0 || o.block_size > 256))
         throw ArgError("block_size must be a multiple of 32, at most 256");
-    if (o.layout != 0 && o.layout != MBG_LAYOUT_LANE && o.layout != MBG_LAYOUT_WARP)
-        throw ArgError("batch layout must be 0 (auto), MBG_LAYOUT_LANE or MBG_LAYOUT_WARP");
+    if (o.layout != 0 && o.layout != MBG_LAYOUT_LANE && o.layout != MBG_LAYOUT_WARP &&
+        o.layout != MBG_LAYOUT_LANE_GLOBAL)
+        throw ArgError("batch layout must be 0 (auto), MBG_LAYOUT_LANE, MBG_LAYOUT_LANE_GLOBAL or MBG_LAYOUT_WARP");
     opts = o;
     for (size_t i = 0; i < models.size(); ++i)  // argument checks come before any device call
         check_model_limits(*models[i], n_traj.empty() || n_traj[i] == 0 ? models[i]->sample_count : n_traj[i]);
@@ -292,6 +294,8 @@ void Batch::create(const std::vector<const CompiledModel*>& models, const std::v
         const int blk = o.block_size > 0 ? o.block_size : 128;
         const bool lane_fits = sim_lane_smem(k.max_n, blk) <= kSmemLimit;
         const int lay = o.layout ? o.layout : (lane_fits ? MBG_LAYOUT_LANE : MBG_LAYOUT_WARP);
+        if (lay == MBG_LAYOUT_LANE && !lane_fits)
+            throw ModelError("largest instance of a size class too large for the batched lane layout");
         const bool variant =
             lay == MBG_LAYOUT_WARP && (size_t)(blk / 32) * sim_warp_batch_slice_bytes(k.max_n, true) <= 100 * 1024;
         configure((int)c, lay, blk, variant);
@@ -307,6 +311,30 @@ void Batch::configure(int c, int lay, int blk, bool variant) {
         sm = sim_lane_smem(k.max_n, blk);
         if (sm > kSmemLimit) throw ModelError("largest instance of a size class too large for the batched lane layout");
         ck(sim_lane_batch_configure(variant, k.full, sm, blk, &bps), "batched lane kernel occupancy");
+    } else if (lay == MBG_LAYOUT_LANE_GLOBAL) {
+        variant = false;  // per-lane reader update only
+        ck(sim_lane_batch_global_configure(k.full, blk, &bps), "batched global-row lane kernel occupancy");
+        if (bps < 1) throw CudaError("batched kernel cannot be resident with this block size");
+        if (opts.blocks_per_sm > 0) bps = std::min(bps, (int)opts.blocks_per_sm);
+        // one share of rows per resident block, 256-byte aligned
+        const size_t block_bytes = (sim_lane_smem(k.max_n, blk) + 255) & ~(size_t)255;
+        const size_t need = block_bytes * (size_t)sms * (size_t)bps;
+        if (need > k.lane_buf_bytes) {
+            if (k.lane_buf) cudaFree(k.lane_buf);
+            k.lane_buf = nullptr;
+            k.lane_buf_bytes = 0;
+            cudaError_t e = cudaMalloc(&k.lane_buf, need);
+            if (e != cudaSuccess) {
+                k.lane_buf = nullptr;
+                cudaGetLastError();
+                throw NoMemError("cudaMalloc of " + std::to_string(need) + " bytes: " + cudaGetErrorString(e));
+            }
+            k.lane_buf_bytes = need;
+        }
+        for (BatchDesc* d : {&k.desc, &k.pilot, &k.pilot_long}) {
+            d->lane_state = static_cast<unsigned char*>(k.lane_buf);
+            d->lane_block_bytes = block_bytes;
+        }
     } else {
         const unsigned slice = sim_warp_batch_slice_bytes(k.max_n, variant);
         sm = (size_t)(blk / 32) * slice;
@@ -325,6 +353,7 @@ void Batch::configure(int c, int lay, int blk, bool variant) {
 
 cudaError_t Batch::launch_class(const Class& k, const BatchDesc& d, cudaStream_t s) const {
     if (k.layout == MBG_LAYOUT_LANE) return launch_sim_lane_batch(d, k.variant, k.full, k.grid, k.block, k.smem, s);
+    if (k.layout == MBG_LAYOUT_LANE_GLOBAL) return launch_sim_lane_batch_global(d, k.full, k.grid, k.block, s);
     return launch_sim_warp_batch(d, k.variant, k.grid, k.block, k.smem, s);
 }
 
@@ -380,11 +409,17 @@ void Batch::autotune() {
         double best = -1;
         int best_lay = k.layout, best_blk = k.block;
         bool best_var = k.variant;
-        for (int lay : {MBG_LAYOUT_LANE, MBG_LAYOUT_WARP}) {
+        // global rows only where shared memory holds fewer than 512 of a class's trajectories
+        // per SM (rows over 454 B: above 1184 nodes); below that the shared-memory lane layout is
+        // faster
+        const bool try_global = opts.layout == MBG_LAYOUT_LANE_GLOBAL || sim_lane_smem(k.max_n, 512) > kSmemLimit;
+        for (int lay : {MBG_LAYOUT_LANE, MBG_LAYOUT_WARP, MBG_LAYOUT_LANE_GLOBAL}) {
             if (opts.layout && lay != opts.layout) continue;
+            if (lay == MBG_LAYOUT_LANE_GLOBAL && !try_global) continue;
             for (int blk : {64, 128, 256}) {
                 if (opts.block_size > 0 && blk != opts.block_size) continue;
                 for (int var = 0; var < 2; ++var) {
+                    if (lay == MBG_LAYOUT_LANE_GLOBAL && (var || blk == 64)) continue;
                     if (lay == MBG_LAYOUT_LANE && sim_lane_smem(k.max_n, blk) > kSmemLimit) continue;
                     if (lay == MBG_LAYOUT_WARP &&
                         (size_t)(blk / 32) * sim_warp_batch_slice_bytes(k.max_n, var != 0) > 100 * 1024)
@@ -461,12 +496,19 @@ void Batch::apply_limits() {
     // classes that share a kernel need its largest shared-memory size and a carve-out that keeps
     // every class's resident blocks; kernel attributes are process-wide, so they are re-applied
     // before each launch of the graph
-    for (int kern : {1, 2, 5}) {
+    // kernel numbers of sim_kernel_limits: 1 / 5 batched lane (plain / `_full`, variant: cooperative
+    // update), 2 batched warp, 7 batched lane with global rows (variant: `_full`)
+    auto kernel_of = [](const Class& k) -> std::pair<int, int> {
+        if (k.layout == MBG_LAYOUT_LANE) return {k.full ? 5 : 1, k.variant ? 1 : 0};
+        if (k.layout == MBG_LAYOUT_LANE_GLOBAL) return {7, k.full ? 1 : 0};
+        return {2, k.variant ? 1 : 0};
+    };
+    for (int kern : {1, 2, 5, 7}) {
         for (int var = 0; var < 2; ++var) {
             std::vector<int> blocks, want;
             std::vector<size_t> smems;
             for (const Class& k : classes) {
-                if ((k.layout == MBG_LAYOUT_LANE ? (k.full ? 5 : 1) : 2) != kern || (int)k.variant != var) continue;
+                if (kernel_of(k) != std::make_pair(kern, var)) continue;
                 blocks.push_back(k.block);
                 smems.push_back(k.smem);
                 want.push_back(std::max(1, k.grid / std::max(1, sms)));
@@ -519,7 +561,7 @@ void Batch::run(cudaStream_t stream) {
         r.layout = k.layout;
         r.block_size = k.block;
         r.grid_size = k.grid;
-        r.lane_update = k.layout == MBG_LAYOUT_LANE && !k.variant ? 1 : 0;
+        r.lane_update = (k.layout == MBG_LAYOUT_LANE && !k.variant) || k.layout == MBG_LAYOUT_LANE_GLOBAL ? 1 : 0;
         r.kernel_ms = k.kernel_ms;
         summary.trajectories += r.trajectories;
         summary.transitions += r.transitions;

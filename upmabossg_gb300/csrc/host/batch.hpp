@@ -40,11 +40,13 @@ public:
         BatchDesc pilot{};                  // a subset of every member's trajectories, for timing shapes
         BatchDesc pilot_long{};             // four times the pilot, for re-timing the closest shapes
         bool has_long = false;              // pilot_long covers more than the pilot
-        int layout = MBG_LAYOUT_LANE;       // MBG_LAYOUT_LANE or MBG_LAYOUT_WARP
+        int layout = MBG_LAYOUT_LANE;       // MBG_LAYOUT_LANE, MBG_LAYOUT_LANE_GLOBAL or MBG_LAYOUT_WARP
         int block = 128;
         bool variant = false;               // lane: cooperative reader update; warp: regulator index cache
         size_t smem = 0;
         int grid = 0;
+        void* lane_buf = nullptr;           // global rows of the resident blocks (MBG_LAYOUT_LANE_GLOBAL)
+        size_t lane_buf_bytes = 0;
         cudaEvent_t e0 = nullptr, e1 = nullptr;
         cudaStream_t stream = nullptr;      // the class's branch of the graph
         cudaEvent_t join = nullptr;         // end of that branch
