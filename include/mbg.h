@@ -131,6 +131,30 @@ mbg_status mbg_model_parse_strings(const char* bnd_text, const char* cfg_text, m
  * without editing the model files (the role of MaBoSS's `-e` configuration expressions). */
 mbg_status mbg_model_parse_files_overrides(const char* bnd_path, const char* cfg_path, const char* cfg_overrides,
                                            mbg_model** out);
+/* Run constants of a model built from arrays (the cfg's max_time, time_tick, sample_count,
+ * seed_pseudorandom and discrete_time). */
+typedef struct {
+    double max_time;
+    double time_tick;
+    uint64_t sample_count;
+    uint64_t seed;
+    int32_t discrete_time;
+    int32_t reserved;
+} mbg_model_run;
+/* A model given by arrays instead of .bnd/.cfg text (synthetic and generated networks, sweeps
+ * built by a program); it replaces writing a .bnd/.cfg pair for driver::parse
+ * (src/parser/driver.cpp:16-31). Node i reads regs[reg_off[i] .. reg_off[i + 1]) (n + 1 offsets,
+ * reg_off[0] = 0; distinct node indices other than i, in any order, at most 24); its logic over
+ * them is bit idx = sum_j state(regs[reg_off[i] + j]) << j of the words starting at
+ * logic[logic_off[i]] (2^k bits for k regulators). The node turns on at rate_up[i] while it is off
+ * and its logic is 1, and off at rate_down[i] while it is on and its logic is 0: MaBoSS's
+ * `rate_up = @logic ? u : 0; rate_down = @logic ? 0 : d;` (generator.cpp:84-122), compiled
+ * exactly as that .bnd text would be. istate[i] in [0, 1]; is_output (NULL: every node) marks the
+ * non-internal nodes; names (NULL: "N0", "N1", ...) must be distinct and non-empty. */
+mbg_status mbg_model_from_arrays(int32_t n, const char* const* names, const int32_t* reg_off, const int32_t* regs,
+                                 const uint32_t* logic, const int64_t* logic_off, const double* rate_up,
+                                 const double* rate_down, const double* istate, const uint8_t* is_output,
+                                 const mbg_model_run* run, mbg_model** out);
 void mbg_model_destroy(mbg_model* m);
 mbg_status mbg_model_info_get(const mbg_model* m, mbg_model_info* out);
 const char* mbg_model_node_name(const mbg_model* m, int32_t i);

@@ -24,7 +24,7 @@ EXPORTS = (
     "mbg_last_error", "mbg_version", "mbg_device_count", "mbg_model_parse_files", "mbg_model_parse_strings",
     "mbg_model_destroy", "mbg_model_info_get", "mbg_model_node_name", "mbg_model_outputs", "mbg_model_rate",
     "mbg_model_with_rate_scales", "mbg_model_parse_files_overrides", "mbg_model_with_mutations",
-    "mbg_model_jit_check", "mbg_model_layout_check",
+    "mbg_model_jit_check", "mbg_model_layout_check", "mbg_model_from_arrays",
     "mbg_sim_opts_default", "mbg_sim_create", "mbg_sim_destroy", "mbg_sim_run", "mbg_sim_summary",
     "mbg_sim_probtraj", "mbg_sim_probtraj_raw", "mbg_sim_probtraj_sparse", "mbg_sim_final_states", "mbg_sim_fixed_points",
     "mbg_sim_trajectories", "mbg_write_probtraj_csv", "mbg_write_fp_csv", "mbg_print_results",
@@ -71,6 +71,11 @@ class ModelInfo(ctypes.Structure):
                 ("sample_count", ctypes.c_uint64), ("seed", ctypes.c_uint64)]
 
 
+class ModelRun(ctypes.Structure):
+    _fields_ = [("max_time", ctypes.c_double), ("time_tick", ctypes.c_double), ("sample_count", ctypes.c_uint64),
+                ("seed", ctypes.c_uint64), ("discrete_time", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+
+
 class SimOpts(ctypes.Structure):
     _fields_ = [("n_traj", ctypes.c_uint64), ("traj_base", ctypes.c_uint64), ("seed", ctypes.c_uint64),
                 ("use_cfg_seed", ctypes.c_int32), ("layout", ctypes.c_int32),
@@ -113,6 +118,8 @@ def lib():
             "mbg_device_count": (ctypes.c_int, []),
             "mbg_model_parse_files": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_char_p, ctypes.POINTER(vp)]),
             "mbg_model_parse_strings": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_char_p, ctypes.POINTER(vp)]),
+            "mbg_model_from_arrays": (ctypes.c_int, [i32, ctypes.POINTER(ctypes.c_char_p), vp, vp, vp, vp, vp, vp,
+                                                     vp, vp, ctypes.POINTER(ModelRun), ctypes.POINTER(vp)]),
             "mbg_model_parse_files_overrides": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p,
                                                                ctypes.POINTER(vp)]),
             "mbg_model_with_mutations": (ctypes.c_int, [vp, dp, dp, i32, ctypes.POINTER(vp)]),
@@ -228,6 +235,47 @@ class Model:
     def from_strings(cls, bnd, cfg):
         h = ctypes.c_void_p()
         _check(lib().mbg_model_parse_strings(bnd.encode(), cfg.encode(), ctypes.byref(h)))
+        return cls(h)
+
+    @classmethod
+    def from_arrays(cls, regulators, logic, rate_up, rate_down, istate, is_output=None, names=None, max_time=10.0,
+                    time_tick=0.1, sample_count=1000000, seed=0, discrete=False):
+        """A model from arrays (mbg_model_from_arrays): regulators[i] lists node i's regulators,
+        logic[i] its truth table over them (2^k entries of 0/1, entry idx = sum_j state(reg_j) << j);
+        the node turns on at rate_up[i] while off with logic 1, off at rate_down[i] while on with
+        logic 0. is_output (default: every node) marks the non-internal nodes."""
+        n = len(regulators)
+        reg_off = np.zeros(n + 1, np.int32)
+        for i, r in enumerate(regulators):
+            reg_off[i + 1] = reg_off[i] + len(r)
+        regs = np.ascontiguousarray(np.concatenate([np.asarray(r, np.int32) for r in regulators])
+                                    if reg_off[-1] else np.zeros(1, np.int32), dtype=np.int32)
+        words, logic_off = [], np.zeros(n, np.int64)
+        for i, (r, t) in enumerate(zip(regulators, logic)):
+            t = np.asarray(t, np.uint8).ravel()
+            if t.size != 1 << len(r):
+                raise ValueError(f"node {i}: truth table needs {1 << len(r)} entries")
+            logic_off[i] = len(words)
+            bits = np.zeros(((t.size + 31) // 32) * 32, np.uint8)
+            bits[:t.size] = t != 0
+            w = (bits.reshape(-1, 32).astype(np.uint64) << np.arange(32, dtype=np.uint64)).sum(axis=1)
+            words.extend(int(x) for x in w)
+        logic_w = np.ascontiguousarray(np.array(words, np.uint32))
+        up = np.ascontiguousarray(np.asarray(rate_up, np.float64))
+        down = np.ascontiguousarray(np.asarray(rate_down, np.float64))
+        ist = np.ascontiguousarray(np.asarray(istate, np.float64))
+        if not (up.size == down.size == ist.size == n) or (is_output is not None and len(is_output) != n):
+            raise ValueError("one rate_up, rate_down, istate (and is_output) entry per node")
+        outs = None if is_output is None else np.ascontiguousarray(np.asarray(is_output, np.uint8))
+        cnames = None
+        if names is not None:
+            if len(names) != n:
+                raise ValueError("one name per node")
+            cnames = (ctypes.c_char_p * n)(*[s.encode() for s in names])
+        run = ModelRun(max_time, time_tick, sample_count, seed, 1 if discrete else 0, 0)
+        h = ctypes.c_void_p()
+        _check(lib().mbg_model_from_arrays(n, cnames, _p(reg_off), _p(regs), _p(logic_w), _p(logic_off), _p(up),
+                                           _p(down), _p(ist), _p(outs), ctypes.byref(run), ctypes.byref(h)))
         return cls(h)
 
     def rate(self, node: int, state) -> tuple:

@@ -9,6 +9,7 @@
 #include <fstream>
 #include <iostream>
 #include <memory>
+#include <set>
 
 #include "batch.hpp"
 #include "sim.hpp"
@@ -140,6 +141,43 @@ mbg_status mbg_model_parse_strings(const char* bnd_text, const char* cfg_text, m
 }
 
 void mbg_model_destroy(mbg_model* m) { delete m; }
+
+mbg_status mbg_model_from_arrays(int32_t n, const char* const* names, const int32_t* reg_off, const int32_t* regs,
+                                 const uint32_t* logic, const int64_t* logic_off, const double* rate_up,
+                                 const double* rate_down, const double* istate, const uint8_t* is_output,
+                                 const mbg_model_run* run, mbg_model** out) {
+    if (!out) return fail(MBG_ERR_ARG, "null output pointer");
+    *out = nullptr;
+    if (!run) return fail(MBG_ERR_ARG, "null run constants");
+    if (n < 1) return fail(MBG_ERR_ARG, "model has no nodes");
+    std::unique_ptr<mbg_model> m(new mbg_model());
+    mbg_status st = guard([&] {
+        std::set<std::string> seen;
+        for (int32_t i = 0; i < n; ++i) {
+            std::string name = names ? (names[i] ? names[i] : "") : "N" + std::to_string(i);
+            if (name.empty() || !seen.insert(name).second)
+                throw mbg::ArgError("node names must be distinct and non-empty (node " + std::to_string(i) + ")");
+            m->names.push_back(std::move(name));
+        }
+    });
+    if (st != MBG_OK) return st;
+    st = guard([&] {
+        mbg::RunConstants rc;
+        rc.max_time = run->max_time;
+        rc.tick = run->time_tick;
+        rc.sample_count = run->sample_count;
+        rc.seed = run->seed;
+        rc.discrete = run->discrete_time != 0;
+        try {
+            m->cm = mbg::compile_arrays(n, reg_off, regs, logic, logic_off, rate_up, rate_down, istate, is_output, rc);
+        } catch (const mbg::Error& e) {
+            throw mbg::ModelError(e.what());
+        }
+    });
+    if (st != MBG_OK) return st;
+    *out = m.release();
+    return MBG_OK;
+}
 
 mbg_status mbg_model_info_get(const mbg_model* m, mbg_model_info* out) {
     if (!m || !out) return fail(MBG_ERR_ARG, "null argument");

@@ -547,6 +547,107 @@ CompiledModel rescale_model(const CompiledModel& src, const double* up_scale, co
     return cm;
 }
 
+CompiledModel compile_arrays(int n, const int32_t* reg_off, const int32_t* regs, const uint32_t* logic,
+                             const int64_t* logic_off, const double* rate_up, const double* rate_down,
+                             const double* istate, const uint8_t* is_output, const RunConstants& rc) {
+    if (n < 1) throw Error("model has no nodes");
+    if (n > kMaxNodes) throw Error("model has more than 65535 nodes");
+    if (!reg_off || !logic || !logic_off || !rate_up || !rate_down || !istate)
+        throw Error("null model array");
+    if (reg_off[0] != 0) throw Error("reg_off[0] must be 0");
+    for (int i = 0; i < n; ++i)
+        if (reg_off[i + 1] < reg_off[i]) throw Error("reg_off must not decrease");
+    if (reg_off[n] > 0 && !regs) throw Error("null regulator array");
+    CompiledModel cm;
+    cm.n = n;
+    cm.words = (n + 31) / 32;
+    cm.nodes.resize(n);
+    cm.out_pos.assign(n, -1);
+    for (int i = 0; i < n; ++i)
+        if (!is_output || is_output[i]) {
+            cm.out_pos[i] = (int)cm.out_nodes.size();
+            cm.out_nodes.push_back(i);
+        }
+    cm.n_out = (int)cm.out_nodes.size();
+    double sum_max = 0;
+    for (int i = 0; i < n; ++i) {
+        const int k = reg_off[i + 1] - reg_off[i];
+        const std::string name = "#" + std::to_string(i);
+        if (k > kMaxBinaryRegs)
+            throw Error("node " + name + " reads " + std::to_string(k) + " nodes (limit " +
+                        std::to_string(kMaxBinaryRegs) + ")");
+        const double up = rate_up[i], down = rate_down[i];
+        if (!(up >= 0) || !(down >= 0) || std::isinf(up) || std::isinf(down))
+            throw Error("node " + name + " has a negative or non-finite rate");
+        // regulators in ascending order, and where each one sits in the caller's order
+        std::vector<std::pair<int, int>> order;
+        for (int j = 0; j < k; ++j) {
+            const int r = regs[reg_off[i] + j];
+            if (r < 0 || r >= n || r == i) throw Error("node " + name + " has a regulator out of range or itself");
+            order.push_back({r, j});
+        }
+        std::sort(order.begin(), order.end());
+        for (int j = 1; j < k; ++j)
+            if (order[j].first == order[j - 1].first) throw Error("node " + name + " lists a regulator twice");
+        CompiledNode& cn = cm.nodes[i];
+        for (auto& o : order) cn.regs.push_back(o.first);
+        cm.max_k = std::max(cm.max_k, k);
+        const uint64_t half = 1ull << k, total = half << 1;
+        cn.kind = NODE_BINARY;
+        cn.up_real = up;
+        cn.down_real = down;
+        cn.bits.assign((total + 31) / 32, 0u);
+        const uint32_t* tab = logic + logic_off[i];
+        bool any_up = false, any_down = false;
+        for (uint64_t a = 0; a < half; ++a) {
+            uint64_t idx = 0;  // the assignment's index in the caller's regulator order
+            for (int j = 0; j < k; ++j) idx |= ((a >> j) & 1ull) << order[j].second;
+            const bool on = (tab[idx >> 5] >> (idx & 31)) & 1u;
+            if (on && up > 0) {
+                cn.bits[a >> 5] |= 1u << (a & 31);
+                any_up = true;
+            }
+            if (!on && down > 0) {
+                const uint64_t b = a + half;
+                cn.bits[b >> 5] |= 1u << (b & 31);
+                any_down = true;
+            }
+        }
+        sum_max += std::max(any_up ? up : 0.0, any_down ? down : 0.0);
+    }
+    cm.frac_bits = frac_bits_for(sum_max);
+    for (auto& cn : cm.nodes) {
+        cn.up = quantize_rate(cn.up_real, cm.frac_bits);
+        cn.down = quantize_rate(cn.down_real, cm.frac_bits);
+    }
+    cm.deps.assign(n, {});
+    for (int i = 0; i < n; ++i) {
+        cm.deps[i].push_back(i);
+        for (int r : cm.nodes[i].regs) cm.deps[r].push_back(i);
+    }
+    for (auto& d : cm.deps) {
+        std::sort(d.begin(), d.end());
+        d.erase(std::unique(d.begin(), d.end()), d.end());
+    }
+    cm.istate.resize(n);
+    cm.istate_thr.resize(n);
+    for (int i = 0; i < n; ++i) {
+        const double p = istate[i];
+        if (!(p >= 0 && p <= 1)) throw Error("istate of node #" + std::to_string(i) + " is outside [0, 1]");
+        cm.istate[i] = p;
+        cm.istate_thr[i] = (uint32_t)std::floor(p * 16777216.0);
+    }
+    cm.discrete = rc.discrete;
+    cm.max_time = rc.max_time;
+    cm.tick = rc.tick;
+    cm.sample_count = rc.sample_count;
+    cm.seed = rc.seed;
+    if (!(cm.max_time > 0) || !(cm.tick > 0)) throw Error("max_time and time_tick must be positive");
+    cm.windows = (int)std::ceil((float)cm.max_time / (float)cm.tick);
+    if (cm.windows < 1) cm.windows = 1;
+    return cm;
+}
+
 CompiledModel compile_model(const Model& m) {
     CompiledModel cm;
     cm.n = (int)m.nodes.size();
