@@ -426,17 +426,23 @@ static int frac_bits_for(double sum_max) {
 static void classify_node(CompiledNode& cn, const std::vector<double>& tab, int fb, const std::string& name) {
     const int k = (int)cn.regs.size();
     const uint64_t half = 1ull << k, total = half << 1;
-    std::set<double> upv, dnv;
-    for (uint64_t a = 0; a < total; ++a)
-        if (tab[a] != 0) (a < half ? upv : dnv).insert(tab[a]);
+    // the binary form needs at most one distinct non-zero value per half
+    double upv = 0, dnv = 0;
+    bool binary = true;
+    for (uint64_t a = 0; a < total && binary; ++a) {
+        if (tab[a] == 0) continue;
+        double& v = a < half ? upv : dnv;
+        if (v == 0) v = tab[a];
+        else if (v != tab[a]) binary = false;
+    }
     cn.bits.clear();
     cn.pidx.clear();
     cn.palette.clear();
     cn.palette_real.clear();
-    if (upv.size() <= 1 && dnv.size() <= 1) {
+    if (binary) {
         cn.kind = NODE_BINARY;
-        cn.up_real = upv.empty() ? 0 : *upv.begin();
-        cn.down_real = dnv.empty() ? 0 : *dnv.begin();
+        cn.up_real = upv;
+        cn.down_real = dnv;
         cn.up = quantize_rate(cn.up_real, fb);
         cn.down = quantize_rate(cn.down_real, fb);
         cn.bits.assign((total + 31) / 32, 0u);
@@ -667,12 +673,17 @@ CompiledModel compile_model(const Model& m) {
     // Tabulate every node's rate over (self, regulators) in double.
     std::vector<std::vector<double>> tabs(cm.n);
     double sum_max = 0;
+    // scratch reused from node to node
+    std::vector<int> sup, inputs;
+    std::vector<Instr> pu, pd;
+    std::vector<double> stack;
+    std::vector<Slot> slots;
     for (int i = 0; i < cm.n; ++i) {
         const Node& nd = m.nodes[i];
         const Expr* up = nd.attr("rate_up");
         const Expr* down = nd.attr("rate_down");
         if (!up || !down) throw Error("Node " + nd.name + " lacks rate_up or rate_down");
-        std::vector<int> sup;
+        sup.clear();
         collect_support(*up, m, i, sup);
         collect_support(*down, m, i, sup);
         std::sort(sup.begin(), sup.end());
@@ -685,14 +696,15 @@ CompiledModel compile_model(const Model& m) {
             throw Error("node " + nd.name + " reads " + std::to_string(k) + " nodes (limit " +
                         std::to_string(kMaxBinaryRegs) + ")");
         cm.max_k = std::max(cm.max_k, k);
-        std::vector<int> inputs = cn.regs;
+        inputs.assign(cn.regs.begin(), cn.regs.end());
         inputs.push_back(i);  // input bit k is the node itself
-        std::vector<Instr> pu, pd;
+        pu.clear();
+        pd.clear();
         flatten(*up, m, i, inputs, pu, 0);
         flatten(*down, m, i, inputs, pd, 0);
         const size_t depth = std::max(stack_depth(pu), stack_depth(pd)) + 1;
-        std::vector<double> stack(kBlock * depth);
-        std::vector<Slot> slots(depth);
+        stack.assign(kBlock * depth, 0.0);
+        slots.assign(depth, Slot{});
         const uint64_t half = 1ull << k, total = half << 1;
         std::vector<double>& tab = tabs[i];
         tab.assign(std::max<uint64_t>(total, kBlock), 0.0);

@@ -49,7 +49,7 @@ struct Node {
 
 struct Model {
     std::vector<Node> nodes;
-    std::map<std::string, double> variables;  // "$name" -> value
+    std::unordered_map<std::string, double> variables;  // "$name" -> value
     std::map<std::string, double> constants;  // defaults from driver.cpp:9-13
 
     std::unordered_map<std::string, int> index;  // node name -> position in `nodes`

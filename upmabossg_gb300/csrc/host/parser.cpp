@@ -32,6 +32,11 @@ struct Token {
     int line = 1, col = 1;
 };
 
+// ASCII character classes (the grammar is ASCII; no locale lookups).
+inline bool is_alpha(char c) { return (unsigned)((c | 0x20) - 'a') < 26u; }
+inline bool is_digit(char c) { return (unsigned)(c - '0') < 10u; }
+inline bool is_ident(char c) { return is_alpha(c) || is_digit(c) || c == '_'; }
+
 bool ieq(const std::string& a, const char* b) {
     size_t n = 0;
     for (; b[n]; ++n) {
@@ -59,37 +64,40 @@ public:
         tk.col = col_;
         if (p_ >= s_.size()) return tk;
         char c = s_[p_];
-        auto is_id0 = [](char ch) { return std::isalpha((unsigned char)ch) != 0; };
-        auto is_id = [](char ch) { return std::isalnum((unsigned char)ch) != 0 || ch == '_'; };
-        if (is_id0(c)) {
+        if (is_alpha(c)) {
             size_t b = p_;
-            while (p_ < s_.size() && is_id(s_[p_])) adv();
-            tk.text = s_.substr(b, p_ - b);
-            if (ieq(tk.text, "AND")) tk.t = Tok::And;
-            else if (ieq(tk.text, "OR")) tk.t = Tok::Or;
-            else if (ieq(tk.text, "XOR")) tk.t = Tok::Xor;
-            else if (ieq(tk.text, "NOT")) tk.t = Tok::Not;
-            else if (ieq(tk.text, "TRUE")) { tk.t = Tok::Number; tk.num = 1; }
-            else if (ieq(tk.text, "FALSE")) { tk.t = Tok::Number; tk.num = 0; }
-            else tk.t = Tok::Ident;
+            while (p_ < s_.size() && is_ident(s_[p_])) ++p_;  // no newline inside a word
+            col_ += (int)(p_ - b);
+            tk.text.assign(s_, b, p_ - b);
+            tk.t = Tok::Ident;
+            if (tk.text.size() <= 5) {  // keywords: AND OR XOR NOT TRUE FALSE, any case
+                if (ieq(tk.text, "AND")) tk.t = Tok::And;
+                else if (ieq(tk.text, "OR")) tk.t = Tok::Or;
+                else if (ieq(tk.text, "XOR")) tk.t = Tok::Xor;
+                else if (ieq(tk.text, "NOT")) tk.t = Tok::Not;
+                else if (ieq(tk.text, "TRUE")) { tk.t = Tok::Number; tk.num = 1; }
+                else if (ieq(tk.text, "FALSE")) { tk.t = Tok::Number; tk.num = 0; }
+            }
             return tk;
         }
-        if ((c == '$' || c == '@') && p_ + 1 < s_.size() && is_id0(s_[p_ + 1])) {
+        if ((c == '$' || c == '@') && p_ + 1 < s_.size() && is_alpha(s_[p_ + 1])) {
             size_t b = p_;
-            adv();
-            while (p_ < s_.size() && is_id(s_[p_])) adv();
-            tk.text = s_.substr(b, p_ - b);
+            ++p_;
+            while (p_ < s_.size() && is_ident(s_[p_])) ++p_;
+            col_ += (int)(p_ - b);
+            tk.text.assign(s_, b, p_ - b);
             tk.t = c == '$' ? Tok::Var : Tok::Alias;
             return tk;
         }
-        bool digit = std::isdigit((unsigned char)c) != 0;
-        bool dot_digit = c == '.' && p_ + 1 < s_.size() && std::isdigit((unsigned char)s_[p_ + 1]);
+        bool digit = is_digit(c);
+        bool dot_digit = c == '.' && p_ + 1 < s_.size() && is_digit(s_[p_ + 1]);
         if (digit || dot_digit) return number(tk);
         auto two = [&](char a, char b) { return c == a && p_ + 1 < s_.size() && s_[p_ + 1] == b; };
-        auto emit = [&](Tok t, int len) {
+        auto emit = [&](Tok t, int len) {  // operators and punctuation: no newline inside
             tk.t = t;
-            tk.text = s_.substr(p_, len);
-            for (int i = 0; i < len; ++i) adv();
+            tk.text.assign(s_, p_, len);
+            p_ += len;
+            col_ += len;
             return tk;
         };
         if (two('&', '&')) return emit(Tok::And, 2);
@@ -153,22 +161,23 @@ private:
     Token number(Token tk) {
         size_t b = p_;
         bool is_float = false;
-        while (p_ < s_.size() && std::isdigit((unsigned char)s_[p_])) adv();
+        while (p_ < s_.size() && is_digit(s_[p_])) ++p_;
         if (p_ < s_.size() && s_[p_] == '.') {
             is_float = true;
-            adv();
-            while (p_ < s_.size() && std::isdigit((unsigned char)s_[p_])) adv();
+            ++p_;
+            while (p_ < s_.size() && is_digit(s_[p_])) ++p_;
         }
         if (p_ < s_.size() && (s_[p_] == 'e' || s_[p_] == 'E')) {
             size_t q = p_ + 1;
             if (q < s_.size() && (s_[q] == '+' || s_[q] == '-')) ++q;
-            if (q < s_.size() && std::isdigit((unsigned char)s_[q])) {
+            if (q < s_.size() && is_digit(s_[q])) {
                 is_float = true;
-                while (p_ < q) adv();
-                while (p_ < s_.size() && std::isdigit((unsigned char)s_[p_])) adv();
+                p_ = q;
+                while (p_ < s_.size() && is_digit(s_[p_])) ++p_;
             }
         }
-        tk.text = s_.substr(b, p_ - b);
+        col_ += (int)(p_ - b);
+        tk.text.assign(s_, b, p_ - b);
         errno = 0;
         if (is_float) {
             tk.t = Tok::Float;
@@ -324,16 +333,19 @@ private:
     }
 
     Token take() {
-        Token t = cur_;
+        Token t = std::move(cur_);
         cur_ = lx_.next();
         return t;
     }
 
+    [[noreturn]] __attribute__((noinline)) void unexpected(Tok want) const {
+        lx_.fail(cur_.line, cur_.col,
+                 std::string("syntax error, unexpected ") + tok_name(cur_.t) +
+                     (cur_.text.empty() ? "" : " '" + cur_.text + "'") + ", expecting " + tok_name(want));
+    }
+
     Token expect(Tok t) {
-        if (cur_.t != t)
-            lx_.fail(cur_.line, cur_.col,
-                     std::string("syntax error, unexpected ") + tok_name(cur_.t) +
-                         (cur_.text.empty() ? "" : " '" + cur_.text + "'") + ", expecting " + tok_name(t));
+        if (cur_.t != t) unexpected(t);
         return take();
     }
 
@@ -362,31 +374,21 @@ private:
             e->kind = k;
             return e;
         };
-        Token t = cur_;
-        switch (t.t) {
+        switch (cur_.t) {
             case Tok::Number:
             case Tok::Float: {
-                take();
                 auto e = mk(Expr::Kind::Literal);
-                e->value = t.num;
-                return e;
-            }
-            case Tok::Ident: {
+                e->value = cur_.num;
                 take();
-                auto e = mk(Expr::Kind::Ident);
-                e->name = t.text;
                 return e;
             }
-            case Tok::Var: {
-                take();
-                auto e = mk(Expr::Kind::Var);
-                e->name = t.text;
-                return e;
-            }
+            case Tok::Ident:
+            case Tok::Var:
             case Tok::Alias: {
+                auto e = mk(cur_.t == Tok::Ident ? Expr::Kind::Ident
+                                                 : cur_.t == Tok::Var ? Expr::Kind::Var : Expr::Kind::Alias);
+                e->name = std::move(cur_.text);
                 take();
-                auto e = mk(Expr::Kind::Alias);
-                e->name = t.text;
                 return e;
             }
             case Tok::LParen: {
@@ -399,16 +401,16 @@ private:
             case Tok::Minus:
             case Tok::Plus:
             case Tok::Not: {
-                take();
                 auto e = mk(Expr::Kind::Unary);
-                e->op = t.t == Tok::Minus ? Op::Minus : t.t == Tok::Plus ? Op::Plus : Op::Not;
+                e->op = cur_.t == Tok::Minus ? Op::Minus : cur_.t == Tok::Plus ? Op::Plus : Op::Not;
+                take();
                 e->a = expr(L_UNARY);
                 return e;
             }
             default:
-                lx_.fail(t.line, t.col,
-                         std::string("syntax error, unexpected ") + tok_name(t.t) +
-                             (t.text.empty() ? "" : " '" + t.text + "'"));
+                lx_.fail(cur_.line, cur_.col,
+                         std::string("syntax error, unexpected ") + tok_name(cur_.t) +
+                             (cur_.text.empty() ? "" : " '" + cur_.text + "'"));
         }
     }
 
