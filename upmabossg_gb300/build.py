@@ -26,7 +26,7 @@ NVCC = os.path.join(CUDA, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 HOST_SOURCES = ["parser.cpp", "model.cpp", "codegen.cpp", "jit.cpp", "sim.cpp", "batch.cpp", "surrogate.cpp",
-                "output.cpp", "capi.cpp"]
+                "output.cpp", "capi.cpp", "devmem.cpp"]
 DEVICE_SOURCES = ["sim_aot.cu", "sim_aot_hash.cu", "window_table.cu", "noalloc.cu", "mlp.cu", "mlp_tc.cu",
                   "mlp_train.cu"]
 JIT_HEADERS = ["sim_types.h", "philox.h", "sim_core.cuh", "sim_thread.cuh"]

@@ -19,6 +19,7 @@
 #include <string>
 
 #include "../../../include/mbg.h"
+#include "../host/devmem.hpp"
 
 namespace mbg {
 // Records the message for mbg_last_error() and returns `st` (defined with the C ABI, capi.cpp).
@@ -98,29 +99,6 @@ __global__ void fp_compact_noalloc(const unsigned* __restrict__ states, int word
     }
 }
 
-// Unique id of the current context (cuCtxGetCurrent + cuCtxGetId through the runtime's driver
-// entry points, so the library still needs no link against libcuda); false if unavailable.
-bool current_context_id(unsigned long long* id) {
-    using GetCurrentFn = CUresult (*)(CUcontext*);
-    using GetIdFn = CUresult (*)(CUcontext, unsigned long long*);
-    static GetCurrentFn get_current = nullptr;
-    static GetIdFn get_id = nullptr;
-    static std::once_flag once;
-    std::call_once(once, [] {
-        void* p = nullptr;
-        cudaDriverEntryPointQueryResult q;
-        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
-            q == cudaDriverEntryPointSuccess)
-            get_current = reinterpret_cast<GetCurrentFn>(p);
-        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
-            q == cudaDriverEntryPointSuccess)
-            get_id = reinterpret_cast<GetIdFn>(p);
-    });
-    CUcontext ctx = nullptr;
-    if (!get_current || !get_id || get_current(&ctx) != CUDA_SUCCESS || !ctx) return false;
-    return get_id(ctx, id) == CUDA_SUCCESS && *id != 0;
-}
-
 // Device address of the scratch array on the current device: looked up with the device current,
 // once per device and context (the first call on a device, and the first after its context was
 // replaced, does the lookup).
@@ -130,7 +108,7 @@ cudaError_t scratch_for_current_device(unsigned** out) {
     if (e != cudaSuccess) return e;
     if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
     unsigned long long id = 0;
-    bool have_id = current_context_id(&id);
+    bool have_id = mbg::current_context_id(&id);
     std::lock_guard<std::mutex> lock(g_setup_mu);
     ScratchAddr& a = g_scratch_addr[dev];
     if (have_id && a.ptr && a.ctx_id == id) {
@@ -140,7 +118,7 @@ cudaError_t scratch_for_current_device(unsigned** out) {
     void* p = nullptr;
     e = cudaGetSymbolAddress(&p, g_fp_scratch);  // also creates the context if it did not exist yet
     if (e != cudaSuccess) return e;
-    if (!have_id) have_id = current_context_id(&id);
+    if (!have_id) have_id = mbg::current_context_id(&id);
     a.ptr = static_cast<unsigned*>(p);
     a.ctx_id = have_id ? id : 0ull;
     *out = a.ptr;

@@ -19,6 +19,7 @@
 #include <tuple>
 
 #include "../device/kernels.h"
+#include "devmem.hpp"
 
 namespace mbg {
 
@@ -30,13 +31,7 @@ void ck(cudaError_t e, const char* what) {
 
 template <class T>
 T* dalloc(size_t n, std::vector<void*>& owned) {
-    if (n == 0) n = 1;
-    void* p = nullptr;
-    cudaError_t e = cudaMalloc(&p, n * sizeof(T));
-    if (e != cudaSuccess) {
-        cudaGetLastError();
-        throw NoMemError("cudaMalloc of " + std::to_string(n * sizeof(T)) + " bytes: " + cudaGetErrorString(e));
-    }
+    void* p = dev_alloc((n ? n : 1) * sizeof(T), "simulation buffer");
     owned.push_back(p);
     return static_cast<T*>(p);
 }
@@ -216,15 +211,14 @@ void check_model_limits(const CompiledModel& cm, uint64_t n_traj) {
 
 namespace {
 
-void* raw_alloc(size_t bytes, const char* what) {
-    void* p = nullptr;
-    cudaError_t e = cudaMalloc(&p, bytes ? bytes : 1);
-    if (e != cudaSuccess) {
-        cudaGetLastError();  // the failed allocation's own error
-        throw NoMemError(std::string("cudaMalloc of ") + std::to_string(bytes) + " bytes (" + what +
-                         "): " + cudaGetErrorString(e));
-    }
-    return p;
+void* raw_alloc(size_t bytes, const char* what) { return dev_alloc(bytes, what); }
+
+// Returns a block to the cache once nothing can still be using it (a replacement in mid-life:
+// the device is synchronised, as cudaFree would).
+void free_now(void* p) {
+    if (!p) return;
+    cudaDeviceSynchronize();
+    dev_free(p);
 }
 
 int ceil_log2_u64(uint64_t x) {
@@ -283,7 +277,7 @@ void Sim::choose_window_table() {
 
 void Sim::set_window_table(int bits) {
     if (hslots) {
-        cudaFree(hslots);
+        free_now(hslots);
         hslots = nullptr;
     }
     if (bits == 0) {
@@ -291,7 +285,7 @@ void Sim::set_window_table(int bits) {
             dense_hist = static_cast<unsigned long long*>(raw_alloc(n_bins * 8, "dense window table"));
     } else {
         if (dense_hist) {
-            cudaFree(dense_hist);
+            free_now(dense_hist);
             dense_hist = nullptr;
         }
         hslots = static_cast<unsigned long long*>(raw_alloc((size_t)16 << bits, "window hash table"));
@@ -315,15 +309,18 @@ void Sim::grow_window_table(int bits) {
 }
 
 Sim::~Sim() {
+    // the blocks go back to the process cache: nothing may still use them (cudaFree synchronised
+    // the device implicitly; the cache does not)
+    if (!owned.empty()) cudaDeviceSynchronize();
     for (void* p : {(void*)dense_hist, (void*)hslots, (void*)wc_bitmap, (void*)wc_wpre, (void*)wc_chunk,
                     (void*)wc_total, (void*)wc_bin, (void*)wc_sum, (void*)lane_state})
-        if (p) cudaFree(p);
+        dev_free(p);
     if (ev0) cudaEventDestroy(ev0);
     if (ev1) cudaEventDestroy(ev1);
     if (evk0) cudaEventDestroy(evk0);
     if (evk1) cudaEventDestroy(evk1);
-    if (host_small) cudaFreeHost(host_small);
-    for (void* p : owned) cudaFree(p);
+    pinned_free(host_small);
+    for (void* p : owned) dev_free(p);
 }
 
 void Sim::create(const CompiledModel& model, const std::vector<std::string>& node_names, const mbg_sim_opts& o) {
@@ -392,7 +389,7 @@ void Sim::create(const CompiledModel& model, const std::vector<std::string>& nod
     fp_out_states = dalloc<unsigned int>((size_t)fp_capacity * cm.words, owned);
     fp_out_cnt = dalloc<unsigned int>(fp_capacity, owned);
     fp_unique = dalloc<unsigned int>(1, owned);
-    ck(cudaMallocHost(&host_small, 256), "cudaMallocHost");
+    host_small = pinned_alloc(256);
     ck(cudaEventCreate(&ev0), "cudaEventCreate");
     ck(cudaEventCreate(&ev1), "cudaEventCreate");
     ck(cudaEventCreate(&evk0), "cudaEventCreate");
@@ -610,16 +607,10 @@ void Sim::setup_layout(int lay, int blk, bool coop) {
         const uint64_t block_bytes = (sim_lane_smem(cm.n, block) + 255) & ~(uint64_t)255;
         const uint64_t need = block_bytes * (uint64_t)grid;
         if (need > lane_state_bytes) {
-            if (lane_state) cudaFree(lane_state);
+            free_now(lane_state);
             lane_state = nullptr;
             lane_state_bytes = 0;
-            void* p = nullptr;
-            cudaError_t e = cudaMalloc(&p, need);
-            if (e != cudaSuccess) {
-                cudaGetLastError();  // the failed allocation's own error
-                throw NoMemError("cudaMalloc of the lane layout's rows: " + std::string(cudaGetErrorString(e)));
-            }
-            lane_state = static_cast<unsigned char*>(p);
+            lane_state = static_cast<unsigned char*>(dev_alloc(need, "lane layout rows"));
             lane_state_bytes = need;
         }
         prm.lane_state = lane_state;
@@ -778,8 +769,8 @@ void Sim::fetch() {
         unsigned long long total = 0;
         ck(cudaMemcpy(&total, wc_total, 8, cudaMemcpyDeviceToHost), "cudaMemcpy D2H");
         if (total > wc_cap) {
-            if (wc_bin) cudaFree(wc_bin);
-            if (wc_sum) cudaFree(wc_sum);
+            free_now(wc_bin);
+            free_now(wc_sum);
             wc_bin = nullptr;
             wc_sum = nullptr;
             wc_cap = 0;
