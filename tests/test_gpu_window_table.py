@@ -1,10 +1,10 @@
 """Window sums in the hash table against the dense table, through the C ABI.
 
 The two tables hold the same integer sums, so every comparison here is exact: the reached bins
-and their sums, the transition entropy, the CSV and stdout reports. Covered: every layout, the
-discrete-time counts, a table too small for the run (grown and re-run until it holds), the
-automatic choice on the 20-output and 10-output workloads, and the sparse read-back against the
-dense one.
+and their sums, the transition entropy, the CSV and stdout reports. Covered: every layout that
+runs on the hash table (the warp layout keeps the dense table), the discrete-time counts, a table
+too small for the run (grown and re-run until it holds), the automatic choice on the 20-output
+and 10-output workloads, and the sparse read-back against the dense one.
 """
 import os
 
@@ -27,7 +27,9 @@ def simulate(bnd, cfg, n, table, bits=0, **kw):
     return model, sim
 
 
-def same_windows(a, b):
+def same_windows(a, b, same_layout=True):
+    """Integer window sums and final states agree across layouts; the transition entropy (float
+    arithmetic evaluated per layout) bit for bit within one layout."""
     ba, sa, pa = a.probtraj_sparse()
     bb, sb, pb = b.probtraj_sparse()
     assert np.array_equal(ba, bb), "reached bins differ"
@@ -35,11 +37,15 @@ def same_windows(a, b):
     assert np.array_equal(pa, pb)
     assert np.all(np.diff(ba.astype(np.int64)) > 0), "bins not in increasing order"
     assert np.all(sa > 0)
-    assert np.array_equal(a.tr_entropy(), b.tr_entropy())
+    if same_layout:
+        assert np.array_equal(a.tr_entropy(), b.tr_entropy())
     assert np.array_equal(a.final_states(), b.final_states())
 
 
-@pytest.mark.parametrize("layout", [mbg.LAYOUT_THREAD, mbg.LAYOUT_WARP, mbg.LAYOUT_LANE])
+HASH_LAYOUTS = [mbg.LAYOUT_THREAD, mbg.LAYOUT_LANE, mbg.LAYOUT_LANE_GLOBAL]
+
+
+@pytest.mark.parametrize("layout", HASH_LAYOUTS)
 def test_hash_table_equals_dense_table(layout):
     net = synth.small()  # 20 outputs: 2^20 states per window
     bnd, cfg = net.bnd(), net.cfg()
@@ -52,13 +58,14 @@ def test_hash_table_equals_dense_table(layout):
     same_windows(dense, hashed)
 
 
-def test_full_table_grows_and_reruns():
+@pytest.mark.parametrize("layout", HASH_LAYOUTS)
+def test_full_table_grows_and_reruns(layout):
     """A 1024-slot table for a run that reaches ~10^5 bins: the first attempts overflow, the run
     repeats on tables four times larger until it holds, and the result is the dense table's."""
     net = synth.small()
     bnd, cfg = net.bnd(), net.cfg()
-    _, dense = simulate(bnd, cfg, 20000, DENSE, layout=mbg.LAYOUT_LANE)
-    _, hashed = simulate(bnd, cfg, 20000, HASH, bits=10, layout=mbg.LAYOUT_LANE)
+    _, dense = simulate(bnd, cfg, 20000, DENSE, layout=layout)
+    _, hashed = simulate(bnd, cfg, 20000, HASH, bits=10, layout=layout)
     s = hashed.summary()
     assert s["window_reruns"] >= 1 and s["window_hash_bits"] > 10
     assert s["window_entries"] * 2 > (1 << 10)
@@ -67,6 +74,24 @@ def test_full_table_grows_and_reruns():
     s2 = hashed.summary()
     assert s2["window_reruns"] == 0 and 2 * s2["window_entries"] <= (1 << s2["window_hash_bits"])
     same_windows(dense, hashed)
+
+
+def test_warp_layout_keeps_dense_table():
+    """The warp layout runs on the dense window table only: a forced hash table is refused, the
+    automatic table choice keeps the dense table for it beyond the size at which other layouts
+    switch, and an automatic layout under a hash table is never the warp layout."""
+    net = synth.small()
+    model = mbg.Model.from_strings(net.bnd(), net.cfg())
+    with pytest.raises(mbg.MbgError):
+        mbg.Simulation(model, n_traj=1000, layout=mbg.LAYOUT_WARP, window_table=HASH)
+    bnd, cfg = wide_output_network()  # 40 x 2^24 bins: 5.4 GB dense
+    model, w = simulate(bnd, cfg, 3000, 0, layout=mbg.LAYOUT_WARP)
+    assert w.summary()["window_table"] == DENSE
+    _, h = simulate(bnd, cfg, 3000, 0)
+    assert h.summary()["window_table"] == HASH and h.summary()["layout"] != mbg.LAYOUT_WARP
+    same_windows(w, h, same_layout=False)
+    _, t = simulate(bnd, cfg, 3000, 0, thread_cutoff=8)  # fixed cutoff: the large-model choice
+    assert t.summary()["window_table"] == HASH and t.summary()["layout"] != mbg.LAYOUT_WARP
 
 
 def test_discrete_time_counts():
@@ -108,7 +133,9 @@ def test_automatic_choice():
     bnd, cfg = wide_output_network()
     model, h = simulate(bnd, cfg, 3000, 0)  # 40 x 2^24 bins: 5.4 GB dense, beyond the 2 GiB the auto mode allows
     assert model.info.outputs == 24 and h.summary()["window_table"] == HASH
-    _, d = simulate(bnd, cfg, 3000, DENSE)
+    hs = h.summary()
+    _, d = simulate(bnd, cfg, 3000, DENSE, layout=hs["layout"], lane_update=hs["lane_update"],
+                    block_size=hs["block_size"])
     same_windows(d, h)
 
 

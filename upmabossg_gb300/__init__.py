@@ -396,9 +396,9 @@ class Simulation:
         bin = window * 2^outputs + output state."""
         n = ctypes.c_size_t()
         _check(lib().mbg_sim_probtraj_sparse(self._h, None, None, None, 0, ctypes.byref(n)))
-        bins = np.zeros(n.value, np.uint64)
-        sums = np.zeros(n.value, np.uint64)
-        probs = np.zeros(n.value, np.float64)
+        bins = np.empty(n.value, np.uint64)  # every entry is written
+        sums = np.empty(n.value, np.uint64)
+        probs = np.empty(n.value, np.float64)
         _check(lib().mbg_sim_probtraj_sparse(self._h, _p(bins), _p(sums), _p(probs), n.value, ctypes.byref(n)))
         return bins, sums, probs
 
@@ -409,7 +409,7 @@ class Simulation:
         return TH
 
     def final_states(self):
-        F = np.zeros(1 << self.model.info.outputs, np.float64)
+        F = np.empty(1 << self.model.info.outputs, np.float64)  # every entry is written
         _check(lib().mbg_sim_final_states(self._h, _p(F)))
         return F
 

@@ -30,12 +30,13 @@ int sim_lane_rows(int n);                 // BatchDesc::rows for models of up to
 // Re-applies the attributes of a simulation kernel for the launch shapes that are about to use it
 // (kernel 0: mbg_sim_lane[_coop], 1: mbg_sim_lane_batch[_coop], 2: mbg_sim_warp_batch[_gather],
 // 3: mbg_sim_warp[_gather], 4: mbg_sim_lane[_coop]_full, 5: mbg_sim_lane_batch[_coop]_full;
-// variant selects the second name; hash: the window-hash twin of kernel 0, 3 or 4): kernel attributes
+// variant selects the second name; hash: the window-hash twin of kernel 0, 4 or 6): kernel attributes
 // are process-wide, so another handle may have changed them since this one was configured.
 cudaError_t sim_kernel_limits(int kernel, bool variant, const int* blocks, const size_t* smems, const int* want,
                               int count, bool hash = false);
-// The window-hash twins of the single-simulation kernels (sim_aot_hash.cu), by the numbering of
-// sim_kernel_limits (0, 3, 4, 6); the launchers pick them when SimParams::hash_bits > 0.
+// The window-hash twins of the lane-layout single-simulation kernels (sim_aot_hash.cu), by the
+// numbering of sim_kernel_limits (0, 4, 6); the launchers pick them when SimParams::hash_bits > 0.
+// The warp layout has none: it runs on the dense window table only.
 const void* sim_kernel_hash(int kernel, bool variant);
 std::mutex& kernel_attr_mutex();
 cudaError_t launch_sim_lane_batch(const BatchDesc& b, bool coop, bool full, int grid, int block, size_t smem,

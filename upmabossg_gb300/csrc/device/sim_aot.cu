@@ -255,8 +255,7 @@ cudaError_t launch_fp_aggregate_batch(const SimParams* params, const FpSlots* fp
 
 cudaError_t launch_sim_warp(const SimParams& p, bool cached_index, int grid, int block, size_t smem,
                             cudaStream_t stream) {
-    if (p.hash_bits > 0) return launch((void (*)(SimParams))sim_kernel_hash(3, cached_index), grid, block, smem,
-                                       stream, p);
+    if (p.hash_bits > 0) return cudaErrorInvalidValue;  // the warp layout runs on the dense window table only
     return launch(cached_index ? mbg_sim_warp : mbg_sim_warp_gather, grid, block, smem, stream, p);
 }
 

@@ -1,6 +1,8 @@
-// The single-simulation kernels of sim_aot.cu compiled with their window sums going to the window
-// hash table (MBG_WINDOW_HASH, sim_core.cuh:bin_add) instead of the dense table. Same layouts,
-// same arithmetic; launched when a run's table is the hash table (large, sparse output spaces).
+// The lane-layout single-simulation kernels of sim_aot.cu compiled with their window sums going to
+// the window hash table (MBG_WINDOW_HASH, sim_core.cuh:bin_add) instead of the dense table. Same
+// layouts, same arithmetic; launched when a run's table is the hash table (large, sparse output
+// spaces). The warp layout has no such twin: on the GB300 its hash form stalled or mis-picked
+// whenever the table overflowed, so the warp layout keeps the dense table (see sim.cpp).
 #define MBG_WINDOW_HASH 1
 
 #include <cuda_runtime.h>
@@ -16,16 +18,6 @@
 #include "kernels.h"
 
 namespace mbg {
-
-extern "C" __global__ void __launch_bounds__(256, 4) mbg_sim_warp_hash(const SimParams p) {
-    extern __shared__ __align__(16) unsigned char smem[];
-    sim_warp_body<true>(p, smem);
-}
-
-extern "C" __global__ void __launch_bounds__(256, 4) mbg_sim_warp_gather_hash(const SimParams p) {
-    extern __shared__ __align__(16) unsigned char smem[];
-    sim_warp_body<false>(p, smem);
-}
 
 extern "C" __global__ void __launch_bounds__(256, 2) mbg_sim_lane_hash(const SimParams p) {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -60,8 +52,7 @@ const void* sim_kernel_hash(int kernel, bool variant) {
         case 6: return variant ? (const void*)mbg_sim_lane_global_full_hash : (const void*)mbg_sim_lane_global_hash;
         case 0: return variant ? (const void*)mbg_sim_lane_coop_hash : (const void*)mbg_sim_lane_hash;
         case 4: return variant ? (const void*)mbg_sim_lane_coop_full_hash : (const void*)mbg_sim_lane_full_hash;
-        case 3: return variant ? (const void*)mbg_sim_warp_hash : (const void*)mbg_sim_warp_gather_hash;
-        default: return nullptr;  // the batched kernels always use the dense tables
+        default: return nullptr;  // the warp layout and the batched kernels use the dense tables only
     }
 }
 

@@ -345,14 +345,25 @@ mbg_status mbg_sim_probtraj_sparse(mbg_sim* s, uint64_t* bins, uint64_t* sums, d
                                    size_t* count) {
     if (!s || !count) return fail(MBG_ERR_ARG, "null argument");
     return guard([&] {
-        s->sim.fetch();
-        const size_t n = s->sim.wbin.size();
+        mbg::Sim& sim = s->sim;
+        sim.fetch();
+        const size_t n = sim.wbin.size();
         *count = n;
         const size_t m = n < cap ? n : cap;
-        for (size_t e = 0; e < m; ++e) {
-            if (bins) bins[e] = s->sim.wbin[e];
-            if (sums) sums[e] = s->sim.wsum[e];
-            if (probs) probs[e] = mbg::window_prob(s->sim, s->sim.wsum[e]);
+        const uint32_t* wb = sim.wbin.data();
+        const uint64_t* ws = sim.wsum.data();
+        if (bins)
+            for (size_t e = 0; e < m; ++e) bins[e] = wb[e];
+        if (sums) std::memcpy(sums, ws, m * sizeof(uint64_t));
+        if (probs) {
+            // window_prob's arithmetic, in the same order (the dense read gives the same doubles)
+            const double n_traj = (double)sim.n_traj;
+            if (sim.cm.discrete) {
+                for (size_t e = 0; e < m; ++e) probs[e] = (double)ws[e] / n_traj;
+            } else {
+                const double denom = n_traj * sim.cm.tick;
+                for (size_t e = 0; e < m; ++e) probs[e] = ((double)ws[e] / 4294967296.0) / denom;
+            }
         }
     });
 }
@@ -361,7 +372,10 @@ mbg_status mbg_sim_final_states(mbg_sim* s, double* probs) {
     if (!s || !probs) return fail(MBG_ERR_ARG, "null argument");
     return guard([&] {
         s->sim.fetch();
-        for (size_t i = 0; i < s->sim.fin.size(); ++i) probs[i] = (double)s->sim.fin[i] / (double)s->sim.n_traj;
+        const double n = (double)s->sim.n_traj;
+        const uint32_t* f = s->sim.fin.data();
+        // most of 2^outputs states are never final: divide only the reached ones
+        for (size_t i = 0; i < s->sim.fin.size(); ++i) probs[i] = f[i] ? (double)f[i] / n : 0.0;
     });
 }
 

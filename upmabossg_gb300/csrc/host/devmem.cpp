@@ -4,6 +4,7 @@
 #include <cuda.h>  // driver types only: the two driver calls come through cudaGetDriverEntryPoint
 #include <cuda_runtime.h>
 
+#include <cstdlib>
 #include <map>
 #include <mutex>
 #include <string>
@@ -64,10 +65,18 @@ void* take_spare(const Key& k) {
     return p;
 }
 
+bool cache_enabled() {
+    static const bool on = [] {
+        const char* e = std::getenv("MBG_DEVICE_CACHE");
+        return !(e && e[0] == '0');
+    }();
+    return on;
+}
+
 void* alloc(size_t bytes, bool pinned, const char* what) {
     if (bytes == 0) bytes = 1;
     unsigned long long ctx = 0;
-    bool have = current_context_id(&ctx);
+    bool have = cache_enabled() && current_context_id(&ctx);
     if (have)
         if (void* p = take_spare(Key{ctx, bytes, pinned})) return p;
     void* p = nullptr;
@@ -77,7 +86,7 @@ void* alloc(size_t bytes, bool pinned, const char* what) {
         throw NoMemError(std::string(pinned ? "cudaMallocHost" : "cudaMalloc") + " of " + std::to_string(bytes) +
                          " bytes (" + what + "): " + cudaGetErrorString(e));
     }
-    if (!have) have = current_context_id(&ctx);  // the allocation may have created the context
+    if (!have && cache_enabled()) have = current_context_id(&ctx);  // the allocation may have created the context
     Cache& c = cache();
     std::lock_guard<std::mutex> lock(c.mu);
     c.live.emplace(p, Key{have ? ctx : 0ull, bytes, pinned});

@@ -6,7 +6,8 @@
 // synchronisation, after the first. At most kDevCacheBytes of device blocks and kPinnedCacheBytes
 // of pinned host blocks are kept; a block freed beyond that is released. Contexts are told apart
 // by their unique id, so a block of a context that no longer exists (cudaDeviceReset) is never
-// handed out again; without a context id nothing is cached.
+// handed out again; without a context id nothing is cached, nor with MBG_DEVICE_CACHE=0 in the
+// environment.
 #pragma once
 
 #include <cstddef>

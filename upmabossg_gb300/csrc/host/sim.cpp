@@ -9,6 +9,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -256,8 +257,13 @@ void Sim::choose_window_table() {
     // the device either way. So the dense table is used while it is affordable and the hash table
     // only beyond that, where it holds what a run reaches: every trajectory holds at least one
     // output state per window, so trajectories x windows estimates the reached bins.
+    // the warp layout runs on the dense table only (its hash-table form could stall the GPU when the
+    // table overflowed): a run that asks for it keeps the dense table at any size
+    const bool warp = opts.layout == MBG_LAYOUT_WARP;
+    if (warp && mode == 2)
+        throw ArgError("the warp layout uses the dense window table only (window_table = 1 or 0, or another layout)");
     const uint64_t est = std::min<uint64_t>(n_bins, n_traj * (uint64_t)cm.windows);
-    const bool hash = mode == 2 || (mode == 0 && hash_ok && n_bins * 8 > kDenseWindowMaxBytes);
+    const bool hash = mode == 2 || (mode == 0 && !warp && hash_ok && n_bins * 8 > kDenseWindowMaxBytes);
     int bits = 0;
     if (hash) {
         bits = std::min(kDefaultHashBits, std::max(10, ceil_log2_u64(2 * est)));
@@ -410,7 +416,8 @@ void Sim::create(const CompiledModel& model, const std::vector<std::string>& nod
         }
         setup_layout(o.layout, blk, o.lane_update != 1);
     } else if (o.thread_cutoff > 0) {
-        const int lay = cm.words <= 16 && cm.n <= o.thread_cutoff ? MBG_LAYOUT_THREAD : MBG_LAYOUT_WARP;
+        const int big = hash_bits > 0 ? MBG_LAYOUT_LANE_GLOBAL : MBG_LAYOUT_WARP;  // warp: dense table only
+        const int lay = cm.words <= 16 && cm.n <= o.thread_cutoff ? MBG_LAYOUT_THREAD : big;
         setup_layout(lay, o.block_size > 0 ? o.block_size : 256);
     } else {
         autotune();
@@ -425,7 +432,7 @@ struct Shape {
     int layout, block;
     bool coop;
 };
-std::map<std::tuple<int, int, int>, Shape> g_tuned;
+std::map<std::tuple<int, int, int, int>, Shape> g_tuned;
 
 int ceil_log2(uint64_t x) {
     int c = 0;
@@ -436,7 +443,7 @@ int ceil_log2(uint64_t x) {
 // Tuned shapes also persist on disk, one line per (GPU, library build, class), so that a new
 // process (a command-line run, say) finds them without timing the pilots again. A line from
 // another GPU model or another build of the library never matches.
-std::string tune_key(int device, const std::tuple<int, int, int>& cls) {
+std::string tune_key(int device, const std::tuple<int, int, int, int>& cls) {
     cudaDeviceProp prop{};
     if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) return std::string();
     std::string name = prop.name;
@@ -444,7 +451,7 @@ std::string tune_key(int device, const std::tuple<int, int, int>& cls) {
         if (c == ' ' || c == '|') c = '_';
     return name + "|" + std::to_string(prop.multiProcessorCount) + "|" + __DATE__ + "_" + __TIME__ + "|" +
            std::to_string(std::get<0>(cls)) + "|" + std::to_string(std::get<1>(cls)) + "|" +
-           std::to_string(std::get<2>(cls));
+           std::to_string(std::get<2>(cls)) + "|" + std::to_string(std::get<3>(cls));
 }
 
 std::string tune_path() { return cache_dir() + "/autotune_v1.txt"; }
@@ -475,8 +482,10 @@ void Sim::autotune() {
     // the pilot is large enough to fill the GPU in every layout (or the whole run when smaller),
     // so that the choice reflects occupancy as well as per-transition cost
     const uint64_t pilot = std::min<uint64_t>(n_traj, 1u << 17);
-    // the lane layout has no redraw_period: such runs are tuned (and cached) apart
-    const std::tuple<int, int, int> cls{ceil_log2((uint64_t)cm.n), ceil_log2(pilot), opts.redraw_period ? 1 : 0};
+    // the lane layout has no redraw_period and the warp layout no window hash table: such runs are
+    // tuned (and cached) apart
+    const std::tuple<int, int, int, int> cls{ceil_log2((uint64_t)cm.n), ceil_log2(pilot), opts.redraw_period ? 1 : 0,
+                                             hash_bits > 0 ? 1 : 0};
     const std::string key = tune_key(device, cls);
     {
         std::lock_guard<std::mutex> lock(g_tune_mu);
@@ -507,6 +516,7 @@ void Sim::autotune() {
                 if (opts.block_size > 0 && blk != opts.block_size) continue;
                 if (lay != MBG_LAYOUT_LANE && (blk == 64 || coop)) continue;
                 if (lay == MBG_LAYOUT_LANE_GLOBAL && opts.redraw_period) continue;
+                if (lay == MBG_LAYOUT_WARP && hash_bits > 0) continue;  // dense window table only
                 if (lay == MBG_LAYOUT_THREAD && cm.words > 16) continue;
                 if (lay == MBG_LAYOUT_LANE && (opts.redraw_period || sim_lane_smem(cm.n, blk) > 227 * 1024)) continue;
                 try {
@@ -648,7 +658,9 @@ void Sim::run(cudaStream_t stream) {
     // stay in the current table until then)
     if (hash_bits > 0 && 2 * summary.window_entries > (1ull << hash_bits))
         pending_hash_bits = std::max(hash_bits + 1, ceil_log2_u64(2 * summary.window_entries));
-    if (opts.window_table == 0 && opts.window_hash_bits == 0) {
+    // the table that held, for the next automatic choice of this model shape (not a dense table the
+    // warp layout kept regardless)
+    if (opts.window_table == 0 && opts.window_hash_bits == 0 && opts.layout != MBG_LAYOUT_WARP) {
         std::lock_guard<std::mutex> lock(g_window_mu);
         g_window_bits[window_class(cm, n_traj)] = pending_hash_bits > 0 ? pending_hash_bits : hash_bits;
     }
@@ -736,12 +748,23 @@ void Sim::launch(cudaStream_t stream) {
 void Sim::fetch() {
     if (!ran) throw StateError("results requested before mbg_sim_run");
     if (fetched) return;
+    // MBG_FETCH_LOG=1: the host time of each read-back phase on stderr
+    static const bool log = std::getenv("MBG_FETCH_LOG") != nullptr;
+    auto t_last = std::chrono::steady_clock::now();
+    auto phase = [&](const char* what) {
+        if (!log) return;
+        const auto now = std::chrono::steady_clock::now();
+        std::fprintf(stderr, "mbg fetch: %s %.3f ms\n", what,
+                     std::chrono::duration<double, std::milli>(now - t_last).count());
+        t_last = now;
+    };
     ck(cudaSetDevice(device), "cudaSetDevice");
     const uint64_t S = 1ull << cm.n_out;
     th.resize(cm.windows);
     fin.resize(S);
     ck(cudaMemcpy(th.data(), prm.th_hist, th.size() * 8, cudaMemcpyDeviceToHost), "cudaMemcpy D2H");
     ck(cudaMemcpy(fin.data(), prm.final_hist, fin.size() * 4, cudaMemcpyDeviceToHost), "cudaMemcpy D2H");
+    phase("transition entropy and final states");
     // window sums: the non-zero bins in increasing order
     wbin.clear();
     wsum.clear();
@@ -768,6 +791,7 @@ void Sim::fetch() {
            "window compaction (count)");
         unsigned long long total = 0;
         ck(cudaMemcpy(&total, wc_total, 8, cudaMemcpyDeviceToHost), "cudaMemcpy D2H");
+        phase("window compaction: count");
         if (total > wc_cap) {
             free_now(wc_bin);
             free_now(wc_sum);
@@ -788,9 +812,14 @@ void Sim::fetch() {
             ck(cudaMemcpy(wsum.data(), wc_sum, total * 8, cudaMemcpyDeviceToHost), "cudaMemcpy D2H");
         }
     }
+    phase("window bins and sums");
+    // first entry of every window: the bins are in increasing order, window w starts at w * 2^n_out
     wstart.assign((size_t)cm.windows + 1, 0);
-    for (uint32_t b : wbin) ++wstart[(b >> cm.n_out) + 1];
-    for (int w = 0; w < cm.windows; ++w) wstart[w + 1] += wstart[w];
+    for (int w = 1; w <= cm.windows; ++w)
+        wstart[w] = (size_t)(std::lower_bound(wbin.begin(), wbin.end(), (uint64_t)w << cm.n_out,
+                                              [](uint32_t b, uint64_t v) { return (uint64_t)b < v; }) -
+                             wbin.begin());
+    phase("window index");
     // fixed points: representatives, counts, then their states
     const uint32_t nu = (uint32_t)summary.fixed_point_states;
     std::vector<uint32_t> words((size_t)nu * cm.words), cnt(nu);
@@ -812,6 +841,7 @@ void Sim::fetch() {
             if (a.words[w] != b.words[w]) return a.words[w] < b.words[w];
         return false;
     });
+    phase("fixed points");
     fetched = true;
 }
 
