@@ -6,6 +6,10 @@
 // is the same function and needs no special case here: every node is tabulated over its
 // regulators instead of being emitted as source text.
 #include <algorithm>
+#include <thread>
+#include <mutex>
+#include <exception>
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <set>
@@ -654,6 +658,42 @@ CompiledModel compile_arrays(int n, const int32_t* reg_off, const int32_t* regs,
     return cm;
 }
 
+namespace {
+
+// f(i, scratch) for every node i in [0, n) on up to 16 host threads (one thread for small models),
+// each thread with its own value-initialised Scratch. An exception in f is rethrown here: the one of
+// the lowest-numbered node when several nodes fail, as a single thread would have thrown it.
+template <class Scratch, class F>
+void parallel_nodes(int n, F&& f) {
+    const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+    const int threads = n < 256 ? 1 : (int)std::min<unsigned>(hw, 16u);
+    std::atomic<int> next{0};
+    std::mutex mu;
+    int err_node = n;
+    std::exception_ptr err;
+    auto worker = [&]() {
+        Scratch sc{};
+        for (int i; (i = next.fetch_add(1)) < n;) {
+            try {
+                f(i, sc);
+            } catch (...) {
+                std::lock_guard<std::mutex> lock(mu);
+                if (i < err_node) {
+                    err_node = i;
+                    err = std::current_exception();
+                }
+            }
+        }
+    };
+    std::vector<std::thread> pool;
+    for (int t = 1; t < threads; ++t) pool.emplace_back(worker);
+    worker();
+    for (auto& th : pool) th.join();
+    if (err) std::rethrow_exception(err);
+}
+
+}  // namespace
+
 CompiledModel compile_model(const Model& m) {
     CompiledModel cm;
     cm.n = (int)m.nodes.size();
@@ -670,41 +710,42 @@ CompiledModel compile_model(const Model& m) {
     }
     cm.n_out = (int)cm.out_nodes.size();
 
-    // Tabulate every node's rate over (self, regulators) in double.
+    // Tabulate every node's rate over (self, regulators) in double, nodes spread over host threads
+    // (a node with 20 regulators alone is 2^21 entries); each node's result depends on it alone.
     std::vector<std::vector<double>> tabs(cm.n);
-    double sum_max = 0;
-    // scratch reused from node to node
-    std::vector<int> sup, inputs;
-    std::vector<Instr> pu, pd;
-    std::vector<double> stack;
-    std::vector<Slot> slots;
-    for (int i = 0; i < cm.n; ++i) {
+    std::vector<double> node_max(cm.n, 0.0);
+    struct Scratch {
+        std::vector<int> sup, inputs;
+        std::vector<Instr> pu, pd;
+        std::vector<double> stack;
+        std::vector<Slot> slots;
+    };
+    auto tabulate = [&](int i, Scratch& sc) {
         const Node& nd = m.nodes[i];
         const Expr* up = nd.attr("rate_up");
         const Expr* down = nd.attr("rate_down");
         if (!up || !down) throw Error("Node " + nd.name + " lacks rate_up or rate_down");
-        sup.clear();
-        collect_support(*up, m, i, sup);
-        collect_support(*down, m, i, sup);
-        std::sort(sup.begin(), sup.end());
-        sup.erase(std::unique(sup.begin(), sup.end()), sup.end());
+        sc.sup.clear();
+        collect_support(*up, m, i, sc.sup);
+        collect_support(*down, m, i, sc.sup);
+        std::sort(sc.sup.begin(), sc.sup.end());
+        sc.sup.erase(std::unique(sc.sup.begin(), sc.sup.end()), sc.sup.end());
         CompiledNode& cn = cm.nodes[i];
-        for (int s : sup)
+        for (int s : sc.sup)
             if (s != i) cn.regs.push_back(s);
         const int k = (int)cn.regs.size();
         if (k > kMaxBinaryRegs)
             throw Error("node " + nd.name + " reads " + std::to_string(k) + " nodes (limit " +
                         std::to_string(kMaxBinaryRegs) + ")");
-        cm.max_k = std::max(cm.max_k, k);
-        inputs.assign(cn.regs.begin(), cn.regs.end());
-        inputs.push_back(i);  // input bit k is the node itself
-        pu.clear();
-        pd.clear();
-        flatten(*up, m, i, inputs, pu, 0);
-        flatten(*down, m, i, inputs, pd, 0);
-        const size_t depth = std::max(stack_depth(pu), stack_depth(pd)) + 1;
-        stack.assign(kBlock * depth, 0.0);
-        slots.assign(depth, Slot{});
+        sc.inputs.assign(cn.regs.begin(), cn.regs.end());
+        sc.inputs.push_back(i);  // input bit k is the node itself
+        sc.pu.clear();
+        sc.pd.clear();
+        flatten(*up, m, i, sc.inputs, sc.pu, 0);
+        flatten(*down, m, i, sc.inputs, sc.pd, 0);
+        const size_t depth = std::max(stack_depth(sc.pu), stack_depth(sc.pd)) + 1;
+        sc.stack.assign(kBlock * depth, 0.0);
+        sc.slots.assign(depth, Slot{});
         const uint64_t half = 1ull << k, total = half << 1;
         std::vector<double>& tab = tabs[i];
         tab.assign(std::max<uint64_t>(total, kBlock), 0.0);
@@ -716,12 +757,12 @@ CompiledModel compile_model(const Model& m) {
             const uint64_t n_here = std::min<uint64_t>(kBlock, total - a0);
             const bool any_up = a0 < half, any_down = a0 + n_here > half;
             if (any_up) {
-                run_block_bits(pu, a0, stack, slots, buf);
+                run_block_bits(sc.pu, a0, sc.stack, sc.slots, buf);
                 for (uint64_t t = 0; t < n_here; ++t)
                     if (!(((a0 + t) >> k) & 1u)) tab[a0 + t] = buf[t];
             }
             if (any_down) {
-                run_block_bits(pd, a0, stack, slots, buf);
+                run_block_bits(sc.pd, a0, sc.stack, sc.slots, buf);
                 for (uint64_t t = 0; t < n_here; ++t)
                     if (((a0 + t) >> k) & 1u) tab[a0 + t] = buf[t];
             }
@@ -733,13 +774,19 @@ CompiledModel compile_model(const Model& m) {
                 throw Error("node " + nd.name + " has a negative or non-finite rate");
             mx = std::max(mx, r);
         }
-        sum_max += mx;
+        node_max[i] = mx;
+    };
+    parallel_nodes<Scratch>(cm.n, [&](int i, Scratch& sc) { tabulate(i, sc); });
+    double sum_max = 0;
+    for (int i = 0; i < cm.n; ++i) {
+        sum_max += node_max[i];  // node order, as one thread would add them
+        cm.max_k = std::max(cm.max_k, (int)cm.nodes[i].regs.size());
     }
 
     const int fb = frac_bits_for(sum_max);
     cm.frac_bits = fb;
 
-    for (int i = 0; i < cm.n; ++i) classify_node(cm.nodes[i], tabs[i], fb, m.nodes[i].name);
+    parallel_nodes<int>(cm.n, [&](int i, int&) { classify_node(cm.nodes[i], tabs[i], fb, m.nodes[i].name); });
 
     cm.deps.assign(cm.n, {});
     for (int i = 0; i < cm.n; ++i) {
