@@ -146,15 +146,16 @@ typedef struct {
  * (src/parser/driver.cpp:16-31). Node i reads regs[reg_off[i] .. reg_off[i + 1]) (n + 1 offsets,
  * reg_off[0] = 0; distinct node indices other than i, in any order, at most 24); its logic over
  * them is bit idx = sum_j state(regs[reg_off[i] + j]) << j of the words starting at
- * logic[logic_off[i]] (2^k bits for k regulators). The node turns on at rate_up[i] while it is off
+ * logic[logic_off[i]] (2^k bits for k regulators; every table must lie within the logic_words
+ * words of `logic`). The node turns on at rate_up[i] while it is off
  * and its logic is 1, and off at rate_down[i] while it is on and its logic is 0: MaBoSS's
  * `rate_up = @logic ? u : 0; rate_down = @logic ? 0 : d;` (generator.cpp:84-122), compiled
  * exactly as that .bnd text would be. istate[i] in [0, 1]; is_output (NULL: every node) marks the
  * non-internal nodes; names (NULL: "N0", "N1", ...) must be distinct and non-empty. */
 mbg_status mbg_model_from_arrays(int32_t n, const char* const* names, const int32_t* reg_off, const int32_t* regs,
-                                 const uint32_t* logic, const int64_t* logic_off, const double* rate_up,
-                                 const double* rate_down, const double* istate, const uint8_t* is_output,
-                                 const mbg_model_run* run, mbg_model** out);
+                                 const uint32_t* logic, int64_t logic_words, const int64_t* logic_off,
+                                 const double* rate_up, const double* rate_down, const double* istate,
+                                 const uint8_t* is_output, const mbg_model_run* run, mbg_model** out);
 void mbg_model_destroy(mbg_model* m);
 mbg_status mbg_model_info_get(const mbg_model* m, mbg_model_info* out);
 const char* mbg_model_node_name(const mbg_model* m, int32_t i);

@@ -105,3 +105,25 @@ def test_arrays_simulate_like_text(seed):
     fb, pb = b.fixed_points()
     assert np.array_equal(fa, fb) and np.array_equal(pa, pb)
     assert a.summary()["transitions"] == b.summary()["transitions"]
+
+
+def test_truth_table_outside_the_logic_array_is_refused():
+    """The C entry point checks every node's table against the length of `logic` it is given."""
+    import ctypes
+    from upmabossg_gb300 import lib, ModelRun
+    reg_off = np.array([0, 1, 2], np.int32)
+    regs = np.array([1, 0], np.int32)
+    logic = np.array([0b10, 0b01], np.uint32)
+    up, down, ist = (np.ones(2), np.ones(2), np.full(2, 0.5))
+    run = ModelRun(10.0, 0.5, 100, 0, 0, 0)
+    p = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+    for words, offs in ((2, [0, 1]), (1, [0, 1]), (2, [0, -1])):
+        h = ctypes.c_void_p()
+        off = np.array(offs, np.int64)  # held for the call
+        st = lib().mbg_model_from_arrays(2, None, p(reg_off), p(regs), p(logic), words, p(off), p(up), p(down),
+                                         p(ist), None, ctypes.byref(run), ctypes.byref(h))
+        if words == 2 and offs == [0, 1]:
+            assert st == 0
+            lib().mbg_model_destroy(h)
+        else:
+            assert st != 0 and not h.value

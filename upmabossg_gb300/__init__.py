@@ -118,8 +118,9 @@ def lib():
             "mbg_device_count": (ctypes.c_int, []),
             "mbg_model_parse_files": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_char_p, ctypes.POINTER(vp)]),
             "mbg_model_parse_strings": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_char_p, ctypes.POINTER(vp)]),
-            "mbg_model_from_arrays": (ctypes.c_int, [i32, ctypes.POINTER(ctypes.c_char_p), vp, vp, vp, vp, vp, vp,
-                                                     vp, vp, ctypes.POINTER(ModelRun), ctypes.POINTER(vp)]),
+            "mbg_model_from_arrays": (ctypes.c_int, [i32, ctypes.POINTER(ctypes.c_char_p), vp, vp, vp, ctypes.c_int64,
+                                                     vp, vp, vp, vp, vp, ctypes.POINTER(ModelRun),
+                                                     ctypes.POINTER(vp)]),
             "mbg_model_parse_files_overrides": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p,
                                                                ctypes.POINTER(vp)]),
             "mbg_model_with_mutations": (ctypes.c_int, [vp, dp, dp, i32, ctypes.POINTER(vp)]),
@@ -274,8 +275,8 @@ class Model:
             cnames = (ctypes.c_char_p * n)(*[s.encode() for s in names])
         run = ModelRun(max_time, time_tick, sample_count, seed, 1 if discrete else 0, 0)
         h = ctypes.c_void_p()
-        _check(lib().mbg_model_from_arrays(n, cnames, _p(reg_off), _p(regs), _p(logic_w), _p(logic_off), _p(up),
-                                           _p(down), _p(ist), _p(outs), ctypes.byref(run), ctypes.byref(h)))
+        _check(lib().mbg_model_from_arrays(n, cnames, _p(reg_off), _p(regs), _p(logic_w), logic_w.size, _p(logic_off),
+                                           _p(up), _p(down), _p(ist), _p(outs), ctypes.byref(run), ctypes.byref(h)))
         return cls(h)
 
     def rate(self, node: int, state) -> tuple:

@@ -143,9 +143,9 @@ mbg_status mbg_model_parse_strings(const char* bnd_text, const char* cfg_text, m
 void mbg_model_destroy(mbg_model* m) { delete m; }
 
 mbg_status mbg_model_from_arrays(int32_t n, const char* const* names, const int32_t* reg_off, const int32_t* regs,
-                                 const uint32_t* logic, const int64_t* logic_off, const double* rate_up,
-                                 const double* rate_down, const double* istate, const uint8_t* is_output,
-                                 const mbg_model_run* run, mbg_model** out) {
+                                 const uint32_t* logic, int64_t logic_words, const int64_t* logic_off,
+                                 const double* rate_up, const double* rate_down, const double* istate,
+                                 const uint8_t* is_output, const mbg_model_run* run, mbg_model** out) {
     if (!out) return fail(MBG_ERR_ARG, "null output pointer");
     *out = nullptr;
     if (!run) return fail(MBG_ERR_ARG, "null run constants");
@@ -169,7 +169,8 @@ mbg_status mbg_model_from_arrays(int32_t n, const char* const* names, const int3
         rc.seed = run->seed;
         rc.discrete = run->discrete_time != 0;
         try {
-            m->cm = mbg::compile_arrays(n, reg_off, regs, logic, logic_off, rate_up, rate_down, istate, is_output, rc);
+            m->cm = mbg::compile_arrays(n, reg_off, regs, logic, logic_words, logic_off, rate_up, rate_down, istate,
+                                        is_output, rc);
         } catch (const mbg::Error& e) {
             throw mbg::ModelError(e.what());
         }

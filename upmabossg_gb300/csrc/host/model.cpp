@@ -558,8 +558,9 @@ CompiledModel rescale_model(const CompiledModel& src, const double* up_scale, co
 }
 
 CompiledModel compile_arrays(int n, const int32_t* reg_off, const int32_t* regs, const uint32_t* logic,
-                             const int64_t* logic_off, const double* rate_up, const double* rate_down,
-                             const double* istate, const uint8_t* is_output, const RunConstants& rc) {
+                             int64_t logic_words, const int64_t* logic_off, const double* rate_up,
+                             const double* rate_down, const double* istate, const uint8_t* is_output,
+                             const RunConstants& rc) {
     if (n < 1) throw Error("model has no nodes");
     if (n > kMaxNodes) throw Error("model has more than 65535 nodes");
     if (!reg_off || !logic || !logic_off || !rate_up || !rate_down || !istate)
@@ -603,6 +604,9 @@ CompiledModel compile_arrays(int n, const int32_t* reg_off, const int32_t* regs,
         for (auto& o : order) cn.regs.push_back(o.first);
         cm.max_k = std::max(cm.max_k, k);
         const uint64_t half = 1ull << k, total = half << 1;
+        const int64_t words = (int64_t)((half + 31) / 32);
+        if (logic_off[i] < 0 || logic_off[i] > logic_words - words)
+            throw Error("node " + name + ": its truth table lies outside the logic array");
         cn.kind = NODE_BINARY;
         cn.up_real = up;
         cn.down_real = down;

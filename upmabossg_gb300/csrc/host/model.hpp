@@ -136,13 +136,15 @@ struct RunConstants {
 };
 // A model given by arrays instead of text. Node i reads regs[reg_off[i] .. reg_off[i + 1])
 // (distinct node indices other than i, in any order); its logic over them is bit
-// idx = sum_j state(regs[reg_off[i] + j]) << j of the words logic[logic_off[i] ..]; it turns on at
+// idx = sum_j state(regs[reg_off[i] + j]) << j of the words logic[logic_off[i] ..] (within the
+// logic_words words of `logic`); it turns on at
 // rate_up[i] while off with logic 1 and off at rate_down[i] while on with logic 0 (the MaBoSS
 // form `rate_up = @logic ? u : 0; rate_down = @logic ? 0 : d;`, which compile_model tabulates
 // the same way); istate[i] in [0, 1]; an output iff is_output[i] (null: every node). The
 // fixed-point scale and quantisation follow compile_model's rule. Throws Error on bad input.
 CompiledModel compile_arrays(int n, const int32_t* reg_off, const int32_t* regs, const uint32_t* logic,
-                             const int64_t* logic_off, const double* rate_up, const double* rate_down,
-                             const double* istate, const uint8_t* is_output, const RunConstants& rc);
+                             int64_t logic_words, const int64_t* logic_off, const double* rate_up,
+                             const double* rate_down, const double* istate, const uint8_t* is_output,
+                             const RunConstants& rc);
 
 }  // namespace mbg
