@@ -415,7 +415,7 @@ m = mbg.Model.from_strings(bnd, cfg)
 s = mbg.Simulation(m, n_traj={n}, traj_base={base}, device={dev}, **{kw!r})
 s.run()
 bins, sums, probs = s.probtraj_sparse()
-th = s.tr_entropy(); f = s.final_states(); fs, fp = s.fixed_points()
+th = s.tr_entropy(); fst, fpr = s.final_states_sparse(); fs, fp = s.fixed_points()
 t2 = time.perf_counter()
 print(json.dumps({{"ms": (t2 - t1) * 1e3, "import_ms": (t1 - t0) * 1e3, "transitions": s.summary()["transitions"]}}))
 """
@@ -504,16 +504,17 @@ def run_ours(args):
         s2.run()
         bins, sums, probs = s2.probtraj_sparse()
         TH = s2.tr_entropy()
-        F = s2.final_states()
+        fst, fpr = s2.final_states_sparse()
         fs, fp = s2.fixed_points()
         torch.cuda.synchronize()
         dt = time.perf_counter() - t1
         if i > 0:
             e2e_ms.append(dt * 1e3)
         # model text in (the model tables are built and uploaded by mbg_sim_create); out: the
-        # reached window bins (u32 bin + u64 sum each), TH sums, u32 final counts, fixed points
+        # reached window bins (u32 bin + u64 sum each), TH sums, the reached final states (u32
+        # state + u32 count each), fixed points
         h2d = len(bnd) + len(cfg)
-        d2h = bins.size * 12 + TH.size * 8 + F.size * 4 + fs.nbytes + fp.size * 4
+        d2h = bins.size * 12 + TH.size * 8 + fst.size * 8 + fs.nbytes + fp.size * 4
         s2.close()
         m2.close()
     e2e_step_ms = statistics.mean(e2e_ms)

@@ -216,6 +216,11 @@ mbg_status mbg_sim_probtraj_sparse(mbg_sim* s, uint64_t* bins, uint64_t* sums, d
                                    size_t* count);
 /* 2^outputs final-state probabilities. */
 mbg_status mbg_sim_final_states(mbg_sim* s, double* probs);
+/* The reached final output states only, in increasing order, with their probabilities: `cap`
+ * entries at most, `*count` gets their number (states or probs may be NULL). Large output spaces
+ * are compacted on the device, so only the reached states leave it. The reference copies the
+ * dense count array back and prints its non-zero entries (src/statistics/final_states.cpp:45-66). */
+mbg_status mbg_sim_final_states_sparse(mbg_sim* s, uint64_t* states, double* probs, size_t cap, size_t* count);
 /* Distinct fixed points in reference order (highest state word first): states (n x words),
  * probabilities; `cap` entries at most, `*count` gets the total. */
 mbg_status mbg_sim_fixed_points(mbg_sim* s, uint32_t* states, double* probs, size_t cap, size_t* count);

@@ -4,7 +4,8 @@ The two tables hold the same integer sums, so every comparison here is exact: th
 and their sums, the transition entropy, the CSV and stdout reports. Covered: every layout that
 runs on the hash table (the warp layout keeps the dense table), the discrete-time counts, a table
 too small for the run (grown and re-run until it holds), the automatic choice on the 20-output
-and 10-output workloads, and the sparse read-back against the dense one.
+and 10-output workloads, and the sparse read-backs (window bins, final states) against the dense
+ones.
 """
 import os
 
@@ -150,6 +151,26 @@ def test_sparse_read_equals_dense_read():
     assert np.array_equal(nz.astype(np.uint64), bins)
     assert np.array_equal(raw.ravel()[nz], sums)
     assert np.array_equal(probs.ravel()[nz], p)
+
+
+@pytest.mark.parametrize("workload", ["medium", "small", "wide"])
+def test_sparse_final_states_equal_dense(workload):
+    """10 outputs (counts read whole and compacted on the host), 20 and 24 outputs (compacted on
+    the device)."""
+    if workload == "wide":
+        bnd, cfg = wide_output_network()
+    else:
+        net = getattr(synth, workload)()
+        bnd, cfg = net.bnd(), net.cfg()
+    model, sim = simulate(bnd, cfg, 4000, 0)
+    states, probs = sim.final_states_sparse()
+    F = sim.final_states()
+    assert F.size == 1 << model.info.outputs
+    nz = np.flatnonzero(F)
+    assert np.array_equal(nz.astype(np.uint64), states)
+    assert np.array_equal(F[nz], probs)
+    counts = np.rint(probs * 4000)
+    assert np.array_equal(counts / 4000, probs) and counts.sum() == 4000
 
 
 def test_reports_identical(tmp_path):

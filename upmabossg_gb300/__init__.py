@@ -26,7 +26,8 @@ EXPORTS = (
     "mbg_model_with_rate_scales", "mbg_model_parse_files_overrides", "mbg_model_with_mutations",
     "mbg_model_jit_check", "mbg_model_layout_check", "mbg_model_from_arrays",
     "mbg_sim_opts_default", "mbg_sim_create", "mbg_sim_destroy", "mbg_sim_run", "mbg_sim_summary",
-    "mbg_sim_probtraj", "mbg_sim_probtraj_raw", "mbg_sim_probtraj_sparse", "mbg_sim_final_states", "mbg_sim_fixed_points",
+    "mbg_sim_probtraj", "mbg_sim_probtraj_raw", "mbg_sim_probtraj_sparse", "mbg_sim_final_states",
+    "mbg_sim_final_states_sparse", "mbg_sim_fixed_points",
     "mbg_sim_trajectories", "mbg_write_probtraj_csv", "mbg_write_fp_csv", "mbg_print_results",
     "mbg_write_final_states_csv", "mbg_fixed_points_aggregate_noalloc",
     "mbg_batch_opts_default", "mbg_batch_create", "mbg_batch_destroy", "mbg_batch_run", "mbg_batch_summary",
@@ -143,6 +144,8 @@ def lib():
             "mbg_sim_probtraj_sparse": (ctypes.c_int, [vp, dp, dp, dp, ctypes.c_size_t,
                                                         ctypes.POINTER(ctypes.c_size_t)]),
             "mbg_sim_final_states": (ctypes.c_int, [vp, dp]),
+            "mbg_sim_final_states_sparse": (ctypes.c_int, [vp, dp, dp, ctypes.c_size_t,
+                                                            ctypes.POINTER(ctypes.c_size_t)]),
             "mbg_sim_fixed_points": (ctypes.c_int, [vp, dp, dp, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]),
             "mbg_sim_trajectories": (ctypes.c_int, [vp, dp, dp, dp, dp]),
             "mbg_write_probtraj_csv": (ctypes.c_int, [vp, ctypes.c_char_p]),
@@ -413,6 +416,15 @@ class Simulation:
         F = np.empty(1 << self.model.info.outputs, np.float64)  # every entry is written
         _check(lib().mbg_sim_final_states(self._h, _p(F)))
         return F
+
+    def final_states_sparse(self):
+        """The reached final output states only: (states, probabilities), states increasing."""
+        n = ctypes.c_size_t()
+        _check(lib().mbg_sim_final_states_sparse(self._h, None, None, 0, ctypes.byref(n)))
+        states = np.empty(n.value, np.uint64)  # every entry is written
+        probs = np.empty(n.value, np.float64)
+        _check(lib().mbg_sim_final_states_sparse(self._h, _p(states), _p(probs), n.value, ctypes.byref(n)))
+        return states, probs
 
     def fixed_points(self):
         n = ctypes.c_size_t()

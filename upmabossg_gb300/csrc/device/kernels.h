@@ -72,5 +72,14 @@ cudaError_t launch_window_emit(const unsigned long long* hist, const unsigned lo
                                unsigned long long n_bins, const unsigned* bitmap, const unsigned* wpre,
                                const unsigned* chunk, unsigned* out_bin, unsigned long long* out_sum, int sms,
                                cudaStream_t stream);
+// The same two passes over the dense 2^n_out final-state counts (n_states entries): out_state /
+// out_count get the reached output states in increasing order and their counts. The scratch
+// arrays are those of the window compaction, sized for n_states or more.
+cudaError_t launch_final_count(const unsigned* counts, unsigned long long n_states, unsigned* bitmap,
+                               unsigned* wpre, unsigned* chunk, unsigned long long* total, int sms,
+                               cudaStream_t stream);
+cudaError_t launch_final_emit(const unsigned* counts, unsigned long long n_states, const unsigned* bitmap,
+                              const unsigned* wpre, const unsigned* chunk, unsigned* out_state, unsigned* out_count,
+                              int sms, cudaStream_t stream);
 
 }  // namespace mbg

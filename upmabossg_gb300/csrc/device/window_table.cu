@@ -1,6 +1,7 @@
 // Compaction of the window sums for read-back: the non-zero (window, output state) bins of a
 // simulation in increasing bin order, as (bin, sum) pairs, from either the dense windows x 2^n_out
-// table or the window hash table (SimParams::hslots).
+// table or the window hash table (SimParams::hslots). The same passes compact the 2^n_out
+// final-state counts into (output state, count) pairs.
 //
 // The reference reads its dense windows x 2^n_out float table back whole and walks it on the host
 // (src/statistics/window_average_small.cpp:99-140, 181-250). Here a bitmap over all bins marks the
@@ -39,10 +40,11 @@ __global__ void win_mark_hash(const unsigned long long* __restrict__ slots, unsi
     }
 }
 
-// Dense table: warp w builds bitmap words 32w .. 32w + 31, one ballot per word over 32 coalesced
-// sums (no atomics: every word has one writer).
-__global__ void win_mark_dense(const unsigned long long* __restrict__ hist, unsigned long long n_bins,
-                               unsigned long long n_words, unsigned* __restrict__ bitmap) {
+// Dense table (u64 window sums or u32 final-state counts): warp w builds bitmap words 32w .. 32w + 31,
+// one ballot per word over 32 coalesced entries (no atomics: every word has one writer).
+template <typename T>
+__global__ void win_mark_dense(const T* __restrict__ hist, unsigned long long n_bins, unsigned long long n_words,
+                               unsigned* __restrict__ bitmap) {
     const unsigned lane = threadIdx.x & 31u;
     const unsigned long long warps = (unsigned long long)gridDim.x * blockDim.x / 32;
     for (unsigned long long g = (blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x) / 32; g * 32 < n_words;
@@ -51,7 +53,7 @@ __global__ void win_mark_dense(const unsigned long long* __restrict__ hist, unsi
         for (unsigned k = 0; k < 32; ++k) {
             const unsigned long long word = g * 32 + k;
             const unsigned long long bin = word * 32 + lane;
-            const bool set = word < n_words && bin < n_bins && hist[bin] != 0ull;
+            const bool set = word < n_words && bin < n_bins && hist[bin] != T(0);
             const unsigned b = __ballot_sync(0xffffffffu, set);
             if (lane == k) mine = b;
         }
@@ -148,10 +150,11 @@ __global__ void win_emit_hash(const unsigned long long* __restrict__ slots, unsi
     }
 }
 
-__global__ void win_emit_dense(const unsigned long long* __restrict__ hist, unsigned long long n_words,
+template <typename T>
+__global__ void win_emit_dense(const T* __restrict__ hist, unsigned long long n_words,
                                const unsigned* __restrict__ bitmap, const unsigned* __restrict__ wpre,
                                const unsigned* __restrict__ chunk, unsigned* __restrict__ out_bin,
-                               unsigned long long* __restrict__ out_sum) {
+                               T* __restrict__ out_sum) {
     for (unsigned long long word = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; word < n_words;
          word += (unsigned long long)gridDim.x * blockDim.x) {
         unsigned bits = bitmap[word];
@@ -175,9 +178,12 @@ unsigned window_chunks(unsigned long long n_bins) {
     return (unsigned)((window_bitmap_words(n_bins) + kChunkWords - 1) / kChunkWords);
 }
 
-cudaError_t launch_window_count(const unsigned long long* hist, const unsigned long long* hslots, int hash_bits,
-                                unsigned long long n_bins, unsigned* bitmap, unsigned* wpre, unsigned* chunk,
-                                unsigned long long* total, int sms, cudaStream_t stream) {
+namespace {
+
+// The marking kernel of one table, then the two scans that rank its marked entries.
+template <typename Mark>
+cudaError_t count_marked(unsigned long long n_bins, unsigned* bitmap, unsigned* wpre, unsigned* chunk,
+                         unsigned long long* total, int sms, cudaStream_t stream, Mark mark) {
     const unsigned long long n_words = window_bitmap_words(n_bins);
     const unsigned n_chunks = window_chunks(n_bins);
     cudaError_t e = cudaMemsetAsync(bitmap, 0, n_words * 4, stream);
@@ -186,10 +192,7 @@ cudaError_t launch_window_count(const unsigned long long* hist, const unsigned l
     cfg.stream = stream;
     cfg.gridDim = dim3(sms * 8);
     cfg.blockDim = dim3(256);
-    if (hash_bits > 0)
-        e = cudaLaunchKernelEx(&cfg, win_mark_hash, hslots, 1ull << hash_bits, bitmap);
-    else
-        e = cudaLaunchKernelEx(&cfg, win_mark_dense, hist, n_bins, n_words, bitmap);
+    e = mark(cfg, n_words);
     if (e != cudaSuccess) return e;
     cfg.gridDim = dim3(n_chunks);
     cfg.blockDim = dim3(kCountThreads);
@@ -198,6 +201,41 @@ cudaError_t launch_window_count(const unsigned long long* hist, const unsigned l
     cfg.gridDim = dim3(1);
     cfg.blockDim = dim3(1024);
     return cudaLaunchKernelEx(&cfg, win_scan_chunks, chunk, n_chunks, total);
+}
+
+}  // namespace
+
+cudaError_t launch_window_count(const unsigned long long* hist, const unsigned long long* hslots, int hash_bits,
+                                unsigned long long n_bins, unsigned* bitmap, unsigned* wpre, unsigned* chunk,
+                                unsigned long long* total, int sms, cudaStream_t stream) {
+    return count_marked(n_bins, bitmap, wpre, chunk, total, sms, stream,
+                        [&](cudaLaunchConfig_t& cfg, unsigned long long n_words) {
+                            if (hash_bits > 0)
+                                return cudaLaunchKernelEx(&cfg, win_mark_hash, hslots, 1ull << hash_bits, bitmap);
+                            return cudaLaunchKernelEx(&cfg, win_mark_dense<unsigned long long>, hist, n_bins,
+                                                      n_words, bitmap);
+                        });
+}
+
+cudaError_t launch_final_count(const unsigned* counts, unsigned long long n_states, unsigned* bitmap,
+                               unsigned* wpre, unsigned* chunk, unsigned long long* total, int sms,
+                               cudaStream_t stream) {
+    return count_marked(n_states, bitmap, wpre, chunk, total, sms, stream,
+                        [&](cudaLaunchConfig_t& cfg, unsigned long long n_words) {
+                            return cudaLaunchKernelEx(&cfg, win_mark_dense<unsigned>, counts, n_states, n_words,
+                                                      bitmap);
+                        });
+}
+
+cudaError_t launch_final_emit(const unsigned* counts, unsigned long long n_states, const unsigned* bitmap,
+                              const unsigned* wpre, const unsigned* chunk, unsigned* out_state, unsigned* out_count,
+                              int sms, cudaStream_t stream) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.stream = stream;
+    cfg.gridDim = dim3(sms * 8);
+    cfg.blockDim = dim3(256);
+    return cudaLaunchKernelEx(&cfg, win_emit_dense<unsigned>, counts, window_bitmap_words(n_states), bitmap, wpre,
+                              chunk, out_state, out_count);
 }
 
 cudaError_t launch_window_emit(const unsigned long long* hist, const unsigned long long* hslots, int hash_bits,
@@ -211,8 +249,8 @@ cudaError_t launch_window_emit(const unsigned long long* hist, const unsigned lo
     if (hash_bits > 0)
         return cudaLaunchKernelEx(&cfg, win_emit_hash, hslots, 1ull << hash_bits, bitmap, wpre, chunk, out_bin,
                                   out_sum);
-    return cudaLaunchKernelEx(&cfg, win_emit_dense, hist, window_bitmap_words(n_bins), bitmap, wpre, chunk, out_bin,
-                              out_sum);
+    return cudaLaunchKernelEx(&cfg, win_emit_dense<unsigned long long>, hist, window_bitmap_words(n_bins), bitmap,
+                              wpre, chunk, out_bin, out_sum);
 }
 
 // ---------------------------------------------------------------------------------------------

@@ -372,11 +372,27 @@ mbg_status mbg_sim_probtraj_sparse(mbg_sim* s, uint64_t* bins, uint64_t* sums, d
 mbg_status mbg_sim_final_states(mbg_sim* s, double* probs) {
     if (!s || !probs) return fail(MBG_ERR_ARG, "null argument");
     return guard([&] {
+        const mbg::Sim& sim = s->sim;
         s->sim.fetch();
-        const double n = (double)s->sim.n_traj;
-        const uint32_t* f = s->sim.fin.data();
-        // most of 2^outputs states are never final: divide only the reached ones
-        for (size_t i = 0; i < s->sim.fin.size(); ++i) probs[i] = f[i] ? (double)f[i] / n : 0.0;
+        const double n = (double)sim.n_traj;
+        std::memset(probs, 0, sizeof(double) << sim.cm.n_out);
+        for (size_t e = 0; e < sim.fin_state.size(); ++e) probs[sim.fin_state[e]] = (double)sim.fin_count[e] / n;
+    });
+}
+
+mbg_status mbg_sim_final_states_sparse(mbg_sim* s, uint64_t* states, double* probs, size_t cap, size_t* count) {
+    if (!s || !count) return fail(MBG_ERR_ARG, "null argument");
+    return guard([&] {
+        const mbg::Sim& sim = s->sim;
+        s->sim.fetch();
+        const size_t n = sim.fin_state.size();
+        *count = n;
+        const size_t m = n < cap ? n : cap;
+        const double n_traj = (double)sim.n_traj;
+        for (size_t e = 0; e < m; ++e) {
+            if (states) states[e] = sim.fin_state[e];
+            if (probs) probs[e] = (double)sim.fin_count[e] / n_traj;
+        }
     });
 }
 

@@ -123,16 +123,13 @@ void write_fp_csv(const Sim& s, const std::string& path) {
 void write_final_states_csv(const Sim& s, const std::string& path) {
     std::ofstream ofs(path);
     if (!ofs) throw IoError("cannot write " + path);
-    const size_t S = (size_t)1 << s.cm.n_out;
-    size_t reached = 0;
-    for (size_t x = 0; x < S; ++x) reached += s.fin[x] != 0;
-    ofs << "Final States (" << reached << ")\n";
+    ofs << "Final States (" << s.fin_state.size() << ")\n";
     ofs << "Proba\tState";
     for (int q = 0; q < s.cm.n_out; ++q) ofs << "\t" << s.names[s.cm.out_nodes[q]];
     ofs << "\n";
-    for (size_t x = 0; x < S; ++x) {
-        if (s.fin[x] == 0) continue;
-        ofs << (float)((double)s.fin[x] / (double)s.n_traj) << "\t" << out_state_string(s, (uint32_t)x);
+    for (size_t e = 0; e < s.fin_state.size(); ++e) {
+        const uint32_t x = s.fin_state[e];
+        ofs << (float)((double)s.fin_count[e] / (double)s.n_traj) << "\t" << out_state_string(s, x);
         for (int q = 0; q < s.cm.n_out; ++q) ofs << "\t" << ((x >> q) & 1u);
         ofs << "\n";
     }
@@ -143,9 +140,8 @@ void print_results(const Sim& s, std::ostream& os) {
     const size_t S = (size_t)1 << s.cm.n_out;
     const uint32_t smask = (uint32_t)(S - 1);
     os << "final points:\n";
-    for (size_t x = 0; x < S; ++x)
-        if (s.fin[x] != 0)
-            os << (float)((double)s.fin[x] / (double)s.n_traj) << " " << out_state_string(s, (uint32_t)x) << "\n";
+    for (size_t e = 0; e < s.fin_state.size(); ++e)
+        os << (float)((double)s.fin_count[e] / (double)s.n_traj) << " " << out_state_string(s, s.fin_state[e]) << "\n";
     os << "fixed points:\n";
     for (const FixedPoint& f : s.fixed)
         os << (float)((double)f.count / (double)s.n_traj) << " " << state_string(s.names, f.words, s.cm.n) << "\n";

@@ -319,7 +319,8 @@ Sim::~Sim() {
     // the device implicitly; the cache does not)
     if (!owned.empty()) cudaDeviceSynchronize();
     for (void* p : {(void*)dense_hist, (void*)hslots, (void*)wc_bitmap, (void*)wc_wpre, (void*)wc_chunk,
-                    (void*)wc_total, (void*)wc_bin, (void*)wc_sum, (void*)lane_state})
+                    (void*)wc_total, (void*)wc_bin, (void*)wc_sum, (void*)fc_state, (void*)fc_count,
+                    (void*)lane_state})
         dev_free(p);
     if (ev0) cudaEventDestroy(ev0);
     if (ev1) cudaEventDestroy(ev1);
@@ -745,6 +746,15 @@ void Sim::launch(cudaStream_t stream) {
     fetched = false;
 }
 
+void Sim::compaction_scratch() {
+    if (wc_bitmap) return;
+    const uint64_t words = window_bitmap_words(n_bins);
+    wc_bitmap = static_cast<unsigned*>(raw_alloc(words * 4, "window bitmap"));
+    wc_wpre = static_cast<unsigned*>(raw_alloc(words * 4, "window bitmap prefixes"));
+    wc_chunk = static_cast<unsigned*>(raw_alloc((size_t)window_chunks(n_bins) * 4, "window chunk prefixes"));
+    wc_total = static_cast<unsigned long long*>(raw_alloc(8, "window bin count"));
+}
+
 void Sim::fetch() {
     if (!ran) throw StateError("results requested before mbg_sim_run");
     if (fetched) return;
@@ -761,10 +771,45 @@ void Sim::fetch() {
     ck(cudaSetDevice(device), "cudaSetDevice");
     const uint64_t S = 1ull << cm.n_out;
     th.resize(cm.windows);
-    fin.resize(S);
     ck(cudaMemcpy(th.data(), prm.th_hist, th.size() * 8, cudaMemcpyDeviceToHost), "cudaMemcpy D2H");
-    ck(cudaMemcpy(fin.data(), prm.final_hist, fin.size() * 4, cudaMemcpyDeviceToHost), "cudaMemcpy D2H");
-    phase("transition entropy and final states");
+    phase("transition entropy");
+    // final states: the reached output states only
+    fin_state.clear();
+    fin_count.clear();
+    if (S <= (1ull << 16)) {
+        // at most 256 KiB of counts: read whole and compacted here
+        std::vector<uint32_t> f(S);
+        ck(cudaMemcpy(f.data(), prm.final_hist, S * 4, cudaMemcpyDeviceToHost), "cudaMemcpy D2H");
+        for (uint64_t x = 0; x < S; ++x)
+            if (f[x]) {
+                fin_state.push_back((uint32_t)x);
+                fin_count.push_back(f[x]);
+            }
+    } else {
+        compaction_scratch();
+        ck(launch_final_count(prm.final_hist, S, wc_bitmap, wc_wpre, wc_chunk, wc_total, sms, nullptr),
+           "final-state compaction (count)");
+        unsigned long long total = 0;
+        ck(cudaMemcpy(&total, wc_total, 8, cudaMemcpyDeviceToHost), "cudaMemcpy D2H");
+        if (total > fc_cap) {
+            free_now(fc_state);
+            free_now(fc_count);
+            fc_state = fc_count = nullptr;
+            fc_cap = 0;
+            fc_state = static_cast<unsigned*>(raw_alloc(total * 4, "compacted final states"));
+            fc_count = static_cast<unsigned*>(raw_alloc(total * 4, "compacted final-state counts"));
+            fc_cap = total;
+        }
+        if (total) {
+            ck(launch_final_emit(prm.final_hist, S, wc_bitmap, wc_wpre, wc_chunk, fc_state, fc_count, sms, nullptr),
+               "final-state compaction (emit)");
+            fin_state.resize(total);
+            fin_count.resize(total);
+            ck(cudaMemcpy(fin_state.data(), fc_state, total * 4, cudaMemcpyDeviceToHost), "cudaMemcpy D2H");
+            ck(cudaMemcpy(fin_count.data(), fc_count, total * 4, cudaMemcpyDeviceToHost), "cudaMemcpy D2H");
+        }
+    }
+    phase("final states");
     // window sums: the non-zero bins in increasing order
     wbin.clear();
     wsum.clear();
@@ -779,13 +824,7 @@ void Sim::fetch() {
             }
     } else {
         // compacted on the device: only the reached bins are copied
-        if (!wc_bitmap) {
-            const uint64_t words = window_bitmap_words(n_bins);
-            wc_bitmap = static_cast<unsigned*>(raw_alloc(words * 4, "window bitmap"));
-            wc_wpre = static_cast<unsigned*>(raw_alloc(words * 4, "window bitmap prefixes"));
-            wc_chunk = static_cast<unsigned*>(raw_alloc((size_t)window_chunks(n_bins) * 4, "window chunk prefixes"));
-            wc_total = static_cast<unsigned long long*>(raw_alloc(8, "window bin count"));
-        }
+        compaction_scratch();
         ck(launch_window_count(dense_hist, hslots, hash_bits, n_bins, wc_bitmap, wc_wpre, wc_chunk, wc_total, sms,
                                nullptr),
            "window compaction (count)");

@@ -76,6 +76,10 @@ public:
     unsigned* wc_bin = nullptr;
     unsigned long long* wc_sum = nullptr;
     uint64_t wc_cap = 0;
+    unsigned* fc_state = nullptr;      // compacted final states and their counts
+    unsigned* fc_count = nullptr;
+    uint64_t fc_cap = 0;
+    void compaction_scratch();         // allocates wc_bitmap .. wc_total for n_bins (>= 2^n_out) entries
 
     bool ran = false, fetched = false;
     mbg_run_summary summary{};
@@ -85,7 +89,9 @@ public:
     std::vector<uint64_t> wsum;
     std::vector<size_t> wstart;
     std::vector<uint64_t> th;
-    std::vector<uint32_t> fin;
+    // Reached final output states in increasing order and their trajectory counts.
+    std::vector<uint32_t> fin_state;
+    std::vector<uint32_t> fin_count;
     std::vector<FixedPoint> fixed;
 };
 
