@@ -529,7 +529,8 @@ def run_ours(args):
     info = model.info
     kms = sum(kernel_ms) / len(kernel_ms)
     kernel = {MBG_LAYOUTS["thread"]: "mbg_sim_thread", MBG_LAYOUTS["warp"]: "mbg_sim_warp",
-              MBG_LAYOUTS["lane"]: "mbg_sim_lane" if summary.get("lane_update") else "mbg_sim_lane_coop",
+              MBG_LAYOUTS["lane"]: {0: "mbg_sim_lane_coop", 1: "mbg_sim_lane",
+                                    2: "mbg_sim_lane_split"}[summary.get("lane_update", 0)],
               MBG_LAYOUTS["lane_global"]: "mbg_sim_lane_global"}[summary["layout"]]
     prof = profile_figures(kernel, args.workload)
     roofline = issue_roofline(prof, trans_step / (kms * 1e-3), peaks, peaks_kind)
@@ -591,7 +592,7 @@ def main():
     ap.add_argument("--workload", default="medium", choices=sorted(WORKLOADS) + ["sweep", "surrogate", "l2atomics"])
     ap.add_argument("--layout", type=int, default=0, help="0 autotuned, 1 thread, 2 warp, 3 lane, 4 lane (global rows)")
     ap.add_argument("--block", type=int, default=0, help="threads per block (0: the layout's default); profiling")
-    ap.add_argument("--lane-update", type=int, default=0, help="lane layout: 0 cooperative, 1 per lane; profiling")
+    ap.add_argument("--lane-update", type=int, default=0, help="lane layout: 0 cooperative, 1 per lane, 2 per lane with the active words in global memory; profiling")
     ap.add_argument("--window-table", type=int, default=0, help="0 auto, 1 dense, 2 hash table; profiling")
     ap.add_argument("--cpu-seconds", type=float, default=CPU_SAMPLE_SECONDS)
     ap.add_argument("--no-cpu", action="store_true")

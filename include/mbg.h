@@ -84,7 +84,10 @@ typedef struct {
     int32_t thread_cutoff;     /* AUTO: > 0 runs N <= cutoff thread per trajectory and the rest warp
                                   per trajectory without timing; 0: autotune */
     int32_t lane_update;       /* LANE: readers of a flipped node updated 0: warp-cooperatively
-                                  (default), 1: by their own lane; AUTO times both */
+                                  (default), 1: by their own lane, 2: by their own lane with the
+                                  active-node words in global memory instead of shared memory
+                                  (more resident trajectories per SM where shared memory bounds
+                                  them); AUTO times all three */
     int32_t window_table;      /* where the window sums accumulate: 0 auto (the dense table up to
                                   2 GiB, the faster one; the hash table beyond), 1 the dense
                                   windows x 2^outputs table (the reference's layout), 2 an
@@ -112,7 +115,8 @@ typedef struct {
     double jit_ms;             /* NVRTC compile time at create (0 if cached) */
     int32_t block_size;        /* threads per block of the simulation kernel */
     int32_t grid_size;         /* blocks of the simulation kernel */
-    int32_t lane_update;       /* LANE: 0 cooperative, 1 per-lane reader updates */
+    int32_t lane_update;       /* LANE: 0 cooperative, 1 per-lane reader updates, 2 per-lane with
+                                  the active-node words in global memory */
     int32_t window_table;      /* 1 dense table, 2 hash table */
     int32_t window_hash_bits;  /* hash table: log2 of its slot count in the last run */
     int32_t window_reruns;     /* runs repeated with a larger hash table (results are the same) */

@@ -17,14 +17,17 @@ from helpers import compare_histograms, compare_trajectories, golden_model, mixe
 pytestmark = pytest.mark.gpu
 
 
-ALL_LAYOUTS = [mbg.LAYOUT_THREAD, mbg.LAYOUT_WARP, mbg.LAYOUT_LANE, "lane-serial", mbg.LAYOUT_LANE_GLOBAL]
+ALL_LAYOUTS = [mbg.LAYOUT_THREAD, mbg.LAYOUT_WARP, mbg.LAYOUT_LANE, "lane-serial", "lane-split", mbg.LAYOUT_LANE_GLOBAL]
 
 
 def layout_kw(layout):
     """Simulation keyword arguments for a layout id; "lane-serial" is the lane layout with each
-    lane updating its own readers."""
+    lane updating its own readers, "lane-split" the same with the active-node words in global
+    memory."""
     if layout == "lane-serial":
         return {"layout": mbg.LAYOUT_LANE, "lane_update": 1}
+    if layout == "lane-split":
+        return {"layout": mbg.LAYOUT_LANE, "lane_update": 2}
     return {"layout": layout}
 
 
@@ -55,12 +58,14 @@ def test_mixed_rate_forms_parity(seed, discrete, layout):
     compare_histograms(model, sim, orc, 2000)
 
 
-@pytest.mark.parametrize("layout", [mbg.LAYOUT_WARP, mbg.LAYOUT_LANE, "lane-serial", mbg.LAYOUT_LANE_GLOBAL])
+@pytest.mark.parametrize("layout", [mbg.LAYOUT_WARP, mbg.LAYOUT_LANE, "lane-serial", "lane-split", mbg.LAYOUT_LANE_GLOBAL])
 def test_medium_network_parity(layout):
     net = synth.medium()
     bnd, cfg = net.bnd(), net.cfg(sample_count=192)
     model, sim = run_device(bnd, cfg, 192, **layout_kw(layout))
     assert sim.summary()["layout"] == layout_kw(layout)["layout"]
+    if "lane_update" in layout_kw(layout):
+        assert sim.summary()["lane_update"] == layout_kw(layout)["lane_update"]
     orc = run_oracle(bnd, cfg, model, 192)
     compare_trajectories(sim, orc)
     compare_histograms(model, sim, orc, 192)
@@ -112,13 +117,13 @@ def test_wide_node_parity(layout):
     compare_histograms(model, sim, orc, 3000)
 
 
-@pytest.mark.parametrize("layout", [mbg.LAYOUT_WARP, mbg.LAYOUT_LANE, mbg.LAYOUT_LANE_GLOBAL])
+@pytest.mark.parametrize("layout", [mbg.LAYOUT_WARP, mbg.LAYOUT_LANE, "lane-split", mbg.LAYOUT_LANE_GLOBAL])
 def test_large_network_parity(layout):
     """The 5000-node workload at its own max_time (20) and tick (0.2): 256 trajectories of about
     7000 transitions each, every window compared."""
     net = synth.large()
     bnd, cfg = net.bnd(), net.cfg(sample_count=256)
-    model, sim = run_device(bnd, cfg, 256, layout=layout)
+    model, sim = run_device(bnd, cfg, 256, **layout_kw(layout))
     assert model.info.max_time == 20.0 and model.info.windows == 100
     orc = run_oracle(bnd, cfg, model, 256)
     assert orc.counters["transitions"] > 256 * 1000
@@ -126,7 +131,7 @@ def test_large_network_parity(layout):
     compare_histograms(model, sim, orc, 256)
 
 
-@pytest.mark.parametrize("layout", [mbg.LAYOUT_AUTO, "lane-serial"])
+@pytest.mark.parametrize("layout", [mbg.LAYOUT_AUTO, "lane-serial", "lane-split"])
 def test_medium_network_parity_2000(layout):
     """2000 trajectories of the 1000-node workload, the autotuned kernel included."""
     net = synth.medium()
@@ -138,7 +143,7 @@ def test_medium_network_parity_2000(layout):
 
 
 @pytest.mark.parametrize("layout", [mbg.LAYOUT_AUTO, mbg.LAYOUT_WARP, mbg.LAYOUT_LANE, "lane-serial",
-                                    mbg.LAYOUT_LANE_GLOBAL])
+                                    "lane-split", mbg.LAYOUT_LANE_GLOBAL])
 @pytest.mark.parametrize("name,n", [("cellcycle", 3000), ("metastasis", 300), ("sizek", 300), ("montagud", 200)])
 def test_reference_models_parity(name, n, layout):
     bnd, cfg = golden_model(name)
@@ -148,7 +153,7 @@ def test_reference_models_parity(name, n, layout):
     compare_histograms(model, sim, orc, n)
 
 
-@pytest.mark.parametrize("other", [mbg.LAYOUT_WARP, mbg.LAYOUT_LANE, "lane-serial", mbg.LAYOUT_LANE_GLOBAL])
+@pytest.mark.parametrize("other", [mbg.LAYOUT_WARP, mbg.LAYOUT_LANE, "lane-serial", "lane-split", mbg.LAYOUT_LANE_GLOBAL])
 def test_layouts_agree(other):
     """Every layout runs the same integer arithmetic and the same clock: identical window sums,
     final states and fixed points."""
@@ -191,7 +196,7 @@ def test_trajectory_ids_are_partition_independent():
     assert np.array_equal(a, b + c)
 
 
-@pytest.mark.parametrize("layout", [mbg.LAYOUT_WARP, mbg.LAYOUT_LANE, "lane-serial", mbg.LAYOUT_LANE_GLOBAL])
+@pytest.mark.parametrize("layout", [mbg.LAYOUT_WARP, mbg.LAYOUT_LANE, "lane-serial", "lane-split", mbg.LAYOUT_LANE_GLOBAL])
 def test_step_limit_is_counted(layout):
     net = synth.medium()
     bnd, cfg = net.bnd(), net.cfg(sample_count=64)

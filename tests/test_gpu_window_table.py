@@ -43,15 +43,22 @@ def same_windows(a, b, same_layout=True):
     assert np.array_equal(a.final_states(), b.final_states())
 
 
-HASH_LAYOUTS = [mbg.LAYOUT_THREAD, mbg.LAYOUT_LANE, mbg.LAYOUT_LANE_GLOBAL]
+HASH_LAYOUTS = [mbg.LAYOUT_THREAD, mbg.LAYOUT_LANE, "lane-split", mbg.LAYOUT_LANE_GLOBAL]
+
+
+def layout_kw(layout):
+    """"lane-split": the lane layout with the active-node words in global memory."""
+    if layout == "lane-split":
+        return {"layout": mbg.LAYOUT_LANE, "lane_update": 2}
+    return {"layout": layout}
 
 
 @pytest.mark.parametrize("layout", HASH_LAYOUTS)
 def test_hash_table_equals_dense_table(layout):
     net = synth.small()  # 20 outputs: 2^20 states per window
     bnd, cfg = net.bnd(), net.cfg()
-    _, dense = simulate(bnd, cfg, 20000, DENSE, layout=layout)
-    _, hashed = simulate(bnd, cfg, 20000, HASH, layout=layout)
+    _, dense = simulate(bnd, cfg, 20000, DENSE, **layout_kw(layout))
+    _, hashed = simulate(bnd, cfg, 20000, HASH, **layout_kw(layout))
     assert dense.summary()["window_table"] == DENSE
     s = hashed.summary()
     assert s["window_table"] == HASH and s["window_reruns"] == 0
@@ -65,8 +72,8 @@ def test_full_table_grows_and_reruns(layout):
     repeats on tables four times larger until it holds, and the result is the dense table's."""
     net = synth.small()
     bnd, cfg = net.bnd(), net.cfg()
-    _, dense = simulate(bnd, cfg, 20000, DENSE, layout=layout)
-    _, hashed = simulate(bnd, cfg, 20000, HASH, bits=10, layout=layout)
+    _, dense = simulate(bnd, cfg, 20000, DENSE, **layout_kw(layout))
+    _, hashed = simulate(bnd, cfg, 20000, HASH, bits=10, **layout_kw(layout))
     s = hashed.summary()
     assert s["window_reruns"] >= 1 and s["window_hash_bits"] > 10
     assert s["window_entries"] * 2 > (1 << 10)

@@ -26,16 +26,25 @@ cudaError_t sim_lane_global_configure(bool full, int block, int* blocks_per_sm);
 cudaError_t launch_sim_lane_global(const SimParams& p, bool full, int grid, int block, cudaStream_t stream);
 // Dynamic shared memory of a lane-layout block (the same for both reader-update variants).
 size_t sim_lane_smem(int n, int block);
+// Lane layout with the active-word rows in global memory (SimParams::lane_state, G x block words
+// per block at lane_block_bytes; per-lane reader update): shared memory per block, configuration,
+// launch (the window-hash twin when SimParams::hash_bits > 0). sim_kernel_limits numbers it 8
+// (variant: `_full`).
+size_t sim_lane_split_smem(int n, int block);
+cudaError_t sim_lane_split_configure(bool full, size_t smem, int block, int* blocks_per_sm);
+cudaError_t launch_sim_lane_split(const SimParams& p, bool full, int grid, int block, size_t smem,
+                                  cudaStream_t stream);
 int sim_lane_rows(int n);                 // BatchDesc::rows for models of up to n nodes
 // Re-applies the attributes of a simulation kernel for the launch shapes that are about to use it
 // (kernel 0: mbg_sim_lane[_coop], 1: mbg_sim_lane_batch[_coop], 2: mbg_sim_warp_batch[_gather],
-// 3: mbg_sim_warp[_gather], 4: mbg_sim_lane[_coop]_full, 5: mbg_sim_lane_batch[_coop]_full;
-// variant selects the second name; hash: the window-hash twin of kernel 0, 4 or 6): kernel attributes
+// 3: mbg_sim_warp[_gather], 4: mbg_sim_lane[_coop]_full, 5: mbg_sim_lane_batch[_coop]_full,
+// 6: mbg_sim_lane_global[_full], 7: mbg_sim_lane_batch_global[_full], 8: mbg_sim_lane_split[_full];
+// variant selects the second name; hash: the window-hash twin of kernel 0, 4, 6 or 8): kernel attributes
 // are process-wide, so another handle may have changed them since this one was configured.
 cudaError_t sim_kernel_limits(int kernel, bool variant, const int* blocks, const size_t* smems, const int* want,
                               int count, bool hash = false);
 // The window-hash twins of the lane-layout single-simulation kernels (sim_aot_hash.cu), by the
-// numbering of sim_kernel_limits (0, 4, 6); the launchers pick them when SimParams::hash_bits > 0.
+// numbering of sim_kernel_limits (0, 4, 6, 8); the launchers pick them when SimParams::hash_bits > 0.
 // The warp layout has none: it runs on the dense window table only.
 const void* sim_kernel_hash(int kernel, bool variant);
 std::mutex& kernel_attr_mutex();

@@ -67,6 +67,23 @@ extern "C" __global__ void __launch_bounds__(256, 3) mbg_sim_lane_global_full(co
     sim_lane_body<false, true>(p, p.lane_state + (size_t)blockIdx.x * p.lane_block_bytes);
 }
 
+// The lane layout with the Fenwick tree and the state rows in shared memory and the active-word
+// rows (read once per re-evaluated reader and once per walked group) in global memory, per block
+// as in the global-row kernels: 256 instead of 384 bytes of shared memory per trajectory at 1000
+// nodes, so three resident blocks of 256 per SM instead of two, at 80 registers (per-lane reader
+// update).
+extern "C" __global__ void __launch_bounds__(256, 3) mbg_sim_lane_split(const SimParams p) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    sim_lane_body<false, false>(p, smem,
+                                reinterpret_cast<unsigned*>(p.lane_state + (size_t)blockIdx.x * p.lane_block_bytes));
+}
+
+extern "C" __global__ void __launch_bounds__(256, 3) mbg_sim_lane_split_full(const SimParams p) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    sim_lane_body<false, true>(p, smem,
+                               reinterpret_cast<unsigned*>(p.lane_state + (size_t)blockIdx.x * p.lane_block_bytes));
+}
+
 // Batched instances (parameter sweeps) in the lane layout, both reader-update variants.
 extern "C" __global__ void __launch_bounds__(256, 3) mbg_sim_lane_batch(const BatchDesc b) {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -356,6 +373,7 @@ cudaError_t sim_kernel_limits(int kernel, bool variant, const int* blocks, const
         case 2: f = variant ? (const void*)mbg_sim_warp_batch : (const void*)mbg_sim_warp_batch_gather; break;
         case 6: f = variant ? (const void*)mbg_sim_lane_global_full : (const void*)mbg_sim_lane_global; break;
         case 7: f = variant ? (const void*)mbg_sim_lane_batch_global_full : (const void*)mbg_sim_lane_batch_global; break;
+        case 8: f = variant ? (const void*)mbg_sim_lane_split_full : (const void*)mbg_sim_lane_split; break;
         default: f = variant ? (const void*)mbg_sim_warp : (const void*)mbg_sim_warp_gather; break;
     }
     return shared_limits(f, blocks, smems, want, count);
@@ -407,6 +425,23 @@ cudaError_t launch_sim_lane_global(const SimParams& p, bool full, int grid, int 
 }
 
 int sim_lane_rows(int n) { return lane_groups(n); }
+
+size_t sim_lane_split_smem(int n, int block) {
+    const int G = lane_groups(n);
+    return (size_t)block * (8u * (unsigned)lane_leaves(G, lane_leaf_shift(G)) + 4u * (unsigned)G);
+}
+
+cudaError_t sim_lane_split_configure(bool full, size_t smem, int block, int* blocks_per_sm) {
+    return lane_configure(full ? (const void*)mbg_sim_lane_split_full : (const void*)mbg_sim_lane_split, smem, block,
+                          blocks_per_sm);
+}
+
+cudaError_t launch_sim_lane_split(const SimParams& p, bool full, int grid, int block, size_t smem,
+                                  cudaStream_t stream) {
+    if (p.hash_bits > 0)
+        return launch((void (*)(SimParams))sim_kernel_hash(8, full), grid, block, smem, stream, p);
+    return launch(full ? mbg_sim_lane_split_full : mbg_sim_lane_split, grid, block, smem, stream, p);
+}
 
 cudaError_t launch_fp_aggregate(const unsigned* fp_states, const unsigned* fp_count, unsigned capacity, int words,
                                 unsigned* slot_rep, unsigned* slot_cnt, unsigned n_slots, unsigned* out_states,

@@ -47,8 +47,21 @@ extern "C" __global__ void __launch_bounds__(256, 3) mbg_sim_lane_global_full_ha
     sim_lane_body<false, true>(p, p.lane_state + (size_t)blockIdx.x * p.lane_block_bytes);
 }
 
+extern "C" __global__ void __launch_bounds__(256, 3) mbg_sim_lane_split_hash(const SimParams p) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    sim_lane_body<false, false>(p, smem,
+                                reinterpret_cast<unsigned*>(p.lane_state + (size_t)blockIdx.x * p.lane_block_bytes));
+}
+
+extern "C" __global__ void __launch_bounds__(256, 3) mbg_sim_lane_split_full_hash(const SimParams p) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    sim_lane_body<false, true>(p, smem,
+                               reinterpret_cast<unsigned*>(p.lane_state + (size_t)blockIdx.x * p.lane_block_bytes));
+}
+
 const void* sim_kernel_hash(int kernel, bool variant) {
     switch (kernel) {
+        case 8: return variant ? (const void*)mbg_sim_lane_split_full_hash : (const void*)mbg_sim_lane_split_hash;
         case 6: return variant ? (const void*)mbg_sim_lane_global_full_hash : (const void*)mbg_sim_lane_global_hash;
         case 0: return variant ? (const void*)mbg_sim_lane_coop_hash : (const void*)mbg_sim_lane_hash;
         case 4: return variant ? (const void*)mbg_sim_lane_coop_full_hash : (const void*)mbg_sim_lane_full_hash;

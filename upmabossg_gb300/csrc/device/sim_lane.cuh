@@ -43,13 +43,14 @@ struct LaneSmem {
 };
 
 // `G` rows of T entries per array: the largest model's group count in a batched launch, which
-// also sets the leaf width of every trajectory of the launch.
-__device__ __forceinline__ LaneSmem lane_smem_at(unsigned char* base, int G, int T) {
+// also sets the leaf width of every trajectory of the launch. `act_rows`, when given, holds the
+// active-word rows instead of the space after the state rows.
+__device__ __forceinline__ LaneSmem lane_smem_at(unsigned char* base, int G, int T, unsigned* act_rows = nullptr) {
     LaneSmem m;
     m.shift = lane_leaf_shift(G);
     m.fen = reinterpret_cast<unsigned long long*>(base);
     m.st = reinterpret_cast<unsigned*>(m.fen + (size_t)lane_leaves(G, m.shift) * T);
-    m.act = m.st + (size_t)G * T;
+    m.act = act_rows ? act_rows : m.st + (size_t)G * T;
     return m;
 }
 
@@ -593,11 +594,11 @@ __device__ __forceinline__ void lane_step_back(const SimParams& p, const LaneSme
 
 // One simulation: lanes take trajectory ids from the run's work counter.
 template <bool COOP, bool FULL>
-__device__ void sim_lane_body(const SimParams& p, unsigned char* smem) {
+__device__ void sim_lane_body(const SimParams& p, unsigned char* smem, unsigned* act_rows = nullptr) {
     const int T = (int)blockDim.x;
     const unsigned lane = threadIdx.x & 31u;
     const int wbase = (int)(threadIdx.x & ~31u);
-    const LaneSmem m = lane_smem_at(smem, lane_groups(p.n), T);
+    const LaneSmem m = lane_smem_at(smem, lane_groups(p.n), T, act_rows);
     const int col = (int)threadIdx.x;
     LaneTraj tr;
     LaneCounts c;

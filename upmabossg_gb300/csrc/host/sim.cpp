@@ -9,6 +9,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cctype>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -405,7 +406,7 @@ void Sim::create(const CompiledModel& model, const std::vector<std::string>& nod
     if (o.block_size && (o.block_size % 32 != 0 || o.block_size > 256))
         throw ArgError("block_size must be a multiple of 32, at most 256");
     if (o.layout < MBG_LAYOUT_AUTO || o.layout > MBG_LAYOUT_LANE_GLOBAL) throw ArgError("unknown layout");
-    if (o.lane_update < 0 || o.lane_update > 1) throw ArgError("lane_update must be 0 or 1");
+    if (o.lane_update < 0 || o.lane_update > 2) throw ArgError("lane_update must be 0, 1 or 2");
     if (o.layout == MBG_LAYOUT_THREAD && cm.words > 16) throw ModelError("thread layout supports at most 512 nodes");
     if (o.layout != MBG_LAYOUT_AUTO) {
         int blk = o.block_size;
@@ -413,25 +414,28 @@ void Sim::create(const CompiledModel& model, const std::vector<std::string>& nod
             // the lane layout's shared memory grows with N: the largest block that fits
             blk = 256;
             if (o.layout == MBG_LAYOUT_LANE)
-                while (blk > 32 && sim_lane_smem(cm.n, blk) > 227 * 1024) blk >>= 1;
+                while (blk > 32 && (o.lane_update == 2 ? sim_lane_split_smem(cm.n, blk) : sim_lane_smem(cm.n, blk)) >
+                                       227 * 1024)
+                    blk >>= 1;
         }
-        setup_layout(o.layout, blk, o.lane_update != 1);
+        setup_layout(o.layout, blk, o.lane_update);
     } else if (o.thread_cutoff > 0) {
         const int big = hash_bits > 0 ? MBG_LAYOUT_LANE_GLOBAL : MBG_LAYOUT_WARP;  // warp: dense table only
         const int lay = cm.words <= 16 && cm.n <= o.thread_cutoff ? MBG_LAYOUT_THREAD : big;
-        setup_layout(lay, o.block_size > 0 ? o.block_size : 256);
+        setup_layout(lay, o.block_size > 0 ? o.block_size : 256, 1);
     } else {
         autotune();
     }
 }
 
 namespace {
-// Autotuned launch shapes per (model size class ceil(log2 N), pilot size class ceil(log2 pilot),
-// redraw_period set), shared by all simulations of the process: layout and threads per block.
+// Autotuned launch shapes per (model size class ceil(log2 N), class ceil(log2 n) of the longest
+// pilot, redraw_period set, window hash table), shared by all simulations of the process: layout,
+// threads per block and the lane layout's reader update.
 std::mutex g_tune_mu;
 struct Shape {
     int layout, block;
-    bool coop;
+    int update;  // the lane layout's reader update (mbg_sim_opts::lane_update); 1 for the others
 };
 std::map<std::tuple<int, int, int, int>, Shape> g_tuned;
 
@@ -449,23 +453,27 @@ std::string tune_key(int device, const std::tuple<int, int, int, int>& cls) {
     if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) return std::string();
     std::string name = prop.name;
     for (char& c : name)
-        if (c == ' ' || c == '|') c = '_';
-    return name + "|" + std::to_string(prop.multiProcessorCount) + "|" + __DATE__ + "_" + __TIME__ + "|" +
-           std::to_string(std::get<0>(cls)) + "|" + std::to_string(std::get<1>(cls)) + "|" +
-           std::to_string(std::get<2>(cls)) + "|" + std::to_string(std::get<3>(cls));
+        if (c == '|') c = '_';
+    std::string key = name + "|" + std::to_string(prop.multiProcessorCount) + "|" + __DATE__ + "_" + __TIME__ + "|" +
+                      std::to_string(std::get<0>(cls)) + "|" + std::to_string(std::get<1>(cls)) + "|" +
+                      std::to_string(std::get<2>(cls)) + "|" + std::to_string(std::get<3>(cls));
+    // one whitespace-free token per line (the device name and __DATE__ hold spaces)
+    for (char& c : key)
+        if (std::isspace((unsigned char)c)) c = '_';
+    return key;
 }
 
-std::string tune_path() { return cache_dir() + "/autotune_v1.txt"; }
+std::string tune_path() { return cache_dir() + "/autotune_v2.txt"; }
 
 bool tune_lookup_disk(const std::string& key, Shape& out) {
     if (key.empty() || std::getenv("MBG_AUTOTUNE_NOCACHE")) return false;
     std::ifstream f(tune_path());
     std::string k;
-    int lay = 0, blk = 0, coop = 0;
+    int lay = 0, blk = 0, upd = 0;
     bool found = false;
-    while (f >> k >> lay >> blk >> coop)  // the last line for a key wins
+    while (f >> k >> lay >> blk >> upd)  // the last line for a key wins
         if (k == key) {
-            out = Shape{lay, blk, coop != 0};
+            out = Shape{lay, blk, upd};
             found = true;
         }
     return found;
@@ -475,7 +483,7 @@ void tune_store_disk(const std::string& key, const Shape& s) {
     if (key.empty() || std::getenv("MBG_AUTOTUNE_NOCACHE")) return;
     cache_mkdirs(cache_dir());
     std::ofstream f(tune_path(), std::ios::app);
-    f << key << " " << s.layout << " " << s.block << " " << (s.coop ? 1 : 0) << "\n";
+    f << key << " " << s.layout << " " << s.block << " " << s.update << "\n";
 }
 }  // namespace
 
@@ -483,9 +491,11 @@ void Sim::autotune() {
     // the pilot is large enough to fill the GPU in every layout (or the whole run when smaller),
     // so that the choice reflects occupancy as well as per-transition cost
     const uint64_t pilot = std::min<uint64_t>(n_traj, 1u << 17);
+    // the closest candidates again on a longer pilot: the run itself, up to 2^20 trajectories
+    const uint64_t pilot2 = std::min<uint64_t>(n_traj, 8 * pilot);
     // the lane layout has no redraw_period and the warp layout no window hash table: such runs are
     // tuned (and cached) apart
-    const std::tuple<int, int, int, int> cls{ceil_log2((uint64_t)cm.n), ceil_log2(pilot), opts.redraw_period ? 1 : 0,
+    const std::tuple<int, int, int, int> cls{ceil_log2((uint64_t)cm.n), ceil_log2(pilot2), opts.redraw_period ? 1 : 0,
                                              hash_bits > 0 ? 1 : 0};
     const std::string key = tune_key(device, cls);
     {
@@ -495,7 +505,7 @@ void Sim::autotune() {
         if (it == g_tuned.end() && tune_lookup_disk(key, disk)) it = g_tuned.emplace(cls, disk).first;
         if (it != g_tuned.end()) {
             setup_layout(it->second.layout, opts.block_size > 0 ? opts.block_size : it->second.block,
-                         it->second.coop);
+                         it->second.update);
             return;
         }
     }
@@ -509,40 +519,46 @@ void Sim::autotune() {
     } scope(prm, pilot);
     const bool log = std::getenv("MBG_AUTOTUNE_LOG") != nullptr;
     double best = -1;
-    Shape best_shape{MBG_LAYOUT_WARP, 256, false};
+    Shape best_shape{MBG_LAYOUT_WARP, 256, 1};
     std::vector<std::pair<double, Shape>> timed;
     for (int lay : {MBG_LAYOUT_THREAD, MBG_LAYOUT_WARP, MBG_LAYOUT_LANE, MBG_LAYOUT_LANE_GLOBAL}) {
         for (int blk : {64, 128, 256}) {
-            for (int coop = 0; coop < 2; ++coop) {
+            for (int upd = 0; upd < 3; ++upd) {
                 if (opts.block_size > 0 && blk != opts.block_size) continue;
-                if (lay != MBG_LAYOUT_LANE && (blk == 64 || coop)) continue;
+                if (lay != MBG_LAYOUT_LANE && (blk == 64 || upd != 1)) continue;
                 if (lay == MBG_LAYOUT_LANE_GLOBAL && opts.redraw_period) continue;
                 if (lay == MBG_LAYOUT_WARP && hash_bits > 0) continue;  // dense window table only
                 if (lay == MBG_LAYOUT_THREAD && cm.words > 16) continue;
-                if (lay == MBG_LAYOUT_LANE && (opts.redraw_period || sim_lane_smem(cm.n, blk) > 227 * 1024)) continue;
+                if (lay == MBG_LAYOUT_LANE && opts.redraw_period) continue;
+                // the lane layout's rows in shared memory; the active-word rows in global memory
+                // (update 2) only in blocks of 128 and 256
+                if (lay == MBG_LAYOUT_LANE && upd < 2 && sim_lane_smem(cm.n, blk) > 227 * 1024) continue;
+                if (lay == MBG_LAYOUT_LANE && upd == 2 && (blk == 64 || sim_lane_split_smem(cm.n, blk) > 227 * 1024))
+                    continue;
                 try {
-                    setup_layout(lay, blk, coop != 0);
+                    setup_layout(lay, blk, upd);
                 } catch (const JitError&) {
                     continue;  // a thread-layout kernel NVRTC cannot build: the other layouts remain
                 }
                 run(nullptr);  // warm-up (and JIT load)
                 run(nullptr);
                 if (log)
-                    std::fprintf(stderr, "mbg autotune: n=%d pilot=%llu layout=%d block=%d coop=%d kernel_ms=%.3f\n",
-                                 cm.n, (unsigned long long)pilot, lay, blk, coop, summary.kernel_ms);
-                timed.push_back({summary.kernel_ms, Shape{lay, blk, coop != 0}});
+                    std::fprintf(stderr, "mbg autotune: n=%d pilot=%llu layout=%d block=%d update=%d kernel_ms=%.3f\n",
+                                 cm.n, (unsigned long long)pilot, lay, blk, upd, summary.kernel_ms);
+                timed.push_back({summary.kernel_ms, Shape{lay, blk, upd}});
                 if (best < 0 || summary.kernel_ms < best) {
                     best = summary.kernel_ms;
-                    best_shape = Shape{lay, blk, coop != 0};
+                    best_shape = Shape{lay, blk, upd};
                 }
             }
         }
     }
     // A short pilot starts every lane's first trajectory together; a long run reaches a steady
     // state in which the lanes of a warp are at unrelated points of their trajectories, and the
-    // layouts rank differently there. The closest candidates are timed again on a pilot four
-    // times longer.
-    const uint64_t pilot2 = std::min<uint64_t>(n_traj, 4 * pilot);
+    // layouts rank differently there (as do layouts that hold different numbers of trajectories
+    // resident: on the 1000-node workload the active words in global memory hold 768 per SM
+    // against 512, 20% slower on 2^17 trajectories, even on 2^19, 4% faster on 10^6). The closest
+    // candidates are timed again on a pilot up to eight times longer.
     if (pilot2 > pilot && timed.size() > 1) {
         std::sort(timed.begin(), timed.end(), [](const auto& a, const auto& b) { return a.first < b.first; });
         scope.p.n_traj = pilot2;
@@ -552,7 +568,8 @@ void Sim::autotune() {
         for (size_t i = 0; i < timed.size(); ++i) {
             bool first_of_kind = true;
             for (size_t j = 0; j < i; ++j)
-                if (timed[j].second.layout == timed[i].second.layout && timed[j].second.coop == timed[i].second.coop)
+                if (timed[j].second.layout == timed[i].second.layout &&
+                    timed[j].second.update == timed[i].second.update)
                     first_of_kind = false;
             if ((i < 3 && timed[i].first <= 1.15 * timed[0].first) ||
                 (first_of_kind && timed[i].first <= 1.3 * timed[0].first))
@@ -561,12 +578,11 @@ void Sim::autotune() {
         best = -1;
         for (size_t i : pick) {
             const Shape& sh = timed[i].second;
-            setup_layout(sh.layout, sh.block, sh.coop);
+            setup_layout(sh.layout, sh.block, sh.update);
             run(nullptr);
             if (log)
-                std::fprintf(stderr, "mbg autotune: n=%d pilot=%llu layout=%d block=%d coop=%d kernel_ms=%.3f\n",
-                             cm.n, (unsigned long long)pilot2, sh.layout, sh.block, sh.coop ? 1 : 0,
-                             summary.kernel_ms);
+                std::fprintf(stderr, "mbg autotune: n=%d pilot=%llu layout=%d block=%d update=%d kernel_ms=%.3f\n",
+                             cm.n, (unsigned long long)pilot2, sh.layout, sh.block, sh.update, summary.kernel_ms);
             if (best < 0 || summary.kernel_ms < best) {
                 best = summary.kernel_ms;
                 best_shape = sh;
@@ -575,16 +591,17 @@ void Sim::autotune() {
     }
     scope.p.n_traj = scope.saved;
     ran = false;
-    setup_layout(best_shape.layout, best_shape.block, best_shape.coop);
+    setup_layout(best_shape.layout, best_shape.block, best_shape.update);
     std::lock_guard<std::mutex> lock(g_tune_mu);
     g_tuned[cls] = best_shape;
     tune_store_disk(key, best_shape);
 }
 
-void Sim::setup_layout(int lay, int blk, bool coop) {
+void Sim::setup_layout(int lay, int blk, int update) {
     layout = lay;
     block = blk;
-    lane_coop = coop;
+    lane_coop = update == 0;
+    lane_split = lay == MBG_LAYOUT_LANE && update == 2;
     int bps = 0;
     if (layout == MBG_LAYOUT_THREAD) {
         double ms = 0;
@@ -598,9 +615,12 @@ void Sim::setup_layout(int lay, int blk, bool coop) {
         lane_coop = false;  // per-lane reader update only
         ck(sim_lane_global_configure(lane_full, block, &bps), "configuring mbg_sim_lane_global");
     } else if (layout == MBG_LAYOUT_LANE) {
-        smem = sim_lane_smem(cm.n, block);
+        smem = lane_split ? sim_lane_split_smem(cm.n, block) : sim_lane_smem(cm.n, block);
         if (smem > 227 * 1024) throw ModelError("model too large for the lane layout's shared memory at this block size");
-        ck(sim_lane_configure(lane_coop, lane_full, smem, block, &bps), "configuring mbg_sim_lane");
+        if (lane_split)
+            ck(sim_lane_split_configure(lane_full, smem, block, &bps), "configuring mbg_sim_lane_split");
+        else
+            ck(sim_lane_configure(lane_coop, lane_full, smem, block, &bps), "configuring mbg_sim_lane");
     } else {
         // keep every node's regulator index in shared memory while a block's share stays small
         // enough for several resident blocks per SM; otherwise re-gather it on each update
@@ -613,9 +633,12 @@ void Sim::setup_layout(int lay, int blk, bool coop) {
     if (bps < 1) throw CudaError("kernel cannot be resident with this block size");
     if (opts.blocks_per_sm > 0) bps = std::min(bps, (int)opts.blocks_per_sm);
     grid = sms * bps;
-    if (layout == MBG_LAYOUT_LANE_GLOBAL) {
-        // every resident block's rows, each block's share 256-byte aligned
-        const uint64_t block_bytes = (sim_lane_smem(cm.n, block) + 255) & ~(uint64_t)255;
+    if (layout == MBG_LAYOUT_LANE_GLOBAL || (layout == MBG_LAYOUT_LANE && lane_split)) {
+        // every resident block's rows (all of them, or the active words), each block's share
+        // 256-byte aligned
+        const uint64_t rows = layout == MBG_LAYOUT_LANE ? (uint64_t)sim_lane_rows(cm.n) * 4 * block
+                                                        : sim_lane_smem(cm.n, block);
+        const uint64_t block_bytes = (rows + 255) & ~(uint64_t)255;
         const uint64_t need = block_bytes * (uint64_t)grid;
         if (need > lane_state_bytes) {
             free_now(lane_state);
@@ -697,6 +720,9 @@ void Sim::launch(cudaStream_t stream) {
         if (layout == MBG_LAYOUT_LANE_GLOBAL) {
             ck(sim_kernel_limits(6, lane_full, &block, &smem, &want, 1, hash_bits > 0), "mbg_sim_lane_global attributes");
             ck(launch_sim_lane_global(prm, lane_full, grid, block, stream), "launch mbg_sim_lane_global");
+        } else if (layout == MBG_LAYOUT_LANE && lane_split) {
+            ck(sim_kernel_limits(8, lane_full, &block, &smem, &want, 1, hash_bits > 0), "mbg_sim_lane_split attributes");
+            ck(launch_sim_lane_split(prm, lane_full, grid, block, smem, stream), "launch mbg_sim_lane_split");
         } else if (layout == MBG_LAYOUT_LANE) {
             ck(sim_kernel_limits(lane_full ? 4 : 0, lane_coop, &block, &smem, &want, 1, hash_bits > 0),
                "mbg_sim_lane attributes");
@@ -738,7 +764,8 @@ void Sim::launch(cudaStream_t stream) {
     summary.jit_ms = jit_ms;
     summary.block_size = block;
     summary.grid_size = grid;
-    summary.lane_update = (layout == MBG_LAYOUT_LANE && !lane_coop) || layout == MBG_LAYOUT_LANE_GLOBAL ? 1 : 0;
+    summary.lane_update = layout == MBG_LAYOUT_LANE ? (lane_split ? 2 : lane_coop ? 0 : 1)
+                          : layout == MBG_LAYOUT_LANE_GLOBAL ? 1 : 0;
     summary.window_table = hash_bits > 0 ? 2 : 1;
     summary.window_hash_bits = hash_bits;
     summary.window_entries = hash_bits > 0 ? hc[CNT_WIN_ENTRIES] : 0;

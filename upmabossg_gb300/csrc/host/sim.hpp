@@ -23,9 +23,9 @@ public:
     void create(const CompiledModel& cm, const std::vector<std::string>& names, const mbg_sim_opts& o);
     void run(cudaStream_t stream);
     void fetch();  // copies results to the host vectors below
-    // Chooses kernel, block size, shared memory and grid for a layout (coop: the lane layout's
-    // warp-cooperative reader update).
-    void setup_layout(int layout, int block, bool coop = true);
+    // Chooses kernel, block size, shared memory and grid for a layout (update: the lane layout's
+    // reader update, mbg_sim_opts::lane_update).
+    void setup_layout(int layout, int block, int update = 0);
     // AUTO layout: times every layout and shape on a pilot subset once per model size class.
     void autotune();
 
@@ -38,10 +38,12 @@ public:
     bool cached_index = false;
     bool lane_coop = true;
     bool lane_full = false;  // palette rates or nodes over 12 regulators: the `_full` lane kernels
+    bool lane_split = false;  // lane layout with the active-word rows in global memory (lane_update 2)
     double jit_ms = 0;
     void* thread_kernel = nullptr;
     void* thread_kernel_hash = nullptr;  // the thread layout's window-hash variant, compiled on first use
-    unsigned char* lane_state = nullptr;  // MBG_LAYOUT_LANE_GLOBAL: every resident block's rows
+    unsigned char* lane_state = nullptr;  // every resident block's rows (global-row lane layout), or
+                                          // its active-word rows (lane_update 2)
     uint64_t lane_state_bytes = 0;
     DeviceLayout dl;
     SimParams prm{};
