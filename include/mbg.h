@@ -302,6 +302,11 @@ mbg_status mbg_batch_summary(const mbg_batch* b, mbg_run_summary* out);
 mbg_status mbg_batch_instance_summary(const mbg_batch* b, int32_t i, mbg_run_summary* out);
 mbg_status mbg_batch_probtraj(mbg_batch* b, int32_t i, double* probs, double* tr_entropy);
 mbg_status mbg_batch_probtraj_raw(mbg_batch* b, int32_t i, uint64_t* sums, uint64_t* th_sums);
+/* One window of every instance at once (window < 0 counts from each instance's last window: -1 is
+ * the final window): the instances' 2^outputs probabilities one after the other in instance order,
+ * instance i's entries after those of instances 0..i-1. One gather on the device and one copy,
+ * instead of a windows x 2^outputs read per instance. */
+mbg_status mbg_batch_window_probs(mbg_batch* b, int32_t window, double* probs);
 mbg_status mbg_batch_final_states(mbg_batch* b, int32_t i, double* probs);
 mbg_status mbg_batch_fixed_points(mbg_batch* b, int32_t i, uint32_t* states, double* probs, size_t cap,
                                   size_t* count);

@@ -117,6 +117,30 @@ def test_graph_replay_and_autotune():
         assert (k["layout"], k["block_size"], k["variant"]) == (best["layout"], best["block_size"], best["variant"])
 
 
+def test_window_gather_equals_per_instance_reads():
+    """mbg_batch_window_probs: one window of every instance gathered on the device, the same
+    doubles as each instance's own probtraj; instances with different output counts come back as a
+    list; a window beyond an instance's last is refused."""
+    texts = instances()
+    models = [mbg.Model.from_strings(b, c) for b, c in texts]
+    batch = mbg.Batch(models, n_traj=[1500] * len(models), seeds=list(range(len(models)))).run()
+    windows = min(m.info.windows for m in models)
+    for w in (0, windows // 2, -1, -2):
+        got = batch.window_probs(w)
+        assert isinstance(got, list) and len(got) == len(models)
+        for i in range(len(models)):
+            P, _ = batch.probtraj(i)
+            assert np.array_equal(got[i], P[w]), (w, i)
+    with pytest.raises(mbg.MbgError):
+        batch.window_probs(max(m.info.windows for m in models))
+    same = [mbg.Model.from_strings(*texts[1])] * 5
+    b2 = mbg.Batch(same, n_traj=[800] * 5, seeds=[3, 4, 5, 6, 7]).run()
+    arr = b2.window_probs(-1)
+    assert arr.shape == (5, 1 << same[0].info.outputs)
+    for i in range(5):
+        assert np.array_equal(arr[i], b2.probtraj(i)[0][-1])
+
+
 def test_batch_probabilities_are_normalised():
     net = synth.sweep_instance(1)
     m = mbg.Model.from_strings(net.bnd(), net.cfg())

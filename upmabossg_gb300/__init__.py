@@ -31,7 +31,7 @@ EXPORTS = (
     "mbg_sim_trajectories", "mbg_write_probtraj_csv", "mbg_write_fp_csv", "mbg_print_results",
     "mbg_write_final_states_csv", "mbg_fixed_points_aggregate_noalloc",
     "mbg_batch_opts_default", "mbg_batch_create", "mbg_batch_destroy", "mbg_batch_run", "mbg_batch_summary",
-    "mbg_batch_instance_summary", "mbg_batch_probtraj", "mbg_batch_probtraj_raw", "mbg_batch_final_states",
+    "mbg_batch_instance_summary", "mbg_batch_probtraj", "mbg_batch_probtraj_raw", "mbg_batch_window_probs", "mbg_batch_final_states",
     "mbg_batch_fixed_points", "mbg_batch_class_count", "mbg_batch_class", "mbg_batch_class_timings",
     "mbg_surrogate_create", "mbg_surrogate_destroy", "mbg_surrogate_train", "mbg_surrogate_predict",
     "mbg_surrogate_param_count", "mbg_surrogate_get_params", "mbg_surrogate_set_params", "mbg_surrogate_gradients",
@@ -161,6 +161,7 @@ def lib():
             "mbg_batch_instance_summary": (ctypes.c_int, [vp, i32, ctypes.POINTER(RunSummary)]),
             "mbg_batch_probtraj": (ctypes.c_int, [vp, i32, dp, dp]),
             "mbg_batch_probtraj_raw": (ctypes.c_int, [vp, i32, dp, dp]),
+            "mbg_batch_window_probs": (ctypes.c_int, [vp, i32, dp]),
             "mbg_batch_final_states": (ctypes.c_int, [vp, i32, dp]),
             "mbg_batch_fixed_points": (ctypes.c_int, [vp, i32, dp, dp, ctypes.c_size_t,
                                                       ctypes.POINTER(ctypes.c_size_t)]),
@@ -212,11 +213,17 @@ def device_count() -> int:
 class Model:
     """A parsed and compiled .bnd/.cfg model (driver::parse of the reference)."""
 
-    def __init__(self, handle):
+    def __init__(self, handle, like=None):
+        """`like`: a model this one was derived from (rate scales, mutants), whose node names and
+        output nodes it shares; they are copied instead of read through the handle."""
         self._h = handle
         info = ModelInfo()
         _check(lib().mbg_model_info_get(self._h, ctypes.byref(info)))
         self.info = info
+        if like is not None:
+            self.names = list(like.names)
+            self.outputs = list(like.outputs)
+            return
         L = lib()
         self.names = [L.mbg_model_node_name(self._h, i).decode() for i in range(info.nodes)]
         out = np.zeros(max(1, info.outputs), np.int32)
@@ -301,7 +308,7 @@ class Model:
                 raise ValueError("one scale per node")
         h = ctypes.c_void_p()
         _check(lib().mbg_model_with_rate_scales(self._h, _p(u), _p(d), ctypes.byref(h)))
-        return Model(h)
+        return Model(h, like=self)
 
     def with_mutations(self, mutants) -> "Model":
         """Mutant copy: `mutants` maps node names (or indices) to "ON"/"OFF" (or 1/0); each such
@@ -319,7 +326,7 @@ class Model:
         w = np.ascontiguousarray(np.asarray(val, dtype=np.int32))
         h = ctypes.c_void_p()
         _check(lib().mbg_model_with_mutations(self._h, _p(n), _p(w), len(idx), ctypes.byref(h)))
-        return Model(h)
+        return Model(h, like=self)
 
     def layout_check(self):
         """Checks the model's device tables on the host (raises MbgError on an index out of range)."""
@@ -524,6 +531,17 @@ class Batch:
         TH = np.zeros(info.windows, np.float64)
         _check(lib().mbg_batch_probtraj(self._h, int(i), _p(P), _p(TH)))
         return P, TH
+
+    def window_probs(self, window=-1):
+        """One window of every instance (negative: from each instance's last window), gathered on
+        the device: an instances x 2^outputs array when all instances have the same outputs, else a
+        list of per-instance arrays."""
+        sizes = [1 << m.info.outputs for m in self.models]
+        out = np.empty(sum(sizes), np.float64)  # every entry is written
+        _check(lib().mbg_batch_window_probs(self._h, int(window), _p(out)))
+        if len(set(sizes)) <= 1:
+            return out.reshape(len(sizes), sizes[0] if sizes else 0)
+        return np.split(out, np.cumsum(sizes)[:-1])
 
     def probtraj_raw(self, i):
         info = self.models[i].info

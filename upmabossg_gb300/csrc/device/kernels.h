@@ -81,6 +81,15 @@ cudaError_t launch_window_emit(const unsigned long long* hist, const unsigned lo
                                unsigned long long n_bins, const unsigned* bitmap, const unsigned* wpre,
                                const unsigned* chunk, unsigned* out_bin, unsigned long long* out_sum, int sms,
                                cudaStream_t stream);
+// One window of many batched instances: span i copies n u64 sums from src to out + dst. Spans in
+// device memory; max_n the largest n.
+struct WindowSpan {
+    const unsigned long long* src;
+    unsigned long long dst;
+    unsigned long long n;
+};
+cudaError_t launch_window_gather(const WindowSpan* spans, int n_spans, unsigned long long max_n,
+                                 unsigned long long* out, cudaStream_t stream);
 // The same two passes over the dense 2^n_out final-state counts (n_states entries): out_state /
 // out_count get the reached output states in increasing order and their counts. The scratch
 // arrays are those of the window compaction, sized for n_states or more.

@@ -11,6 +11,7 @@
 // and three over the bitmap (windows x 2^n_out / 8 bytes).
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <string>
 
 #include "../../../include/mbg.h"
@@ -251,6 +252,35 @@ cudaError_t launch_window_emit(const unsigned long long* hist, const unsigned lo
                                   out_sum);
     return cudaLaunchKernelEx(&cfg, win_emit_dense<unsigned long long>, hist, window_bitmap_words(n_bins), bitmap,
                               wpre, chunk, out_bin, out_sum);
+}
+
+// ---------------------------------------------------------------------------------------------
+// One window of many batched instances gathered into one array: block (x, y) copies entries
+// x * 256 + threadIdx.x (grid-stride in x) of span y.
+
+namespace {
+
+__global__ void win_gather(const WindowSpan* __restrict__ spans, unsigned long long* __restrict__ out) {
+    const WindowSpan s = spans[blockIdx.y];
+    for (unsigned long long e = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; e < s.n;
+         e += (unsigned long long)gridDim.x * blockDim.x)
+        out[s.dst + e] = s.src[e];
+}
+
+}  // namespace
+
+cudaError_t launch_window_gather(const WindowSpan* spans, int n_spans, unsigned long long max_n,
+                                 unsigned long long* out, cudaStream_t stream) {
+    for (int s0 = 0; s0 < n_spans; s0 += 65535) {
+        cudaLaunchConfig_t cfg = {};
+        cfg.stream = stream;
+        cfg.gridDim = dim3((unsigned)std::min<unsigned long long>((max_n + 255) / 256, 1024ull),
+                           (unsigned)std::min(65535, n_spans - s0));
+        cfg.blockDim = dim3(256);
+        const cudaError_t e = cudaLaunchKernelEx(&cfg, win_gather, spans + s0, out);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
 }
 
 // ---------------------------------------------------------------------------------------------

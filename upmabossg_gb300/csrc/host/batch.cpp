@@ -11,6 +11,7 @@
 #include <cstring>
 
 #include "../device/kernels.h"
+#include "devmem.hpp"
 
 namespace mbg {
 
@@ -606,6 +607,40 @@ void Batch::fetch(int i) {
         ck(cudaMemcpy(x.fp_cnt.data(), x.fp.out_cnt, nu * 4, cudaMemcpyDeviceToHost), "cudaMemcpy D2H");
     }
     x.fetched = true;
+}
+
+void Batch::window_sums(int w, std::vector<uint64_t>& out) {
+    if (!ran) throw StateError("results requested before mbg_batch_run");
+    ck(cudaSetDevice(device), "cudaSetDevice");
+    std::vector<WindowSpan> spans(inst.size());
+    uint64_t total = 0, max_n = 0;
+    for (size_t i = 0; i < inst.size(); ++i) {
+        const Inst& x = inst[i];
+        const int wi = w < 0 ? x.cm.windows + w : w;
+        if (wi < 0 || wi >= x.cm.windows)
+            throw ArgError("window " + std::to_string(w) + " out of range for instance " + std::to_string(i));
+        const uint64_t S = 1ull << x.cm.n_out;
+        spans[i] = WindowSpan{x.prm.hist + (size_t)wi * S, total, S};
+        total += S;
+        max_n = std::max(max_n, S);
+    }
+    out.resize(total);
+    if (spans.empty()) return;
+    struct Blocks {  // returned to the block cache however the gather ends (the copies are synchronous)
+        void* spans = nullptr;
+        void* sums = nullptr;
+        ~Blocks() {
+            dev_free(spans);
+            dev_free(sums);
+        }
+    } b;
+    b.spans = dev_alloc(spans.size() * sizeof(WindowSpan), "window spans");
+    b.sums = dev_alloc(total * 8, "gathered window sums");
+    ck(cudaMemcpy(b.spans, spans.data(), spans.size() * sizeof(WindowSpan), cudaMemcpyHostToDevice), "cudaMemcpy H2D");
+    ck(launch_window_gather(static_cast<const WindowSpan*>(b.spans), (int)spans.size(), max_n,
+                            static_cast<unsigned long long*>(b.sums), nullptr),
+       "window gather");
+    ck(cudaMemcpy(out.data(), b.sums, total * 8, cudaMemcpyDeviceToHost), "cudaMemcpy D2H");
 }
 
 }  // namespace mbg

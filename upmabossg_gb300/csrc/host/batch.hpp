@@ -62,6 +62,9 @@ public:
     void autotune();
     void run(cudaStream_t stream);
     void fetch(int i);
+    // Window w (w < 0: counted from each instance's last window) of every instance, gathered on the
+    // device into one array: instance i's 2^outputs sums after those of the instances before it.
+    void window_sums(int w, std::vector<uint64_t>& out);
 
     std::vector<Inst> inst;
     std::vector<Class> classes;

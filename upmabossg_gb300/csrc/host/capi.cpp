@@ -533,6 +533,23 @@ mbg_status mbg_batch_probtraj(mbg_batch* b, int32_t i, double* probs, double* tr
     });
 }
 
+mbg_status mbg_batch_window_probs(mbg_batch* b, int32_t window, double* probs) {
+    if (!b || !probs) return fail(MBG_ERR_ARG, "null argument");
+    return guard([&] {
+        std::vector<uint64_t> sums;
+        b->batch.window_sums(window, sums);
+        size_t o = 0;
+        for (const mbg::Batch::Inst& x : b->batch.inst) {
+            const size_t S = (size_t)1 << x.cm.n_out;
+            const double n = (double)x.n_traj, tick = x.cm.tick;
+            // mbg_batch_probtraj's arithmetic
+            for (size_t k = 0; k < S; ++k)
+                probs[o + k] = x.cm.discrete ? (double)sums[o + k] / n : ((double)sums[o + k] / 4294967296.0) / (n * tick);
+            o += S;
+        }
+    });
+}
+
 mbg_status mbg_batch_probtraj_raw(mbg_batch* b, int32_t i, uint64_t* sums, uint64_t* th_sums) {
     if (!b) return fail(MBG_ERR_ARG, "null batch");
     return guard([&] {

@@ -67,9 +67,7 @@ class PointSimulator:
             s = batch.summary()
             self.stats.device_ms += s["sim_ms"]
             self.stats.transitions += s["transitions"]
-            for j in range(len(models)):
-                P, _ = batch.probtraj(j)
-                out[c0 + j] = P[-1]
+            out[sl] = batch.window_probs(-1)
             batch.close()
             for m in models:
                 m.close()
