@@ -30,13 +30,10 @@ struct Layout {
     }
 };
 
+// Device blocks come from the process-wide block cache (devmem.hpp): a sweep that creates one batch
+// after another of the same shape reuses the blocks instead of allocating and freeing them.
 void* dmalloc(size_t bytes, std::vector<void*>& owned) {
-    void* p = nullptr;
-    cudaError_t e = cudaMalloc(&p, bytes ? bytes : 1);
-    if (e != cudaSuccess) {
-        cudaGetLastError();
-        throw NoMemError("cudaMalloc of " + std::to_string(bytes) + " bytes: " + cudaGetErrorString(e));
-    }
+    void* p = dev_alloc(bytes, "batch arena");
     owned.push_back(p);
     return p;
 }
@@ -67,11 +64,13 @@ Batch::~Batch() {
         for (cudaEvent_t e : {k.e0, k.e1, k.join})
             if (e) cudaEventDestroy(e);
         if (k.stream) cudaStreamDestroy(k.stream);
-        if (k.lane_buf) cudaFree(k.lane_buf);
     }
     if (fork) cudaEventDestroy(fork);
-    if (small_host) cudaFreeHost(small_host);
-    for (void* p : owned) cudaFree(p);
+    // the blocks go back to the cache: nothing of this batch may still run on them
+    cudaDeviceSynchronize();
+    for (Class& k : classes) dev_free(k.lane_buf);
+    pinned_free(small_host);
+    for (void* p : owned) dev_free(p);
 }
 
 void Batch::create(const std::vector<const CompiledModel*>& models, const std::vector<uint64_t>& n_traj,
@@ -200,7 +199,7 @@ void Batch::create(const std::vector<const CompiledModel*>& models, const std::v
     rep_bytes = pl.size;
     char* fpa = static_cast<char*>(dmalloc(fl.size, owned));
     small_dev = res + small_off;
-    ck(cudaMallocHost((void**)&small_host, small_bytes), "cudaMallocHost");
+    small_host = static_cast<char*>(pinned_alloc(small_bytes));
 
     std::vector<SimParams> prms(n);
     std::vector<FpSlots> fps(n);
@@ -321,15 +320,13 @@ void Batch::configure(int c, int lay, int blk, bool variant) {
         const size_t block_bytes = (sim_lane_smem(k.max_n, blk) + 255) & ~(size_t)255;
         const size_t need = block_bytes * (size_t)sms * (size_t)bps;
         if (need > k.lane_buf_bytes) {
-            if (k.lane_buf) cudaFree(k.lane_buf);
+            if (k.lane_buf) {
+                cudaDeviceSynchronize();  // a pilot may still run on the old rows
+                dev_free(k.lane_buf);
+            }
             k.lane_buf = nullptr;
             k.lane_buf_bytes = 0;
-            cudaError_t e = cudaMalloc(&k.lane_buf, need);
-            if (e != cudaSuccess) {
-                k.lane_buf = nullptr;
-                cudaGetLastError();
-                throw NoMemError("cudaMalloc of " + std::to_string(need) + " bytes: " + cudaGetErrorString(e));
-            }
+            k.lane_buf = dev_alloc(need, "batch lane rows");
             k.lane_buf_bytes = need;
         }
         for (BatchDesc* d : {&k.desc, &k.pilot, &k.pilot_long}) {
