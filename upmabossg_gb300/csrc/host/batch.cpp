@@ -12,6 +12,7 @@
 
 #include "../device/kernels.h"
 #include "devmem.hpp"
+#include "parallel.hpp"
 
 namespace mbg {
 
@@ -101,18 +102,24 @@ void Batch::create(const std::vector<const CompiledModel*>& models, const std::v
     std::vector<Class> all(kClasses);
     for (size_t i = 0; i < n; ++i) {
         Inst& x = inst[i];
-        x.cm = *models[i];
-        x.n_traj = n_traj.empty() || n_traj[i] == 0 ? x.cm.sample_count : n_traj[i];
-        x.seed = seeds.empty() ? x.cm.seed : seeds[i];
-        check_model_limits(x.cm, x.n_traj);
-        if (x.cm.n_out > 32) throw ModelError("batched instances support at most 32 outputs");
-        Class& k = all[batch_size_class(x.cm.n)];
+        const CompiledModel& cm = *models[i];
+        x.n_traj = n_traj.empty() || n_traj[i] == 0 ? cm.sample_count : n_traj[i];
+        x.seed = seeds.empty() ? cm.seed : seeds[i];
+        if (cm.n_out > 32) throw ModelError("batched instances support at most 32 outputs");
+        Class& k = all[batch_size_class(cm.n)];
         k.members.push_back((int)i);
-        k.max_n = std::max(k.max_n, x.cm.n);
-        for (const auto& nd : x.cm.nodes) k.full |= nd.kind == NODE_PALETTE;
-        k.full |= x.cm.max_k > 12;
+        k.max_n = std::max(k.max_n, cm.n);
+        for (const auto& nd : cm.nodes) k.full |= nd.kind == NODE_PALETTE;
+        k.full |= cm.max_k > 12;
         k.traj += x.n_traj;
     }
+    // every instance's model copy and device layout (host work, independent per instance)
+    std::vector<DeviceLayout> dls(n);
+    parallel_items<int>((int)n, 64, [&](int i, int&) {
+        inst[i].cm = *models[i];
+        dls[i] = layout_model(inst[i].cm);
+        check_layout(inst[i].cm, dls[i]);
+    });
     for (Class& k : all)
         if (!k.members.empty()) classes.push_back(std::move(k));
     std::vector<int> order;  // class order -> instance
@@ -124,7 +131,6 @@ void Batch::create(const std::vector<const CompiledModel*>& models, const std::v
         }
     }
 
-    std::vector<DeviceLayout> dls(n);
     Layout ml, rl, pl, fl;
     struct Off {
         size_t nodes, lnodes, lwide, regs, tabs, pidx, palette, dep_off, deps, out_nodes, out_pos, istate;
@@ -135,8 +141,6 @@ void Batch::create(const std::vector<const CompiledModel*>& models, const std::v
         Inst& x = inst[i];
         const CompiledModel& cm = x.cm;
         total_traj += x.n_traj;
-        dls[i] = layout_model(cm);
-        check_layout(cm, dls[i]);
         const DeviceLayout& d = dls[i];
         Off& f = off[i];
         f.nodes = ml.add(d.nodes.size() * sizeof(DevNode));

@@ -15,6 +15,7 @@
 #include <set>
 
 #include "model.hpp"
+#include "parallel.hpp"
 
 namespace mbg {
 
@@ -662,41 +663,6 @@ CompiledModel compile_arrays(int n, const int32_t* reg_off, const int32_t* regs,
     return cm;
 }
 
-namespace {
-
-// f(i, scratch) for every node i in [0, n) on up to 16 host threads (one thread for small models),
-// each thread with its own value-initialised Scratch. An exception in f is rethrown here: the one of
-// the lowest-numbered node when several nodes fail, as a single thread would have thrown it.
-template <class Scratch, class F>
-void parallel_nodes(int n, F&& f) {
-    const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
-    const int threads = n < 256 ? 1 : (int)std::min<unsigned>(hw, 16u);
-    std::atomic<int> next{0};
-    std::mutex mu;
-    int err_node = n;
-    std::exception_ptr err;
-    auto worker = [&]() {
-        Scratch sc{};
-        for (int i; (i = next.fetch_add(1)) < n;) {
-            try {
-                f(i, sc);
-            } catch (...) {
-                std::lock_guard<std::mutex> lock(mu);
-                if (i < err_node) {
-                    err_node = i;
-                    err = std::current_exception();
-                }
-            }
-        }
-    };
-    std::vector<std::thread> pool;
-    for (int t = 1; t < threads; ++t) pool.emplace_back(worker);
-    worker();
-    for (auto& th : pool) th.join();
-    if (err) std::rethrow_exception(err);
-}
-
-}  // namespace
 
 CompiledModel compile_model(const Model& m) {
     CompiledModel cm;
@@ -780,7 +746,7 @@ CompiledModel compile_model(const Model& m) {
         }
         node_max[i] = mx;
     };
-    parallel_nodes<Scratch>(cm.n, [&](int i, Scratch& sc) { tabulate(i, sc); });
+    parallel_items<Scratch>(cm.n, 256, [&](int i, Scratch& sc) { tabulate(i, sc); });
     double sum_max = 0;
     for (int i = 0; i < cm.n; ++i) {
         sum_max += node_max[i];  // node order, as one thread would add them
@@ -790,7 +756,7 @@ CompiledModel compile_model(const Model& m) {
     const int fb = frac_bits_for(sum_max);
     cm.frac_bits = fb;
 
-    parallel_nodes<int>(cm.n, [&](int i, int&) { classify_node(cm.nodes[i], tabs[i], fb, m.nodes[i].name); });
+    parallel_items<int>(cm.n, 256, [&](int i, int&) { classify_node(cm.nodes[i], tabs[i], fb, m.nodes[i].name); });
 
     cm.deps.assign(cm.n, {});
     for (int i = 0; i < cm.n; ++i) {
