@@ -268,13 +268,17 @@ typedef struct {
     int32_t layout;        /* 0: autotuned per class (without autotune: lane where it fits);
                               MBG_LAYOUT_LANE, MBG_LAYOUT_LANE_GLOBAL or MBG_LAYOUT_WARP: that
                               layout for every class (global rows: per-lane reader update) */
+    int32_t lane_variant;  /* lane layout without autotune: 0 per-lane reader update (default),
+                              1 cooperative, 2 per-lane with the active-node words in global
+                              memory (mbg_sim_opts::lane_update 2) */
 } mbg_batch_opts;
 
 /* One launch shape the autotuner timed for a class. */
 typedef struct {
     int32_t layout;        /* MBG_LAYOUT_LANE, MBG_LAYOUT_LANE_GLOBAL or MBG_LAYOUT_WARP */
     int32_t block_size;
-    int32_t variant;       /* lane: 1 cooperative reader update; warp: 1 regulator-index cache */
+    int32_t variant;       /* lane: 0 per-lane reader update, 1 cooperative, 2 per-lane with the
+                              active-node words in global memory; warp: 1 regulator-index cache */
     int32_t reserved;
     double kernel_ms;      /* pilot kernel time */
 } mbg_batch_class_timing;

@@ -79,6 +79,26 @@ def test_batch_shape_does_not_change_results(layout, block):
         assert np.array_equal(fa, fb) and np.array_equal(pa, pb)
 
 
+@pytest.mark.parametrize("block", [128, 256])
+def test_split_rows_variant_matches(block):
+    """Lane variant 2 (active words in global memory; the `_full` kernel for the class holding
+    the multi-valued-rate instance) gives the default batch's results bit for bit."""
+    texts = instances()
+    models = [mbg.Model.from_strings(b, c) for b, c in texts]
+    ref = mbg.Batch(models, n_traj=[1200] * len(models), seeds=list(range(len(models)))).run()
+    other = mbg.Batch(models, n_traj=[1200] * len(models), seeds=list(range(len(models))), layout=mbg.LAYOUT_LANE,
+                      block_size=block, lane_variant=2).run()
+    assert all(k["layout"] == "lane" and k["variant"] == 2 for k in other.classes())
+    assert all(other.summary(i)["lane_update"] == 2 for i in range(len(models)))
+    for i in range(len(models)):
+        assert np.array_equal(ref.probtraj_raw(i)[0], other.probtraj_raw(i)[0])
+        assert np.array_equal(ref.final_states(i), other.final_states(i))
+        fa, pa = ref.fixed_points(i)
+        fb, pb = other.fixed_points(i)
+        assert np.array_equal(fa, fb) and np.array_equal(pa, pb)
+        assert ref.summary(i)["transitions"] == other.summary(i)["transitions"]
+
+
 def test_size_classes():
     """Instances are grouped by node count (<= 32, 64, ..., 4096, larger), one launch each."""
     texts = instances()

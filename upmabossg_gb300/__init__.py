@@ -42,7 +42,8 @@ EXPORTS = (
 
 class BatchOpts(ctypes.Structure):
     _fields_ = [("device", ctypes.c_int32), ("max_steps", ctypes.c_uint32), ("block_size", ctypes.c_int32),
-                ("blocks_per_sm", ctypes.c_int32), ("autotune", ctypes.c_int32), ("layout", ctypes.c_int32)]
+                ("blocks_per_sm", ctypes.c_int32), ("autotune", ctypes.c_int32), ("layout", ctypes.c_int32),
+                ("lane_variant", ctypes.c_int32)]
 
 
 class BatchClassTiming(ctypes.Structure):
@@ -477,12 +478,13 @@ class Batch:
     """Many instances (models, trajectory counts, seeds) run in one graph-captured launch."""
 
     def __init__(self, models, n_traj=None, seeds=None, device=0, max_steps=0, block_size=0, blocks_per_sm=0,
-                 autotune=False, layout=0):
+                 autotune=False, layout=0, lane_variant=0):
         o = BatchOpts()
         lib().mbg_batch_opts_default(ctypes.byref(o))
         o.device, o.max_steps, o.block_size, o.blocks_per_sm = device, max_steps, block_size, blocks_per_sm
         o.autotune = 1 if autotune else 0
         o.layout = layout
+        o.lane_variant = lane_variant
         self.models = list(models)
         handles = (ctypes.c_void_p * len(self.models))(*[m._h for m in self.models])
         nt = None if n_traj is None else np.ascontiguousarray(np.asarray(n_traj, dtype=np.uint64))

@@ -34,11 +34,16 @@ size_t sim_lane_split_smem(int n, int block);
 cudaError_t sim_lane_split_configure(bool full, size_t smem, int block, int* blocks_per_sm);
 cudaError_t launch_sim_lane_split(const SimParams& p, bool full, int grid, int block, size_t smem,
                                   cudaStream_t stream);
+// The batched form (BatchDesc::lane_state); sim_kernel_limits numbers it 9 (variant: `_full`).
+cudaError_t sim_lane_batch_split_configure(bool full, size_t smem, int block, int* blocks_per_sm);
+cudaError_t launch_sim_lane_batch_split(const BatchDesc& b, bool full, int grid, int block, size_t smem,
+                                        cudaStream_t stream);
 int sim_lane_rows(int n);                 // BatchDesc::rows for models of up to n nodes
 // Re-applies the attributes of a simulation kernel for the launch shapes that are about to use it
 // (kernel 0: mbg_sim_lane[_coop], 1: mbg_sim_lane_batch[_coop], 2: mbg_sim_warp_batch[_gather],
 // 3: mbg_sim_warp[_gather], 4: mbg_sim_lane[_coop]_full, 5: mbg_sim_lane_batch[_coop]_full,
-// 6: mbg_sim_lane_global[_full], 7: mbg_sim_lane_batch_global[_full], 8: mbg_sim_lane_split[_full];
+// 6: mbg_sim_lane_global[_full], 7: mbg_sim_lane_batch_global[_full], 8: mbg_sim_lane_split[_full],
+// 9: mbg_sim_lane_batch_split[_full];
 // variant selects the second name; hash: the window-hash twin of kernel 0, 4, 6 or 8): kernel attributes
 // are process-wide, so another handle may have changed them since this one was configured.
 cudaError_t sim_kernel_limits(int kernel, bool variant, const int* blocks, const size_t* smems, const int* want,

@@ -105,6 +105,21 @@ extern "C" __global__ void __launch_bounds__(256, 3) mbg_sim_lane_batch_coop_ful
     sim_lane_batch_body<true, true>(b, smem);
 }
 
+// Batched instances in the lane layout with the active-word rows in global memory (per-lane reader
+// update), as mbg_sim_lane_split: for size classes whose shared-memory rows hold fewer than three
+// blocks of 256 per SM.
+extern "C" __global__ void __launch_bounds__(256, 3) mbg_sim_lane_batch_split(const BatchDesc b) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    sim_lane_batch_body<false, false>(b, smem,
+                                      reinterpret_cast<unsigned*>(b.lane_state + (size_t)blockIdx.x * b.lane_block_bytes));
+}
+
+extern "C" __global__ void __launch_bounds__(256, 3) mbg_sim_lane_batch_split_full(const BatchDesc b) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    sim_lane_batch_body<false, true>(b, smem,
+                                     reinterpret_cast<unsigned*>(b.lane_state + (size_t)blockIdx.x * b.lane_block_bytes));
+}
+
 // Batched instances in the lane layout with each block's rows in global memory (per-lane reader
 // update): for size classes whose rows leave few trajectories resident in shared memory.
 extern "C" __global__ void __launch_bounds__(256, 3) mbg_sim_lane_batch_global(const BatchDesc b) {
@@ -374,6 +389,7 @@ cudaError_t sim_kernel_limits(int kernel, bool variant, const int* blocks, const
         case 6: f = variant ? (const void*)mbg_sim_lane_global_full : (const void*)mbg_sim_lane_global; break;
         case 7: f = variant ? (const void*)mbg_sim_lane_batch_global_full : (const void*)mbg_sim_lane_batch_global; break;
         case 8: f = variant ? (const void*)mbg_sim_lane_split_full : (const void*)mbg_sim_lane_split; break;
+        case 9: f = variant ? (const void*)mbg_sim_lane_batch_split_full : (const void*)mbg_sim_lane_batch_split; break;
         default: f = variant ? (const void*)mbg_sim_warp : (const void*)mbg_sim_warp_gather; break;
     }
     return shared_limits(f, blocks, smems, want, count);
@@ -429,6 +445,16 @@ int sim_lane_rows(int n) { return lane_groups(n); }
 size_t sim_lane_split_smem(int n, int block) {
     const int G = lane_groups(n);
     return (size_t)block * (8u * (unsigned)lane_leaves(G, lane_leaf_shift(G)) + 4u * (unsigned)G);
+}
+
+cudaError_t sim_lane_batch_split_configure(bool full, size_t smem, int block, int* blocks_per_sm) {
+    return lane_configure(full ? (const void*)mbg_sim_lane_batch_split_full : (const void*)mbg_sim_lane_batch_split,
+                          smem, block, blocks_per_sm);
+}
+
+cudaError_t launch_sim_lane_batch_split(const BatchDesc& b, bool full, int grid, int block, size_t smem,
+                                        cudaStream_t stream) {
+    return launch(full ? mbg_sim_lane_batch_split_full : mbg_sim_lane_batch_split, grid, block, smem, stream, b);
 }
 
 cudaError_t sim_lane_split_configure(bool full, size_t smem, int block, int* blocks_per_sm) {

@@ -643,11 +643,11 @@ __device__ void sim_lane_body(const SimParams& p, unsigned char* smem, unsigned*
 // counts to that instance's counters when it moves to another instance. Shared memory has rows
 // for the largest instance of the launch (b.rows groups).
 template <bool COOP, bool FULL>
-__device__ void sim_lane_batch_body(const BatchDesc& b, unsigned char* smem) {
+__device__ void sim_lane_batch_body(const BatchDesc& b, unsigned char* smem, unsigned* act_rows = nullptr) {
     const int T = (int)blockDim.x;
     const unsigned lane = threadIdx.x & 31u;
     const int wbase = (int)(threadIdx.x & ~31u);
-    const LaneSmem m = lane_smem_at(smem, b.rows, T);
+    const LaneSmem m = lane_smem_at(smem, b.rows, T, act_rows);
     const int col = (int)threadIdx.x;
     const unsigned long long items = __ldg(b.prefix + b.n_inst);
     const SimParams* pp = b.params;

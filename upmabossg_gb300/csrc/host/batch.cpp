@@ -82,6 +82,7 @@ void Batch::create(const std::vector<const CompiledModel*>& models, const std::v
     if (o.layout != 0 && o.layout != MBG_LAYOUT_LANE && o.layout != MBG_LAYOUT_WARP &&
         o.layout != MBG_LAYOUT_LANE_GLOBAL)
         throw ArgError("batch layout must be 0 (auto), MBG_LAYOUT_LANE, MBG_LAYOUT_LANE_GLOBAL or MBG_LAYOUT_WARP");
+    if (o.lane_variant < 0 || o.lane_variant > 2) throw ArgError("lane_variant must be 0, 1 or 2");
     opts = o;
     for (size_t i = 0; i < models.size(); ++i)  // argument checks come before any device call
         check_model_limits(*models[i], n_traj.empty() || n_traj[i] == 0 ? models[i]->sample_count : n_traj[i]);
@@ -300,28 +301,46 @@ void Batch::create(const std::vector<const CompiledModel*>& models, const std::v
         const int lay = o.layout ? o.layout : (lane_fits ? MBG_LAYOUT_LANE : MBG_LAYOUT_WARP);
         if (lay == MBG_LAYOUT_LANE && !lane_fits)
             throw ModelError("largest instance of a size class too large for the batched lane layout");
-        const bool variant =
-            lay == MBG_LAYOUT_WARP && (size_t)(blk / 32) * sim_warp_batch_slice_bytes(k.max_n, true) <= 100 * 1024;
+        const int variant =
+            lay == MBG_LAYOUT_WARP ? ((size_t)(blk / 32) * sim_warp_batch_slice_bytes(k.max_n, true) <= 100 * 1024)
+            : lay == MBG_LAYOUT_LANE ? o.lane_variant : 0;
         configure((int)c, lay, blk, variant);
     }
     build_graph();
 }
 
-void Batch::configure(int c, int lay, int blk, bool variant) {
+void Batch::configure(int c, int lay, int blk, int variant) {
     Class& k = classes[c];
+    if (variant < 0 || variant > 2 || (lay != MBG_LAYOUT_LANE && variant > 1))
+        throw ArgError("batched lane variant must be 0, 1 or 2");
     int bps = 0;
     size_t sm = 0;
-    if (lay == MBG_LAYOUT_LANE) {
+    size_t row_bytes = 0;  // per block, in global memory
+    if (lay == MBG_LAYOUT_LANE && variant == 2) {
+        sm = sim_lane_split_smem(k.max_n, blk);
+        if (sm > kSmemLimit) throw ModelError("largest instance of a size class too large for the batched lane layout");
+        ck(sim_lane_batch_split_configure(k.full, sm, blk, &bps), "batched lane kernel occupancy");
+        row_bytes = (size_t)sim_lane_rows(k.max_n) * 4 * (size_t)blk;  // the active words
+    } else if (lay == MBG_LAYOUT_LANE) {
         sm = sim_lane_smem(k.max_n, blk);
         if (sm > kSmemLimit) throw ModelError("largest instance of a size class too large for the batched lane layout");
-        ck(sim_lane_batch_configure(variant, k.full, sm, blk, &bps), "batched lane kernel occupancy");
+        ck(sim_lane_batch_configure(variant == 1, k.full, sm, blk, &bps), "batched lane kernel occupancy");
     } else if (lay == MBG_LAYOUT_LANE_GLOBAL) {
-        variant = false;  // per-lane reader update only
+        variant = 0;  // per-lane reader update only
         ck(sim_lane_batch_global_configure(k.full, blk, &bps), "batched global-row lane kernel occupancy");
+        row_bytes = sim_lane_smem(k.max_n, blk);  // every row
+    } else {
+        const unsigned slice = sim_warp_batch_slice_bytes(k.max_n, variant != 0);
+        sm = (size_t)(blk / 32) * slice;
+        if (sm > kSmemLimit) throw ModelError("largest instance of a size class too large for the batched warp layout");
+        ck(sim_warp_batch_configure(variant != 0, sm, blk, &bps), "batched warp kernel occupancy");
+        k.desc.slice_bytes = k.pilot.slice_bytes = slice;
+    }
+    if (row_bytes) {
         if (bps < 1) throw CudaError("batched kernel cannot be resident with this block size");
         if (opts.blocks_per_sm > 0) bps = std::min(bps, (int)opts.blocks_per_sm);
         // one share of rows per resident block, 256-byte aligned
-        const size_t block_bytes = (sim_lane_smem(k.max_n, blk) + 255) & ~(size_t)255;
+        const size_t block_bytes = (row_bytes + 255) & ~(size_t)255;
         const size_t need = block_bytes * (size_t)sms * (size_t)bps;
         if (need > k.lane_buf_bytes) {
             if (k.lane_buf) {
@@ -337,12 +356,6 @@ void Batch::configure(int c, int lay, int blk, bool variant) {
             d->lane_state = static_cast<unsigned char*>(k.lane_buf);
             d->lane_block_bytes = block_bytes;
         }
-    } else {
-        const unsigned slice = sim_warp_batch_slice_bytes(k.max_n, variant);
-        sm = (size_t)(blk / 32) * slice;
-        if (sm > kSmemLimit) throw ModelError("largest instance of a size class too large for the batched warp layout");
-        ck(sim_warp_batch_configure(variant, sm, blk, &bps), "batched warp kernel occupancy");
-        k.desc.slice_bytes = k.pilot.slice_bytes = slice;
     }
     if (bps < 1) throw CudaError("batched kernel cannot be resident with this block size");
     if (opts.blocks_per_sm > 0) bps = std::min(bps, (int)opts.blocks_per_sm);
@@ -354,7 +367,10 @@ void Batch::configure(int c, int lay, int blk, bool variant) {
 }
 
 cudaError_t Batch::launch_class(const Class& k, const BatchDesc& d, cudaStream_t s) const {
-    if (k.layout == MBG_LAYOUT_LANE) return launch_sim_lane_batch(d, k.variant, k.full, k.grid, k.block, k.smem, s);
+    if (k.layout == MBG_LAYOUT_LANE && k.variant == 2)
+        return launch_sim_lane_batch_split(d, k.full, k.grid, k.block, k.smem, s);
+    if (k.layout == MBG_LAYOUT_LANE)
+        return launch_sim_lane_batch(d, k.variant == 1, k.full, k.grid, k.block, k.smem, s);
     if (k.layout == MBG_LAYOUT_LANE_GLOBAL) return launch_sim_lane_batch_global(d, k.full, k.grid, k.block, s);
     return launch_sim_warp_batch(d, k.variant, k.grid, k.block, k.smem, s);
 }
@@ -410,23 +426,30 @@ void Batch::autotune() {
         k.timings.clear();
         double best = -1;
         int best_lay = k.layout, best_blk = k.block;
-        bool best_var = k.variant;
+        int best_var = k.variant;
         // global rows only where shared memory holds fewer than 512 of a class's trajectories
         // per SM (rows over 454 B: above 1184 nodes); below that the shared-memory lane layout is
         // faster
         const bool try_global = opts.layout == MBG_LAYOUT_LANE_GLOBAL || sim_lane_smem(k.max_n, 512) > kSmemLimit;
+        // the active words in global memory (lane variant 2) only where the shared-memory rows hold
+        // fewer than three blocks of 256 per SM (the register limit of the batched lane kernels)
+        const bool try_split = sim_lane_smem(k.max_n, 768) > kSmemLimit;
         for (int lay : {MBG_LAYOUT_LANE, MBG_LAYOUT_WARP, MBG_LAYOUT_LANE_GLOBAL}) {
             if (opts.layout && lay != opts.layout) continue;
             if (lay == MBG_LAYOUT_LANE_GLOBAL && !try_global) continue;
             for (int blk : {64, 128, 256}) {
                 if (opts.block_size > 0 && blk != opts.block_size) continue;
-                for (int var = 0; var < 2; ++var) {
+                for (int var = 0; var < 3; ++var) {
                     if (lay == MBG_LAYOUT_LANE_GLOBAL && (var || blk == 64)) continue;
-                    if (lay == MBG_LAYOUT_LANE && sim_lane_smem(k.max_n, blk) > kSmemLimit) continue;
+                    if (lay == MBG_LAYOUT_WARP && var == 2) continue;
+                    if (lay == MBG_LAYOUT_LANE && var < 2 && sim_lane_smem(k.max_n, blk) > kSmemLimit) continue;
+                    if (lay == MBG_LAYOUT_LANE && var == 2 &&
+                        (!try_split || blk == 64 || sim_lane_split_smem(k.max_n, blk) > kSmemLimit))
+                        continue;
                     if (lay == MBG_LAYOUT_WARP &&
                         (size_t)(blk / 32) * sim_warp_batch_slice_bytes(k.max_n, var != 0) > 100 * 1024)
                         continue;
-                    configure((int)c, lay, blk, var != 0);
+                    configure((int)c, lay, blk, var);
                     float ms = 0.f;
                     for (int rep = 0; rep < 2; ++rep) {
                         ck(cudaMemsetAsync(k.desc.work, 0, 8, s), "cudaMemsetAsync");
@@ -444,7 +467,7 @@ void Batch::autotune() {
                         best = ms;
                         best_lay = lay;
                         best_blk = blk;
-                        best_var = var != 0;
+                        best_var = var;
                     }
                 }
             }
@@ -469,7 +492,7 @@ void Batch::autotune() {
             best = -1;
             for (size_t i : pick) {
                 const mbg_batch_class_timing& t = order[i];
-                configure((int)c, t.layout, t.block_size, t.variant != 0);
+                configure((int)c, t.layout, t.block_size, t.variant);
                 float ms = 0.f;
                 ck(cudaMemsetAsync(k.desc.work, 0, 8, s), "cudaMemsetAsync");
                 ck(cudaEventRecord(ev0, s), "cudaEventRecord");
@@ -484,7 +507,7 @@ void Batch::autotune() {
                     best = ms;
                     best_lay = t.layout;
                     best_blk = t.block_size;
-                    best_var = t.variant != 0;
+                    best_var = t.variant;
                 }
             }
         }
@@ -499,13 +522,15 @@ void Batch::apply_limits() {
     // every class's resident blocks; kernel attributes are process-wide, so they are re-applied
     // before each launch of the graph
     // kernel numbers of sim_kernel_limits: 1 / 5 batched lane (plain / `_full`, variant: cooperative
-    // update), 2 batched warp, 7 batched lane with global rows (variant: `_full`)
+    // update), 2 batched warp, 7 batched lane with global rows and 9 with global active words
+    // (variant: `_full`)
     auto kernel_of = [](const Class& k) -> std::pair<int, int> {
-        if (k.layout == MBG_LAYOUT_LANE) return {k.full ? 5 : 1, k.variant ? 1 : 0};
+        if (k.layout == MBG_LAYOUT_LANE && k.variant == 2) return {9, k.full ? 1 : 0};
+        if (k.layout == MBG_LAYOUT_LANE) return {k.full ? 5 : 1, k.variant == 1 ? 1 : 0};
         if (k.layout == MBG_LAYOUT_LANE_GLOBAL) return {7, k.full ? 1 : 0};
         return {2, k.variant ? 1 : 0};
     };
-    for (int kern : {1, 2, 5, 7}) {
+    for (int kern : {1, 2, 5, 7, 9}) {
         for (int var = 0; var < 2; ++var) {
             std::vector<int> blocks, want;
             std::vector<size_t> smems;
@@ -563,7 +588,9 @@ void Batch::run(cudaStream_t stream) {
         r.layout = k.layout;
         r.block_size = k.block;
         r.grid_size = k.grid;
-        r.lane_update = (k.layout == MBG_LAYOUT_LANE && !k.variant) || k.layout == MBG_LAYOUT_LANE_GLOBAL ? 1 : 0;
+        // as mbg_sim_opts::lane_update: 0 cooperative, 1 per-lane, 2 per-lane with global active words
+        r.lane_update = k.layout == MBG_LAYOUT_LANE ? (k.variant == 2 ? 2 : k.variant == 1 ? 0 : 1)
+                        : k.layout == MBG_LAYOUT_LANE_GLOBAL ? 1 : 0;
         r.kernel_ms = k.kernel_ms;
         summary.trajectories += r.trajectories;
         summary.transitions += r.transitions;

@@ -42,10 +42,12 @@ public:
         bool has_long = false;              // pilot_long covers more than the pilot
         int layout = MBG_LAYOUT_LANE;       // MBG_LAYOUT_LANE, MBG_LAYOUT_LANE_GLOBAL or MBG_LAYOUT_WARP
         int block = 128;
-        bool variant = false;               // lane: cooperative reader update; warp: regulator index cache
+        int variant = 0;                    // lane: 0 per-lane reader update, 1 cooperative, 2 per-lane with
+                                            // the active words in global memory; warp: 1 regulator index cache
         size_t smem = 0;
         int grid = 0;
-        void* lane_buf = nullptr;           // global rows of the resident blocks (MBG_LAYOUT_LANE_GLOBAL)
+        void* lane_buf = nullptr;           // global rows (MBG_LAYOUT_LANE_GLOBAL) or active-word rows (lane
+                                            // variant 2) of the resident blocks
         size_t lane_buf_bytes = 0;
         cudaEvent_t e0 = nullptr, e1 = nullptr;
         cudaStream_t stream = nullptr;      // the class's branch of the graph
@@ -58,7 +60,7 @@ public:
     void create(const std::vector<const CompiledModel*>& models, const std::vector<uint64_t>& n_traj,
                 const std::vector<uint64_t>& seeds, const mbg_batch_opts& o);
     // Launch shape of class c (no graph rebuild).
-    void configure(int c, int layout, int block, bool variant);
+    void configure(int c, int layout, int block, int variant);
     void autotune();
     void run(cudaStream_t stream);
     void fetch(int i);

@@ -684,7 +684,7 @@ mbg_status mbg_batch_class(const mbg_batch* b, int32_t c, mbg_batch_class_info* 
     out->trajectories = k.traj;
     out->layout = k.layout;
     out->block_size = k.block;
-    out->variant = k.variant ? 1 : 0;
+    out->variant = k.variant;
     out->grid = k.grid;
     out->kernel_ms = k.kernel_ms;
     out->timings = (int32_t)k.timings.size();
