@@ -262,29 +262,39 @@ SURROGATE_DESC = ("200-node network (2-3 regulators, rates 1) with 32 rate block
 
 
 def measure_surrogate(n_train=20000, n_traj=10000, n_cand=1_000_000, epochs=120, batch=64, seed=7, n_recall=10000,
-                      with_gemm=True):
+                      with_gemm=True, label_traj=None):
     """Sweep points/s of surrogate-screened versus plain batched simulation, with the TV error of
-    the surrogate against re-simulation of every reported point."""
+    the surrogate against re-simulation of every reported point. Training labels are simulated
+    with `label_traj` trajectories per point (default n_traj); the plain method, the held-out
+    points, the recall subsample and every re-simulation use n_traj."""
     import numpy as np
 
     import upmabossg_gb300 as mbg
     from upmabossg_gb300 import screen, synth
+    label_traj = label_traj or n_traj
     space = synth.surrogate_space()
     base = mbg.Model.from_strings(space.base.bnd(), space.base.cfg())
     sim = screen.PointSimulator(base, space.blocks, n_traj=n_traj, chunk=1024)
+    label_sim = sim if label_traj == n_traj else screen.PointSimulator(base, space.blocks, n_traj=label_traj,
+                                                                         chunk=1024, seed=3)
     rng = np.random.default_rng(seed)
     train = space.sample(rng, n_train)
     t0 = time.perf_counter()
-    y = sim.final_window(train).astype(np.float32)
+    y = label_sim.final_window(train).astype(np.float32)
     data_s = time.perf_counter() - t0
-    plain = sim.stats.points / sim.stats.seconds
-    plain_transitions = sim.stats.transitions / sim.stats.seconds
     s = mbg.Surrogate(32, 256, hidden=512, hidden_layers=3, ensemble=4, seed=seed)
     t1 = time.perf_counter()
     loss = s.train(screen.encode(train), y, epochs=epochs, batch=batch, lr=1e-3, seed=seed)
     train_s = time.perf_counter() - t1
     held = space.sample(rng, 1000)
     y_held = sim.final_window(held, ids=np.arange(n_train, n_train + 1000))
+    cands = space.sample(rng, n_cand)
+    # the recall subsample (below) is simulated plainly here, before the screen: with the held-out
+    # points it times the plain method (11 000 points at n_traj trajectories)
+    sub = np.sort(rng.choice(n_cand, size=n_recall, replace=False))
+    y_sub_all = sim.final_window(cands[sub], ids=sub)
+    plain = sim.stats.points / sim.stats.seconds
+    plain_transitions = sim.stats.transitions / sim.stats.seconds
     p_held, spread_held = s.predict(screen.encode(held))
     tv_held = screen.total_variation(p_held, y_held)
     target = int(np.argmax(y.var(axis=0)))
@@ -305,14 +315,12 @@ def measure_surrogate(n_train=20000, n_traj=10000, n_cand=1_000_000, epochs=120,
             "spearman_spread_tv": float(np.corrcoef(np.argsort(np.argsort(spread_held)),
                                                     np.argsort(np.argsort(tv_held)))[0, 1])}
     threshold = 0.9
-    cands = space.sample(rng, n_cand)
     rep = screen.screen(s, sim, cands, target, threshold=threshold, spread_cut=spread_cut, plain_points_per_s=plain,
                         max_report=1000)
     # recall of the screening criterion: a random subsample of the candidates simulated plainly;
     # a true hit has simulated P(target) >= threshold; the screen finds it when its predicted
     # P(target) >= threshold (before the report cap)
-    sub = np.sort(rng.choice(n_cand, size=n_recall, replace=False))
-    y_sub = sim.final_window(cands[sub], ids=sub)[:, target]
+    y_sub = y_sub_all[:, target]
     score_sub, _ = s.predict_column(screen.encode(cands[sub]), target)
     true_hit = y_sub >= threshold
     found = score_sub >= threshold
@@ -354,7 +362,8 @@ def measure_surrogate(n_train=20000, n_traj=10000, n_cand=1_000_000, epochs=120,
         "resimulated": rep.resimulated, "uncertain": rep.uncertain, "candidates": rep.candidates,
         "uncertainty_gate": gate, "recall": recall,
         "predict_s": rep.predict_s, "resim_s": rep.resim_s, "train_s": train_s, "train_loss": loss,
-        "training_data_s": data_s, "tv_vs_1e5_trajectories": fine_ref, "gemm": gemm, "workload": SURROGATE_DESC}
+        "training_data_s": data_s, "label_trajectories": label_traj, "tv_vs_1e5_trajectories": fine_ref, "gemm": gemm,
+        "workload": SURROGATE_DESC}
 
 
 def measure_surrogate_gemm(rows=131072, reps=10):
