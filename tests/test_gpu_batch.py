@@ -161,6 +161,23 @@ def test_window_gather_equals_per_instance_reads():
         assert np.array_equal(arr[i], b2.probtraj(i)[0][-1])
 
 
+def test_warp_shapes_on_the_long_pilot():
+    """The autotuner re-times its closest shapes on a pilot four times longer; with the warp layout
+    forced those are warp shapes, whose per-warp shared-memory slices the long pilot's work
+    description carries too. The tuned batch gives the untuned one's results."""
+    net = synth.sweep_instance(2)
+    m = mbg.Model.from_strings(net.bnd(), net.cfg())
+    n = [160000, 160000]  # 320 000 trajectories: a long pilot beyond the 262 144 of the first one
+    tuned = mbg.Batch([m, m], n_traj=n, seeds=[1, 2], layout=mbg.LAYOUT_WARP, autotune=True).run()
+    k = tuned.classes()[0]
+    assert k["layout"] == "warp" and len(k["timings"]) >= 2
+    assert tuned.summary()["errors"] == 0
+    plain = mbg.Batch([m, m], n_traj=n, seeds=[1, 2], layout=mbg.LAYOUT_WARP).run()
+    for i in range(2):
+        assert np.array_equal(tuned.probtraj_raw(i)[0], plain.probtraj_raw(i)[0])
+        assert tuned.summary(i)["transitions"] == plain.summary(i)["transitions"]
+
+
 def test_batch_probabilities_are_normalised():
     net = synth.sweep_instance(1)
     m = mbg.Model.from_strings(net.bnd(), net.cfg())

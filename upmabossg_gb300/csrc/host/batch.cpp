@@ -334,7 +334,9 @@ void Batch::configure(int c, int lay, int blk, int variant) {
         sm = (size_t)(blk / 32) * slice;
         if (sm > kSmemLimit) throw ModelError("largest instance of a size class too large for the batched warp layout");
         ck(sim_warp_batch_configure(variant != 0, sm, blk, &bps), "batched warp kernel occupancy");
-        k.desc.slice_bytes = k.pilot.slice_bytes = slice;
+        // every work description a launch of this shape may run (the long pilot included: the
+        // autotuner re-times the closest shapes on it)
+        k.desc.slice_bytes = k.pilot.slice_bytes = k.pilot_long.slice_bytes = slice;
     }
     if (row_bytes) {
         if (bps < 1) throw CudaError("batched kernel cannot be resident with this block size");
