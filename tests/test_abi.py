@@ -110,3 +110,18 @@ def test_trajectory_limit_is_checked_before_any_device_work(has_gpu):
         with pytest.raises(mbg.MbgError) as e:
             mbg.Simulation(m, n_traj=1 << 30)
         assert e.value.status == 5
+
+
+def test_option_checks_come_before_any_device_work():
+    """Out-of-range options are argument errors whether or not a GPU is present: they are checked
+    before the library touches a device."""
+    net = synth.small()
+    m = mbg.Model.from_strings(net.bnd(), net.cfg())
+    for kw in (dict(lane_update=3), dict(layout=9), dict(block_size=48),
+               dict(layout=mbg.LAYOUT_LANE, redraw_period=99)):
+        with pytest.raises(mbg.MbgError) as e:
+            mbg.Simulation(m, n_traj=100, **kw)
+        assert e.value.status == 1, kw
+    with pytest.raises(mbg.MbgError) as e:
+        mbg.Batch([m], n_traj=[100], lane_variant=3)
+    assert e.value.status == 1 and "lane_variant" in e.value.message

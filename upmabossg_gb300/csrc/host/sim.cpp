@@ -339,6 +339,14 @@ void Sim::create(const CompiledModel& model, const std::vector<std::string>& nod
     seed = o.use_cfg_seed ? cm.seed : o.seed;
     check_model_limits(cm, n_traj);
     const uint64_t S = 1ull << cm.n_out;
+    // option checks come before any device call
+    if (o.block_size && (o.block_size % 32 != 0 || o.block_size > 256))
+        throw ArgError("block_size must be a multiple of 32, at most 256");
+    if (o.layout < MBG_LAYOUT_AUTO || o.layout > MBG_LAYOUT_LANE_GLOBAL) throw ArgError("unknown layout");
+    if (o.lane_update < 0 || o.lane_update > 2) throw ArgError("lane_update must be 0, 1 or 2");
+    if (o.layout == MBG_LAYOUT_THREAD && cm.words > 16) throw ModelError("thread layout supports at most 512 nodes");
+    if (o.redraw_period && (o.layout == MBG_LAYOUT_LANE || o.layout == MBG_LAYOUT_LANE_GLOBAL))
+        throw ArgError("redraw_period is supported by the thread and warp layouts");
 
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
@@ -370,8 +378,6 @@ void Sim::create(const CompiledModel& model, const std::vector<std::string>& nod
     lane_full = prm.has_palette || cm.max_k > 12;
     prm.max_steps = o.max_steps ? o.max_steps : 0xFFFFFFFFu;
     prm.redraw_period = o.redraw_period;
-    if (o.redraw_period && (o.layout == MBG_LAYOUT_LANE || o.layout == MBG_LAYOUT_LANE_GLOBAL))
-        throw ArgError("redraw_period is supported by the thread and warp layouts");
     prm.seed = seed;
     prm.n_traj = n_traj;
     prm.traj_base = o.traj_base;
@@ -403,11 +409,6 @@ void Sim::create(const CompiledModel& model, const std::vector<std::string>& nod
     ck(cudaEventCreate(&evk0), "cudaEventCreate");
     ck(cudaEventCreate(&evk1), "cudaEventCreate");
 
-    if (o.block_size && (o.block_size % 32 != 0 || o.block_size > 256))
-        throw ArgError("block_size must be a multiple of 32, at most 256");
-    if (o.layout < MBG_LAYOUT_AUTO || o.layout > MBG_LAYOUT_LANE_GLOBAL) throw ArgError("unknown layout");
-    if (o.lane_update < 0 || o.lane_update > 2) throw ArgError("lane_update must be 0, 1 or 2");
-    if (o.layout == MBG_LAYOUT_THREAD && cm.words > 16) throw ModelError("thread layout supports at most 512 nodes");
     if (o.layout != MBG_LAYOUT_AUTO) {
         int blk = o.block_size;
         if (blk <= 0) {
