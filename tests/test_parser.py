@@ -228,3 +228,24 @@ def test_random_expressions_tabulate_exactly(seed):
         for bits in itertools.product((0, 1), repeat=n):
             want = fd(bits) * fd(bits) / 2 + 0.125 if bits[i] else fu(bits) * fu(bits) + 0.25
             assert m.rate(i, bits)[1] == want, (i, bits)
+
+
+def test_compile_error_names_the_lowest_failing_node():
+    """Nodes are tabulated on several host threads once a model has 256 or more; when several fail,
+    the error is the one of the lowest-numbered node, as a single thread would have reported it."""
+    n = 400
+    names = [f"X{i}" for i in range(n)]
+    bad = (150, 280, 390)  # each reads 25 nodes, one over the limit of 24
+    lines = []
+    for i, nm in enumerate(names):
+        if i in bad:
+            regs = [names[(i + 1 + j) % n] for j in range(25)]
+            logic = " | ".join(regs)
+        else:
+            logic = f"!{names[(i + 1) % n]}"
+        lines.append(f"Node {nm} {{ logic = {logic}; rate_up = @logic ? 1 : 0; rate_down = @logic ? 0 : 1; }}\n")
+    cfg = "max_time = 5;\ntime_tick = 1;\nsample_count = 10;\n"
+    for _ in range(3):  # the same error whichever thread reaches a bad node first
+        with pytest.raises(mbg.MbgError) as e:
+            mbg.Model.from_strings("".join(lines), cfg)
+        assert "node X150 reads 25 nodes" in e.value.message, e.value.message
